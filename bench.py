@@ -1,0 +1,363 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the checkerboard Cellular Potts sweep on GB300.
+
+Metric: copy attempts per second (one attempt per lattice site per MCS).
+Default workload: the 4096x4096 2D tissue (Voronoi tiling at 100 sites per
+cell, 3 types, symmetric random J, area + perimeter constraints, T=20); one
+step is one 500-MCS run of it, continuing from the previous step's state.
+
+  value      device-resident throughput: the lattice and tables live in HBM;
+             each step is timed with CUDA events on the launching stream and
+             L2 is flushed (512 MB write) between steps, outside the events.
+  e2e        the same metric through the public API with host buffers: every
+             step pushes the pinned host lattice (H2D + table recount), runs
+             500 MCS and pulls the lattice back (D2H).
+  roofline   algorithmic bytes = 8 B per attempt (one int32 read and write of
+             every site per MCS) / mean sweep-launch time, against the
+             measured HBM copy bandwidth.
+  cpu_baseline  the C++ oracle (the same deterministic sweep) on the host
+             cores, on a bounded sample of the same lattice.
+
+--impl reference times the CPU oracle (the reference has no CPU sweep of its
+own; its CUDA build is timed separately) on all host threads, one MCS of the
+same lattice per step.
+
+Under torchrun (N>1) every rank runs its own independent replica of the
+workload (replicas only: the path has no data exchange between lattices);
+time is the max over ranks and value the attempts of all ranks / that time.
+"""
+import argparse
+import json
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = pathlib.Path(__file__).resolve().parent
+PKG = ROOT / "gpu-cpm_gb300"
+for _p in (str(ROOT), str(PKG)):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "copy-attempts/s"
+UNIT = "attempts/s"
+BYTES_PER_ATTEMPT = 8
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--workload", default="tissue_2d",
+                   choices=["tissue_2d", "tissue_2d_8192", "tissue_3d", "sorting_2d"])
+    p.add_argument("--mcs", type=int, default=None, help="MCS per step")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def build_workload(name):
+    from gpucpm import workloads as W
+    if name == "tissue_2d":
+        return W.tissue_2d()
+    if name == "tissue_2d_8192":
+        return W.tissue_2d(n=8192, mcs=100)
+    if name == "tissue_3d":
+        return W.tissue_3d()
+    if name == "sorting_2d":
+        return W.sorting_2d()
+    raise ValueError(name)
+
+
+def describe(w, mcs):
+    shape = "x".join(str(s) for s in w.lattice.shape[::-1])
+    return {"workload": f"{w.name} {shape}", "sites": w.nsites, "cells": w.ncells,
+            "types": int(w.J.shape[0]) - 1, "temperature": w.temperature,
+            "mcs_per_step": mcs, "neighbourhood": "moore8" if w.ndim == 2 else "moore26",
+            "l2": "flushed between steps (512 MB write, outside the timed events)",
+            "seed": 0}
+
+
+def measured_peak_hbm():
+    f = ROOT / "MEASURED_PEAKS.json"
+    try:
+        d = json.loads(f.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id):
+        self.gpu_id = gpu_id
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100", "-i", str(self.gpu_id)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def gpu_index_for(torch, dev):
+    """nvidia-smi id of a torch device (its UUID when torch exposes it)."""
+    try:
+        u = str(torch.cuda.get_device_properties(dev).uuid)
+        return u if u.startswith("GPU-") else "GPU-" + u
+    except Exception:
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+        return vis.split(",")[dev] if vis else dev
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def dist_max(world, value):
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64,
+                     device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def cpu_baseline(w, target_s=10.0, max_mcs=20):
+    """The C++ oracle on every host thread, on a bounded sample of `w`."""
+    import oracle
+    threads = os.cpu_count() or 1
+    sim = oracle.OracleSim(w.lattice, w.ncells, **w.oracle_kwargs(), seed=0)
+    t0 = time.perf_counter()
+    sim.run(1, nthreads=threads)
+    first = time.perf_counter() - t0
+    extra = max(0, min(max_mcs - 1, int(target_s / max(first, 1e-3)) - 1))
+    t1 = time.perf_counter()
+    if extra:
+        sim.run(extra, nthreads=threads)
+    total = first + (time.perf_counter() - t1)
+    mcs = 1 + extra
+    return {"value": w.nsites * mcs / total, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{mcs} MCS of the {'x'.join(map(str, w.lattice.shape[::-1]))} "
+                      f"{w.name} lattice from its seeded initial state ({total:.1f} s)"}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    import oracle
+    w = build_workload(args.workload)
+    threads = os.cpu_count() or 1
+    sim = oracle.OracleSim(w.lattice, w.ncells, **w.oracle_kwargs(), seed=0)
+    for _ in range(args.warmup):
+        sim.run(1, nthreads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sim.run(1, nthreads=threads)
+    dt = time.perf_counter() - t0
+    value = w.nsites * args.steps / dt
+    cfg = describe(w, 1)
+    cfg["l2"] = "n/a (host CPU)"
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32+f32",
+            "data": "synthetic (seeded Voronoi tissue)", "config": cfg,
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"1 MCS of the {w.name} lattice per step, "
+                                       f"{threads} OpenMP threads; the reference has no "
+                                       "CPU implementation, so this is the oracle port"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def traffic_per_attempt(workload):
+    """DRAM bytes per attempt of the sweep from the committed ncu summary."""
+    f = ROOT / "profiles" / "traffic.json"
+    try:
+        d = json.loads(f.read_text())
+        return float(d[workload]["dram_bytes_per_attempt"])
+    except Exception:
+        return None
+
+
+def run_ours(args, world, rank, local):
+    import numpy as np
+    import torch
+
+    import gpucpm
+
+    torch.cuda.set_device(local)
+    gpucpm.set_device(local)
+    w = build_workload(args.workload)
+    mcs = args.mcs or w.mcs
+    n = w.lattice.shape[0]
+    sim = gpucpm.Cpm(n, w.ndim, w.ncells, w.temperature, False)
+    sim.get_state()[...] = w.lattice.view(np.int32)
+    w.apply(sim)
+    sim.set_seed(0, rank)
+    stream = torch.cuda.Stream()
+    sim.set_stream(stream.cuda_stream)
+    sim.push_to_gpu()
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+
+    for _ in range(args.warmup):
+        sim.run_mcs(mcs)
+    sim.synchronize()
+    torch.cuda.synchronize()
+
+    sampler = ClockSampler(gpu_index_for(torch, local)) if rank == 0 else None
+    if sampler:
+        sampler.start()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    launches0 = sim.kernel_launches()
+    dist_barrier(world)
+    torch.cuda.synchronize()
+    wall0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            flush.fill_(i & 0xFF)
+            starts[i].record(stream)
+            sim.run_mcs(mcs)
+            ends[i].record(stream)
+    sim.synchronize()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    dist_barrier(world)
+    launches = sim.kernel_launches() - launches0
+    clocks = sampler.stop() if sampler else None
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    dev_s = sum(step_ms) / 1e3
+    dev_s_max = dist_max(world, dev_s)
+    attempts_total = w.nsites * mcs * args.steps * world
+    value = attempts_total / dev_s_max
+    ms_per_step = dev_s_max / args.steps * 1e3
+
+    # End to end through the public API with host buffers.
+    e2e = None
+    if not args.no_e2e:
+        e2e_steps = max(1, min(args.steps, 5))
+        sim.set_stream(None)
+        sim.push_to_gpu()
+        sim.run_mcs(mcs)
+        sim.synchronize()
+        sim.pull_from_gpu()
+        dist_barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            sim.push_to_gpu()
+            sim.run_mcs(mcs)
+            sim.synchronize()
+            sim.pull_from_gpu()
+        e2e_s = dist_max(world, time.perf_counter() - t0)
+        e2e = {"value": w.nsites * mcs * e2e_steps * world / e2e_s, "unit": UNIT,
+               "h2d_bytes_per_step": 4 * w.nsites, "d2h_bytes_per_step": 4 * w.nsites + 4,
+               "steps": e2e_steps, "path": "Cpm.push_to_gpu + run + synchronize + pull_from_gpu"}
+
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peak_hbm()
+    per_launch_s = dev_s / args.steps
+    attempts_per_launch = w.nsites * mcs
+    achieved = BYTES_PER_ATTEMPT * attempts_per_launch / per_launch_s / 1e9
+    tpa = traffic_per_attempt(args.workload)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": f"{peak_kind} HBM copy (burst)",
+                "traffic": tpa * attempts_per_launch if tpa is not None else None,
+                "algorithmic_bytes_per_launch": BYTES_PER_ATTEMPT * attempts_per_launch,
+                "kernel": "sweep_kernel (one cooperative launch per step)"}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u32+f32", "data": "synthetic (seeded Voronoi tissue)",
+            "config": describe(w, mcs), "roofline": roofline, "e2e": e2e,
+            "gpu_launches": int(launches), "clocks": clocks,
+            "mcs_per_s": value / w.nsites / world,
+            "wall_s": wall, "step_ms": step_ms}
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(w)
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

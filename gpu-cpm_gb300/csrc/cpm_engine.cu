@@ -1,0 +1,737 @@
+// cpm_engine.cu — host runtime of the GB300 Cellular Potts engine and the
+// C-ABI of include/gpucpm.h.
+//
+// Replaces the reference's host class Cpm (src/cpm.h:78-151, src/cpm.cu):
+// allocation (src/cpm.cu:176-261), parameter setters (:57-158), addCell
+// (:160-174), the launch schedule of run() (:291-517), host<->device copies
+// (:531-597) and centroid readback (:68-110).  Differences by design:
+//   * one CUDA stream per handle instead of the legacy default stream;
+//   * one cooperative persistent launch per run() covers every MCS, slot and
+//     replica (the reference relaunches per inner_iterations and grid-syncs
+//     per attempt);
+//   * parameters live in per-replica device blocks uploaded once per run
+//     when changed (the reference re-uploads its __constant__ struct in every
+//     setter, src/kernels.cu:50-53);
+//   * every call returns a status and keeps a message (the reference prints
+//     CUDA errors and carries on, src/cpm.cu:52-56).
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/gpucpm.h"
+#include "cpm_internal.h"
+
+using namespace gpucpm;
+
+namespace {
+
+thread_local std::string g_create_error;
+
+constexpr int kMaxMcsPerLaunch = 1 << 16;
+
+}  // namespace
+
+struct cpm_handle {
+  int ndim = 2;
+  int nrep = 0;
+  int device = 0;
+  std::vector<DevReplica> reps;
+  std::vector<DevParams> params;
+  bool params_dirty = true;
+  long long total_sites = 0;
+  long long rows = 0;
+
+  uint32_t* h_lat = nullptr;  // pinned, all replicas back to back
+  uint32_t* d_lat = nullptr;
+  int2* d_ap = nullptr;
+  long long* d_cs = nullptr;
+  int2* d_dap = nullptr;
+  long long* d_dcs = nullptr;
+  uint32_t* d_dflag = nullptr;
+  uint32_t* d_dlist = nullptr;
+  uint32_t* d_ctl = nullptr;
+  unsigned long long* d_counters = nullptr;
+  unsigned long long* d_first = nullptr;
+  int* d_ctype = nullptr;
+  DevReplica* d_reps = nullptr;
+  DevParams* d_params = nullptr;
+  int* d_task_prefix = nullptr;
+
+  cudaStream_t stream = nullptr;      // stream work is enqueued on
+  cudaStream_t own_stream = nullptr;  // created with the handle
+  int grid = 1;
+  std::vector<int> task_prefix;  // [27][nrep + 1]
+  std::vector<int> active_slots;
+  std::vector<unsigned long long> attempts;  // per replica, host-counted
+
+  uint64_t seed = 0;
+  uint32_t stream_id = 0;
+  uint64_t tick = 0;
+  bool pushed = false;
+  int added_cells = 0;
+  uint64_t launches = 0;
+  std::string err;
+
+  int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    err = buf;
+    return code;
+  }
+  int cuda_fail(cudaError_t e, const char* what) {
+    return fail(CPM_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+  }
+};
+
+namespace {
+
+#define CPM_CUDA(h, call)                                   \
+  do {                                                      \
+    cudaError_t e_ = (call);                                \
+    if (e_ != cudaSuccess) return (h)->cuda_fail(e_, #call); \
+  } while (0)
+
+// Entry points that touch the GPU make the handle's device current first:
+// the library carries its own CUDA runtime, whose current device is not the
+// one a caller (torch, another library) selected.
+#define CPM_BIND(h)                                   \
+  do {                                                \
+    if (!(h)) return CPM_ERR_INVALID;                 \
+    CPM_CUDA((h), cudaSetDevice((h)->device));        \
+  } while (0)
+
+int class_count_h(int n, int c) {
+  if (n == 1) return c == 0 ? 1 : 0;
+  return c < 2 ? (n >> 1) : (n & 1);
+}
+
+void free_all(cpm_handle* h) {
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  cudaFreeHost(h->h_lat);
+  cudaFree(h->d_lat);
+  cudaFree(h->d_ap);
+  cudaFree(h->d_cs);
+  cudaFree(h->d_dap);
+  cudaFree(h->d_dcs);
+  cudaFree(h->d_dflag);
+  cudaFree(h->d_dlist);
+  cudaFree(h->d_ctl);
+  cudaFree(h->d_counters);
+  cudaFree(h->d_first);
+  cudaFree(h->d_ctype);
+  cudaFree(h->d_reps);
+  cudaFree(h->d_params);
+  cudaFree(h->d_task_prefix);
+  if (h->own_stream) cudaStreamDestroy(h->own_stream);
+}
+
+void default_params(DevParams& p, float T) {
+  std::memset(&p, 0, sizeof p);
+  p.temperature = T;
+}
+
+bool perim_on(const DevParams& p) {
+  for (int k = 0; k < kMaxTypes; ++k)
+    if (p.lam_perim[k] != 0.0f) return true;
+  return false;
+}
+
+int build_engine(int n, int ndim, const int* nx, const int* ny, const int* nz,
+                 const int* ncells, float T, cpm_handle** out) {
+  if (!out) {
+    g_create_error = "out pointer is NULL";
+    return CPM_ERR_INVALID;
+  }
+  *out = nullptr;
+  if (n < 1 || (ndim != 2 && ndim != 3)) {
+    g_create_error = "need n >= 1 replicas and dimensionality 2 or 3";
+    return CPM_ERR_INVALID;
+  }
+  cpm_handle* h = new (std::nothrow) cpm_handle();
+  if (!h) {
+    g_create_error = "host allocation failed";
+    return CPM_ERR_ALLOC;
+  }
+  h->ndim = ndim;
+  h->nrep = n;
+  long long sites = 0, rows = 0;
+  for (int r = 0; r < n; ++r) {
+    DevReplica R;
+    R.nx = nx[r];
+    R.ny = ny[r];
+    R.nz = ndim == 3 ? nz[r] : 1;
+    R.ncells = ncells[r];
+    if (R.nx < 3 || R.ny < 3 || (ndim == 3 && R.nz < 3)) {
+      g_create_error = "every side must be at least 3";
+      delete h;
+      return CPM_ERR_INVALID;
+    }
+    if (ndim == 2 && nz && nz[r] != 1) {
+      g_create_error = "nz must be 1 for a 2D lattice";
+      delete h;
+      return CPM_ERR_INVALID;
+    }
+    const long long ns = (long long)R.nx * R.ny * R.nz;
+    if (ns >= (1LL << 31)) {
+      g_create_error = "a replica may hold at most 2^31-1 sites";
+      delete h;
+      return CPM_ERR_INVALID;
+    }
+    if (R.ncells < 0 || R.ncells > 0xFFFFFF) {
+      g_create_error = "number_of_cells must be in [0, 2^24-1]";
+      delete h;
+      return CPM_ERR_INVALID;
+    }
+    R.lat_off = sites;
+    R.cell_off = rows;
+    sites += ns;
+    rows += (long long)R.ncells + 1;
+    h->reps.push_back(R);
+  }
+  if (rows >= (1LL << 31)) {
+    g_create_error = "too many cells in total (table rows >= 2^31)";
+    delete h;
+    return CPM_ERR_INVALID;
+  }
+  h->total_sites = sites;
+  h->rows = rows;
+  h->params.resize(n);
+  for (auto& p : h->params) default_params(p, T);
+  h->attempts.assign(n, 0);
+
+  cudaError_t e = cudaGetDevice(&h->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
+  h->stream = h->own_stream;
+  auto al = [&](void** p, size_t bytes) {
+    if (e == cudaSuccess) e = cudaMalloc(p, bytes ? bytes : 1);
+  };
+  al((void**)&h->d_lat, sizeof(uint32_t) * sites);
+  al((void**)&h->d_ap, sizeof(int2) * rows);
+  al((void**)&h->d_cs, sizeof(long long) * rows * ndim);
+  al((void**)&h->d_dap, sizeof(int2) * rows);
+  al((void**)&h->d_dcs, sizeof(long long) * rows * ndim);
+  al((void**)&h->d_dflag, sizeof(uint32_t) * rows);
+  al((void**)&h->d_dlist, sizeof(uint32_t) * rows * 2);
+  al((void**)&h->d_ctl, sizeof(uint32_t) * kCtlWords);
+  al((void**)&h->d_counters, sizeof(unsigned long long) * 2 * n);
+  al((void**)&h->d_first, sizeof(unsigned long long) * rows);
+  al((void**)&h->d_ctype, sizeof(int) * rows);
+  al((void**)&h->d_reps, sizeof(DevReplica) * n);
+  al((void**)&h->d_params, sizeof(DevParams) * n);
+  al((void**)&h->d_task_prefix, sizeof(int) * 27 * (n + 1));
+  if (e == cudaSuccess) e = cudaMallocHost((void**)&h->h_lat, sizeof(uint32_t) * (sites ? sites : 1));
+  if (e != cudaSuccess) {
+    g_create_error = std::string("device/pinned allocation failed: ") + cudaGetErrorString(e);
+    free_all(h);
+    delete h;
+    return e == cudaErrorMemoryAllocation ? CPM_ERR_ALLOC : CPM_ERR_CUDA;
+  }
+  std::memset(h->h_lat, 0, sizeof(uint32_t) * sites);
+
+  // Block tasks per slot and replica (prefix over replicas).
+  h->task_prefix.assign(27 * (n + 1), 0);
+  long long max_tasks = 1;
+  for (int slot = 0; slot < 27; ++slot) {
+    const int cx = slot % 3, cy = (slot / 3) % 3, cz = slot / 9;
+    long long acc = 0;
+    for (int r = 0; r < n; ++r) {
+      h->task_prefix[slot * (n + 1) + r] = (int)acc;
+      const DevReplica& R = h->reps[r];
+      if (ndim == 2 && cz != 0) continue;
+      const long long ncx = class_count_h(R.nx, cx), ncy = class_count_h(R.ny, cy),
+                      ncz = class_count_h(R.nz, cz);
+      const long long segs = ncy * ncz * ((ncx + 31) / 32);
+      acc += (segs + kWarpsPerBlock - 1) / kWarpsPerBlock;
+    }
+    if (acc >= (1LL << 31)) {
+      g_create_error = "batch too large for one launch";
+      free_all(h);
+      delete h;
+      return CPM_ERR_INVALID;
+    }
+    h->task_prefix[slot * (n + 1) + n] = (int)acc;
+    if (acc > 0) h->active_slots.push_back(slot);
+    max_tasks = std::max(max_tasks, acc);
+  }
+
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+  int per_sm = sweep_max_blocks_per_sm(ndim, true);
+  per_sm = std::min(per_sm, sweep_max_blocks_per_sm(ndim, false));
+  if (per_sm < 1 || sms < 1) {
+    g_create_error = "cannot place the sweep kernel on this device";
+    free_all(h);
+    delete h;
+    return CPM_ERR_CUDA;
+  }
+  h->grid = (int)std::min<long long>((long long)per_sm * sms, max_tasks);
+  h->grid = std::max(h->grid, 1);
+
+  e = cudaMemcpyAsync(h->d_reps, h->reps.data(), sizeof(DevReplica) * n,
+                      cudaMemcpyHostToDevice, h->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(h->d_task_prefix, h->task_prefix.data(),
+                        sizeof(int) * h->task_prefix.size(),
+                        cudaMemcpyHostToDevice, h->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(h->d_ctl, 0, sizeof(uint32_t) * kCtlWords, h->stream);
+  if (e == cudaSuccess)
+    e = cudaMemsetAsync(h->d_counters, 0, sizeof(unsigned long long) * 2 * n, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) {
+    g_create_error = std::string("initial upload failed: ") + cudaGetErrorString(e);
+    free_all(h);
+    delete h;
+    return CPM_ERR_CUDA;
+  }
+  *out = h;
+  return CPM_OK;
+}
+
+int check_replica(cpm_handle* h, int r) {
+  if (!h) return CPM_ERR_INVALID;
+  if (r < 0 || r >= h->nrep)
+    return h->fail(CPM_ERR_INVALID, "replica %d out of range [0, %d)", r, h->nrep);
+  return CPM_OK;
+}
+
+int check_type(cpm_handle* h, int t) {
+  if (t < 0 || t >= kMaxTypes)
+    return h->fail(CPM_ERR_INVALID, "cell type %d out of range [0, %d)", t, kMaxTypes);
+  return CPM_OK;
+}
+
+template <class F>
+int for_replicas(cpm_handle* h, int r, F&& f) {
+  if (!h) return CPM_ERR_INVALID;
+  if (r == -1) {
+    for (auto& p : h->params) f(p);
+  } else {
+    if (int rc = check_replica(h, r)) return rc;
+    f(h->params[r]);
+  }
+  h->params_dirty = true;
+  return CPM_OK;
+}
+
+int set_temperature(cpm_handle* h, int r, float T) {
+  if (!h) return CPM_ERR_INVALID;
+  if (!std::isfinite(T)) return h->fail(CPM_ERR_INVALID, "temperature must be finite");
+  return for_replicas(h, r, [&](DevParams& p) { p.temperature = T; });
+}
+
+int set_area(cpm_handle* h, int r, int type, int target, float lambda) {
+  if (!h) return CPM_ERR_INVALID;
+  if (int rc = check_type(h, type)) return rc;
+  return for_replicas(h, r, [&](DevParams& p) {
+    p.tgt_area[type] = target;
+    p.lam_area[type] = lambda;
+  });
+}
+
+int set_perimeter(cpm_handle* h, int r, int type, int target, float lambda) {
+  if (!h) return CPM_ERR_INVALID;
+  if (int rc = check_type(h, type)) return rc;
+  return for_replicas(h, r, [&](DevParams& p) {
+    p.tgt_perim[type] = target;
+    p.lam_perim[type] = lambda;
+    p.perim_on = perim_on(p) ? 1 : 0;
+  });
+}
+
+int set_adhesion(cpm_handle* h, int r, int type, int other, float J, int sym) {
+  if (!h) return CPM_ERR_INVALID;
+  if (int rc = check_type(h, type)) return rc;
+  if (int rc = check_type(h, other)) return rc;
+  return for_replicas(h, r, [&](DevParams& p) {
+    p.J[type * kMaxTypes + other] = J;
+    if (sym) p.J[other * kMaxTypes + type] = J;
+  });
+}
+
+int read_error_word(cpm_handle* h, uint32_t* word) {
+  CPM_CUDA(h, cudaMemcpyAsync(word, h->d_ctl + kCtlErr, sizeof(uint32_t),
+                              cudaMemcpyDeviceToHost, h->stream));
+  CPM_CUDA(h, cudaStreamSynchronize(h->stream));
+  return CPM_OK;
+}
+
+std::string describe_errors(uint32_t w) {
+  std::string s;
+  auto add = [&](const char* m) {
+    if (!s.empty()) s += "; ";
+    s += m;
+  };
+  if (w & kErrBadId) add("a site holds an id above number_of_cells");
+  if (w & kErrBadType) add("a site holds a type >= 32");
+  if (w & kErrMediumType) add("a site holds id 0 with a non-zero type");
+  if (w & kErrTypeConflict) add("one cell id appears with two different types");
+  if (w & kErrTimeout) add("a grid barrier of the sweep timed out");
+  return s;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cpm_create(int dimension, int dimensionality, int number_of_cells,
+               float temperature, int flags, cpm_handle** out) {
+  if (flags != 0) {
+    g_create_error = "flags must be 0 (field / act lattices are not supported)";
+    if (out) *out = nullptr;
+    return CPM_ERR_UNSUPPORTED;
+  }
+  const int nz = dimensionality == 3 ? dimension : 1;
+  return build_engine(1, dimensionality, &dimension, &dimension, &nz,
+                      &number_of_cells, temperature, out);
+}
+
+int cpm_create_box(int nx, int ny, int nz, int dimensionality,
+                   int number_of_cells, float temperature, cpm_handle** out) {
+  return build_engine(1, dimensionality, &nx, &ny, &nz, &number_of_cells,
+                      temperature, out);
+}
+
+int cpm_create_batch(int n, int dimensionality, const int* nx, const int* ny,
+                     const int* nz, const int* ncells, cpm_handle** out) {
+  if (!nx || !ny || !ncells || (dimensionality == 3 && !nz)) {
+    g_create_error = "nx, ny, ncells (and nz in 3D) must be non-NULL";
+    if (out) *out = nullptr;
+    return CPM_ERR_INVALID;
+  }
+  return build_engine(n, dimensionality, nx, ny, nz, ncells, 1.0f, out);
+}
+
+int cpm_destroy(cpm_handle* h) {
+  if (!h) return CPM_OK;
+  cudaSetDevice(h->device);
+  free_all(h);
+  delete h;
+  return CPM_OK;
+}
+
+int cpm_set_device(int device) {
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) {
+    g_create_error = std::string("cudaSetDevice failed: ") + cudaGetErrorString(e);
+    return CPM_ERR_CUDA;
+  }
+  return CPM_OK;
+}
+
+const char* cpm_last_error(const cpm_handle* h) {
+  return h ? h->err.c_str() : g_create_error.c_str();
+}
+
+int cpm_set_temperature(cpm_handle* h, float T) { return set_temperature(h, -1, T); }
+int cpm_set_temperature_r(cpm_handle* h, int r, float T) { return set_temperature(h, r < 0 ? -2 : r, T); }
+int cpm_set_area(cpm_handle* h, int type, int target, float lambda) {
+  return set_area(h, -1, type, target, lambda);
+}
+int cpm_set_area_r(cpm_handle* h, int r, int type, int target, float lambda) {
+  return set_area(h, r < 0 ? -2 : r, type, target, lambda);
+}
+int cpm_set_perimeter(cpm_handle* h, int type, int target, float lambda) {
+  return set_perimeter(h, -1, type, target, lambda);
+}
+int cpm_set_perimeter_r(cpm_handle* h, int r, int type, int target, float lambda) {
+  return set_perimeter(h, r < 0 ? -2 : r, type, target, lambda);
+}
+int cpm_set_adhesion(cpm_handle* h, int type, int other, float J, int symmetric) {
+  return set_adhesion(h, -1, type, other, J, symmetric);
+}
+int cpm_set_adhesion_r(cpm_handle* h, int r, int type, int other, float J, int symmetric) {
+  return set_adhesion(h, r < 0 ? -2 : r, type, other, J, symmetric);
+}
+
+int cpm_add_cell(cpm_handle* h, int type, int x, int y, int z) {
+  if (!h) return CPM_ERR_INVALID;
+  if (int rc = check_type(h, type)) return rc;
+  const DevReplica& R = h->reps[0];
+  if (h->ndim == 2) z = 0;
+  if (x < 0 || x >= R.nx || y < 0 || y >= R.ny || z < 0 || z >= R.nz)
+    return h->fail(CPM_ERR_INVALID, "add_cell position (%d, %d, %d) outside the lattice", x, y, z);
+  if (h->added_cells >= R.ncells)
+    return h->fail(CPM_ERR_INVALID, "add_cell would exceed number_of_cells = %d", R.ncells);
+  h->added_cells += 1;
+  h->h_lat[R.lat_off + ((long long)z * R.ny + y) * R.nx + x] =
+      (uint32_t)h->added_cells | ((uint32_t)type << 24);
+  return CPM_OK;
+}
+
+int cpm_host_lattice_r(cpm_handle* h, int r, uint32_t** ptr, int64_t* nsites) {
+  if (int rc = check_replica(h, r)) return rc;
+  const DevReplica& R = h->reps[r];
+  if (ptr) *ptr = h->h_lat + R.lat_off;
+  if (nsites) *nsites = (int64_t)R.nx * R.ny * R.nz;
+  return CPM_OK;
+}
+int cpm_host_lattice(cpm_handle* h, uint32_t** ptr, int64_t* nsites) {
+  return cpm_host_lattice_r(h, 0, ptr, nsites);
+}
+
+int cpm_device_lattice_r(cpm_handle* h, int r, uint32_t** dptr) {
+  if (int rc = check_replica(h, r)) return rc;
+  if (dptr) *dptr = h->d_lat + h->reps[r].lat_off;
+  return CPM_OK;
+}
+
+int cpm_push(cpm_handle* h) {
+  CPM_BIND(h);
+  h->pushed = false;
+  CPM_CUDA(h, cudaMemcpyAsync(h->d_lat, h->h_lat, sizeof(uint32_t) * h->total_sites,
+                              cudaMemcpyHostToDevice, h->stream));
+  CPM_CUDA(h, cudaMemsetAsync(h->d_ap, 0, sizeof(int2) * h->rows, h->stream));
+  CPM_CUDA(h, cudaMemsetAsync(h->d_cs, 0, sizeof(long long) * h->rows * h->ndim, h->stream));
+  CPM_CUDA(h, cudaMemsetAsync(h->d_dap, 0, sizeof(int2) * h->rows, h->stream));
+  CPM_CUDA(h, cudaMemsetAsync(h->d_dcs, 0, sizeof(long long) * h->rows * h->ndim, h->stream));
+  CPM_CUDA(h, cudaMemsetAsync(h->d_dflag, 0, sizeof(uint32_t) * h->rows, h->stream));
+  CPM_CUDA(h, cudaMemsetAsync(h->d_first, 0xFF, sizeof(unsigned long long) * h->rows, h->stream));
+  CPM_CUDA(h, cudaMemsetAsync(h->d_ctype, 0xFF, sizeof(int) * h->rows, h->stream));
+  CPM_CUDA(h, cudaMemsetAsync(h->d_ctl, 0, sizeof(uint32_t) * kCtlWords, h->stream));
+  CPM_CUDA(h, launch_init(h->ndim, h->d_lat, h->d_reps, h->nrep, h->total_sites,
+                          h->d_ap, h->d_cs, h->d_first, h->d_ctype, h->d_ctl,
+                          h->stream));
+  h->launches += 2;
+  uint32_t w = 0;
+  if (int rc = read_error_word(h, &w)) return rc;
+  if (w) {
+    CPM_CUDA(h, cudaMemsetAsync(h->d_ctl, 0, sizeof(uint32_t) * kCtlWords, h->stream));
+    return h->fail(CPM_ERR_INVALID, "push_to_gpu rejected the lattice: %s",
+                   describe_errors(w).c_str());
+  }
+  h->pushed = true;
+  return CPM_OK;
+}
+
+int cpm_pull(cpm_handle* h) {
+  CPM_BIND(h);
+  CPM_CUDA(h, cudaMemcpyAsync(h->h_lat, h->d_lat, sizeof(uint32_t) * h->total_sites,
+                              cudaMemcpyDeviceToHost, h->stream));
+  CPM_CUDA(h, cudaStreamSynchronize(h->stream));
+  return CPM_OK;
+}
+
+int cpm_run(cpm_handle* h, int mcs) {
+  CPM_BIND(h);
+  if (mcs < 0) return h->fail(CPM_ERR_INVALID, "mcs must be >= 0");
+  if (!h->pushed) return h->fail(CPM_ERR_STATE, "run() before a successful push_to_gpu()");
+  if (mcs == 0) return CPM_OK;
+  if (h->params_dirty) {
+    for (auto& p : h->params) p.perim_on = perim_on(p) ? 1 : 0;
+    CPM_CUDA(h, cudaMemcpyAsync(h->d_params, h->params.data(),
+                                sizeof(DevParams) * h->nrep,
+                                cudaMemcpyHostToDevice, h->stream));
+    h->params_dirty = false;
+  }
+  bool any_perim = false;
+  for (auto& p : h->params) any_perim |= p.perim_on != 0;
+
+  SweepArgs a;
+  std::memset(&a, 0, sizeof a);
+  a.lat = h->d_lat;
+  a.ap = h->d_ap;
+  a.cs = h->d_cs;
+  a.dap = h->d_dap;
+  a.dcs = h->d_dcs;
+  a.dflag = h->d_dflag;
+  a.dlist = h->d_dlist;
+  a.ctl = h->d_ctl;
+  a.counters = h->d_counters;
+  a.reps = h->d_reps;
+  a.params = h->d_params;
+  a.task_prefix = h->d_task_prefix;
+  a.rows = h->rows;
+  a.seed = h->seed;
+  a.nrep = h->nrep;
+  a.stream0 = h->stream_id;
+  a.nslot_active = (int)h->active_slots.size();
+  for (int i = 0; i < a.nslot_active; ++i) a.slots[i] = h->active_slots[i];
+
+  int left = mcs;
+  while (left > 0) {
+    const int chunk = std::min(left, kMaxMcsPerLaunch);
+    a.tick0 = h->tick;
+    a.mcs = chunk;
+    // Barrier counter and both dirty counts start at zero in every launch;
+    // the sticky error word is left alone until cpm_synchronize reads it.
+    CPM_CUDA(h, cudaMemsetAsync(h->d_ctl, 0, sizeof(uint32_t) * kCtlErr, h->stream));
+    CPM_CUDA(h, launch_sweep(h->ndim, any_perim, a, h->grid, h->stream));
+    h->launches += 1;
+    h->tick += (uint64_t)chunk;
+    left -= chunk;
+  }
+  for (int r = 0; r < h->nrep; ++r) {
+    const DevReplica& R = h->reps[r];
+    h->attempts[r] += (unsigned long long)R.nx * R.ny * R.nz * (unsigned long long)mcs;
+  }
+  return CPM_OK;
+}
+
+int cpm_synchronize(cpm_handle* h) {
+  CPM_BIND(h);
+  uint32_t w = 0;
+  if (int rc = read_error_word(h, &w)) return rc;
+  if (w) {
+    CPM_CUDA(h, cudaMemsetAsync(h->d_ctl + kCtlErr, 0, sizeof(uint32_t), h->stream));
+    CPM_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->pushed = false;  // the lattice and tables may disagree now
+    return h->fail((w & kErrTimeout) ? CPM_ERR_TIMEOUT : CPM_ERR_INVALID,
+                   "sweep failed: %s", describe_errors(w).c_str());
+  }
+  return CPM_OK;
+}
+
+int cpm_set_stream(cpm_handle* h, void* stream) {
+  CPM_BIND(h);
+  cudaStream_t next = stream ? (cudaStream_t)stream : h->own_stream;
+  if (next != h->stream) {
+    // Work already queued on the old stream must finish before the new one
+    // touches the same buffers.
+    CPM_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->stream = next;
+  }
+  return CPM_OK;
+}
+
+int cpm_set_seed(cpm_handle* h, uint64_t seed, uint32_t stream_id) {
+  if (!h) return CPM_ERR_INVALID;
+  h->seed = seed;
+  h->stream_id = stream_id;
+  return CPM_OK;
+}
+
+int cpm_get_tick(const cpm_handle* h, uint64_t* tick) {
+  if (!h || !tick) return CPM_ERR_INVALID;
+  *tick = h->tick;
+  return CPM_OK;
+}
+
+int cpm_set_tick(cpm_handle* h, uint64_t tick) {
+  if (!h) return CPM_ERR_INVALID;
+  h->tick = tick;
+  return CPM_OK;
+}
+
+int cpm_get_tables_r(cpm_handle* h, int r, int32_t* area, int32_t* perimeter,
+                     int64_t* centroid_sums) {
+  if (int rc = check_replica(h, r)) return rc;
+  CPM_BIND(h);
+  const DevReplica& R = h->reps[r];
+  const long long n1 = (long long)R.ncells + 1;
+  if (area || perimeter) {
+    std::vector<int2> ap(n1);
+    CPM_CUDA(h, cudaMemcpyAsync(ap.data(), h->d_ap + R.cell_off, sizeof(int2) * n1,
+                                cudaMemcpyDeviceToHost, h->stream));
+    CPM_CUDA(h, cudaStreamSynchronize(h->stream));
+    for (long long c = 0; c < n1; ++c) {
+      if (area) area[c] = ap[c].x;
+      if (perimeter) perimeter[c] = ap[c].y;
+    }
+  }
+  if (centroid_sums) {
+    CPM_CUDA(h, cudaMemcpyAsync(centroid_sums, h->d_cs + R.cell_off * h->ndim,
+                                sizeof(long long) * n1 * h->ndim,
+                                cudaMemcpyDeviceToHost, h->stream));
+    CPM_CUDA(h, cudaStreamSynchronize(h->stream));
+  }
+  return CPM_OK;
+}
+
+int cpm_get_centroids(cpm_handle* h, double* out, int capacity, int* n_out) {
+  CPM_BIND(h);
+  const int n = h->added_cells;
+  if (n_out) *n_out = n;
+  if (!out || capacity <= 0 || n == 0) return CPM_OK;
+  const DevReplica& R = h->reps[0];
+  const int d = h->ndim;
+  const int m = std::min(n, capacity);
+  std::vector<int2> ap(m);
+  std::vector<long long> cs((size_t)m * d);
+  CPM_CUDA(h, cudaMemcpyAsync(ap.data(), h->d_ap + R.cell_off + 1, sizeof(int2) * m,
+                              cudaMemcpyDeviceToHost, h->stream));
+  CPM_CUDA(h, cudaMemcpyAsync(cs.data(), h->d_cs + (R.cell_off + 1) * d,
+                              sizeof(long long) * m * d, cudaMemcpyDeviceToHost, h->stream));
+  CPM_CUDA(h, cudaStreamSynchronize(h->stream));
+  const int dims[3] = {R.nx, R.ny, R.nz};
+  for (int c = 0; c < m; ++c)
+    for (int k = 0; k < d; ++k) {
+      double v = (double)cs[(size_t)c * d + k] / (double)ap[c].x;
+      if (std::isfinite(v)) v -= dims[k] * std::floor(v / dims[k]);
+      out[(size_t)c * d + k] = v;
+    }
+  return CPM_OK;
+}
+
+int cpm_get_counters_r(cpm_handle* h, int r, cpm_counters* out) {
+  if (!out || !h) return CPM_ERR_INVALID;
+  if (r < -1 || r >= h->nrep)
+    return h->fail(CPM_ERR_INVALID, "replica %d out of range", r);
+  CPM_BIND(h);
+  std::vector<unsigned long long> c(2 * h->nrep);
+  CPM_CUDA(h, cudaMemcpyAsync(c.data(), h->d_counters, sizeof(unsigned long long) * 2 * h->nrep,
+                              cudaMemcpyDeviceToHost, h->stream));
+  CPM_CUDA(h, cudaStreamSynchronize(h->stream));
+  out->attempts = out->evaluated = out->accepted = 0;
+  for (int q = 0; q < h->nrep; ++q) {
+    if (r >= 0 && q != r) continue;
+    out->attempts += h->attempts[q];
+    out->evaluated += c[2 * q];
+    out->accepted += c[2 * q + 1];
+  }
+  return CPM_OK;
+}
+
+int cpm_get_counters(cpm_handle* h, cpm_counters* out) {
+  return cpm_get_counters_r(h, -1, out);
+}
+
+int cpm_reset_counters(cpm_handle* h) {
+  CPM_BIND(h);
+  CPM_CUDA(h, cudaMemsetAsync(h->d_counters, 0, sizeof(unsigned long long) * 2 * h->nrep,
+                              h->stream));
+  std::fill(h->attempts.begin(), h->attempts.end(), 0ull);
+  return CPM_OK;
+}
+
+int cpm_info(const cpm_handle* h, int* n_replicas, int* dimensionality,
+             int* sweep_grid, uint64_t* kernel_launches) {
+  if (!h) return CPM_ERR_INVALID;
+  if (n_replicas) *n_replicas = h->nrep;
+  if (dimensionality) *dimensionality = h->ndim;
+  if (sweep_grid) *sweep_grid = h->grid;
+  if (kernel_launches) *kernel_launches = h->launches;
+  return CPM_OK;
+}
+
+int cpm_debug_barrier_timeout(uint64_t timeout_ns, int* status) {
+  if (!status) return CPM_ERR_INVALID;
+  *status = 0;
+  uint32_t* ctl = nullptr;
+  cudaStream_t s = nullptr;
+  cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&ctl, sizeof(uint32_t) * kCtlWords);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ctl, 0, sizeof(uint32_t) * kCtlWords, s);
+  if (e == cudaSuccess) e = launch_barrier_probe(ctl, timeout_ns, s);
+  uint32_t w = 0;
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&w, ctl + kCtlErr, sizeof w, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(ctl);
+  if (s) cudaStreamDestroy(s);
+  if (e != cudaSuccess) {
+    g_create_error = std::string("barrier probe failed: ") + cudaGetErrorString(e);
+    return CPM_ERR_CUDA;
+  }
+  *status = (w & kErrTimeout) ? CPM_ERR_TIMEOUT : CPM_OK;
+  return CPM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,422 @@
+"""gpucpm — drop-in replacement for shabaz/gpu-cpm's Python module, on GB300.
+
+`gpucpm.Cpm` keeps the reference's constructor and method set
+(src/python_wrapper.cpp:365-380): set_constraints, add_cell, push_to_gpu,
+run, synchronize, pull_from_gpu, get_state, get_centroids, get_act_state and
+get_field.  Every call goes through the C-ABI of libgpucpm_gb300.so
+(include/gpucpm.h); there is no CPU fallback — importing this module on a
+machine without the built library raises ImportError, and a CUDA failure
+raises CpmError.
+
+Differences from the reference, all deliberate:
+  * errors raise CpmError instead of printing and continuing
+    (src/cpm.cu:52-56) or returning False (src/python_wrapper.cpp:87,138,217);
+  * adhesion and temperature accept floats (the reference parses int);
+  * set_adhesion_symmetric is honoured (the reference parses an int into a
+    double that stays non-zero, so it always sets both entries,
+    src/python_wrapper.cpp:81-86);
+  * runs are reproducible: the random stream is keyed by a seed (default 0,
+    see set_seed) instead of std::random_device (src/cpm.cu:347-350);
+  * get_state's array keeps its Cpm alive (the reference's view dangles
+    once the object is freed).
+The act, chemotaxis, persistence, fixed and stickiness terms are not part of
+this engine: setting them raises CpmError, and get_act_state / get_field
+return zero arrays of the reference's shapes.
+"""
+import ctypes
+import os
+import pathlib
+
+import numpy as np
+
+_HERE = pathlib.Path(__file__).resolve().parent
+LIB_PATH = _HERE.parent / "libgpucpm_gb300.so"
+
+CPM_OK = 0
+CPM_ERR_INVALID = 1
+CPM_ERR_CUDA = 2
+CPM_ERR_ALLOC = 3
+CPM_ERR_STATE = 4
+CPM_ERR_TIMEOUT = 5
+CPM_ERR_UNSUPPORTED = 6
+MAX_TYPES = 32
+
+
+class CpmError(RuntimeError):
+    """A libgpucpm_gb300 call returned a non-zero status."""
+
+    def __init__(self, code, message):
+        super().__init__(f"[status {code}] {message}")
+        self.code = code
+
+
+class _Counters(ctypes.Structure):
+    _fields_ = [("attempts", ctypes.c_uint64), ("evaluated", ctypes.c_uint64),
+                ("accepted", ctypes.c_uint64)]
+
+
+_lib = None
+
+
+def library():
+    """The loaded C-ABI library (ctypes.CDLL); raises ImportError if absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = os.environ.get("GPUCPM_LIB", str(LIB_PATH))
+    if not os.path.exists(path):
+        raise ImportError(
+            f"libgpucpm_gb300.so not found at {path}; build it with "
+            "`python gpu-cpm_gb300/build.py` (no CPU fallback exists)")
+    L = ctypes.CDLL(path)
+    H = ctypes.c_void_p
+    ip = ctypes.POINTER(ctypes.c_int)
+    sig = {
+        "cpm_create": [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                       ctypes.c_int, ctypes.POINTER(H)],
+        "cpm_create_box": [ctypes.c_int] * 5 + [ctypes.c_float, ctypes.POINTER(H)],
+        "cpm_create_batch": [ctypes.c_int, ctypes.c_int, ip, ip, ip, ip,
+                             ctypes.POINTER(H)],
+        "cpm_destroy": [H],
+        "cpm_set_temperature": [H, ctypes.c_float],
+        "cpm_set_temperature_r": [H, ctypes.c_int, ctypes.c_float],
+        "cpm_set_area": [H, ctypes.c_int, ctypes.c_int, ctypes.c_float],
+        "cpm_set_area_r": [H, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float],
+        "cpm_set_perimeter": [H, ctypes.c_int, ctypes.c_int, ctypes.c_float],
+        "cpm_set_perimeter_r": [H, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                ctypes.c_float],
+        "cpm_set_adhesion": [H, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_int],
+        "cpm_set_adhesion_r": [H, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                               ctypes.c_float, ctypes.c_int],
+        "cpm_add_cell": [H, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int],
+        "cpm_host_lattice": [H, ctypes.POINTER(ctypes.c_void_p),
+                             ctypes.POINTER(ctypes.c_int64)],
+        "cpm_host_lattice_r": [H, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p),
+                               ctypes.POINTER(ctypes.c_int64)],
+        "cpm_device_lattice_r": [H, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)],
+        "cpm_push": [H],
+        "cpm_pull": [H],
+        "cpm_run": [H, ctypes.c_int],
+        "cpm_synchronize": [H],
+        "cpm_set_stream": [H, ctypes.c_void_p],
+        "cpm_set_seed": [H, ctypes.c_uint64, ctypes.c_uint32],
+        "cpm_get_tick": [H, ctypes.POINTER(ctypes.c_uint64)],
+        "cpm_set_tick": [H, ctypes.c_uint64],
+        "cpm_get_centroids": [H, ctypes.c_void_p, ctypes.c_int, ip],
+        "cpm_get_tables_r": [H, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                             ctypes.c_void_p],
+        "cpm_get_counters": [H, ctypes.POINTER(_Counters)],
+        "cpm_get_counters_r": [H, ctypes.c_int, ctypes.POINTER(_Counters)],
+        "cpm_reset_counters": [H],
+        "cpm_info": [H, ip, ip, ip, ctypes.POINTER(ctypes.c_uint64)],
+    }
+    for name, args in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = ctypes.c_int
+    L.cpm_set_device.argtypes = [ctypes.c_int]
+    L.cpm_set_device.restype = ctypes.c_int
+    L.cpm_debug_barrier_timeout.argtypes = [ctypes.c_uint64, ip]
+    L.cpm_debug_barrier_timeout.restype = ctypes.c_int
+    L.cpm_last_error.argtypes = [H]
+    L.cpm_last_error.restype = ctypes.c_char_p
+    _lib = L
+    return L
+
+
+def _check(rc, handle=None):
+    if rc != CPM_OK:
+        msg = library().cpm_last_error(handle)
+        raise CpmError(rc, msg.decode() if msg else "unknown error")
+
+
+def _int_array(values):
+    a = (ctypes.c_int * len(values))(*[int(v) for v in values])
+    return a
+
+
+class _Engine:
+    """Owner of one C handle (a single lattice or a batch of replicas)."""
+
+    def __init__(self, handle):
+        self._h = handle
+        self._lib = library()
+        n, d, g = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _check(self._lib.cpm_info(self._h, ctypes.byref(n), ctypes.byref(d),
+                                  ctypes.byref(g), None), self._h)
+        self.n_replicas, self.dimensionality, self.sweep_grid = n.value, d.value, g.value
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            self._lib.cpm_destroy(h)
+            self._h = None
+
+    def _call(self, name, *args):
+        _check(getattr(self._lib, name)(self._h, *args), self._h)
+
+    # -- shared helpers ---------------------------------------------------
+    def _host_view(self, replica, shape):
+        ptr, n = ctypes.c_void_p(), ctypes.c_int64()
+        self._call("cpm_host_lattice_r", int(replica), ctypes.byref(ptr),
+                   ctypes.byref(n))
+        buf = (ctypes.c_int32 * n.value).from_address(ptr.value)
+        buf._owner = self  # the array keeps this engine (and its memory) alive
+        return np.ctypeslib.as_array(buf).reshape(shape)
+
+    def device_lattice_ptr(self, replica=0):
+        """Device address of a replica's lattice (uint32, row-major)."""
+        p = ctypes.c_void_p()
+        self._call("cpm_device_lattice_r", int(replica), ctypes.byref(p))
+        return p.value
+
+    def set_stream(self, stream):
+        """Enqueue work on a caller-owned CUDA stream (a cudaStream_t as int,
+        e.g. torch.cuda.Stream().cuda_stream); None restores the own stream."""
+        self._call("cpm_set_stream", ctypes.c_void_p(int(stream) if stream else None))
+
+    def set_seed(self, seed, stream_id=0):
+        """Key of the Philox stream; replica r of a batch uses stream_id + r."""
+        self._call("cpm_set_seed", ctypes.c_uint64(int(seed)), ctypes.c_uint32(int(stream_id)))
+
+    @property
+    def tick(self):
+        t = ctypes.c_uint64()
+        self._call("cpm_get_tick", ctypes.byref(t))
+        return t.value
+
+    @tick.setter
+    def tick(self, value):
+        self._call("cpm_set_tick", ctypes.c_uint64(int(value)))
+
+    def tables(self, replica=0):
+        """(area, perimeter, centroid_sums) of every id 0..number_of_cells."""
+        n1 = self._ncells(replica) + 1
+        area = np.empty(n1, np.int32)
+        perim = np.empty(n1, np.int32)
+        cs = np.empty((n1, self.dimensionality), np.int64)
+        self._call("cpm_get_tables_r", int(replica), area.ctypes.data,
+                   perim.ctypes.data, cs.ctypes.data)
+        return area, perim, cs
+
+    def counters(self, replica=None):
+        """dict(attempts, evaluated, accepted) since the last reset."""
+        c = _Counters()
+        if replica is None:
+            self._call("cpm_get_counters", ctypes.byref(c))
+        else:
+            self._call("cpm_get_counters_r", int(replica), ctypes.byref(c))
+        return {"attempts": c.attempts, "evaluated": c.evaluated, "accepted": c.accepted}
+
+    def reset_counters(self):
+        self._call("cpm_reset_counters")
+
+    def kernel_launches(self):
+        k = ctypes.c_uint64()
+        self._call("cpm_info", None, None, None, ctypes.byref(k))
+        return k.value
+
+    def push_to_gpu(self):
+        self._call("cpm_push")
+
+    def pull_from_gpu(self):
+        self._call("cpm_pull")
+
+    def synchronize(self):
+        self._call("cpm_synchronize")
+
+    def run_mcs(self, mcs):
+        """Enqueue `mcs` Monte Carlo steps (asynchronous)."""
+        self._call("cpm_run", int(mcs))
+
+
+class Cpm(_Engine):
+    """Cellular Potts simulation on one lattice (reference: gpucpm.Cpm).
+
+    Cpm(dimension, dimensionality, number_of_cells, temperature, has_field,
+        history=1, has_act=1) — the argument order of PyCpm_init
+    (src/python_wrapper.cpp:27-41).  has_field / has_act select lattices of
+    terms this engine does not model; their getters return zeros.
+    """
+
+    def __init__(self, dimension, dimensionality, number_of_cells, temperature,
+                 has_field=False, history=1, has_act=1):
+        lib = library()
+        h = ctypes.c_void_p()
+        _check(lib.cpm_create(int(dimension), int(dimensionality),
+                              int(number_of_cells), float(temperature), 0,
+                              ctypes.byref(h)), None)
+        super().__init__(h)
+        self.dimension = int(dimension)
+        self.number_of_cells = int(number_of_cells)
+        self.has_field = bool(has_field)
+        self.has_act = bool(has_act)
+        self._shape = (self.dimension,) * self.dimensionality
+
+    def _ncells(self, replica):
+        return self.number_of_cells
+
+    def set_constraints(self, cell_type, *, other_cell_type=-1,
+                        lambda_perimeter=-1, target_perimeter=-1,
+                        lambda_area=-1, target_area=-1, lambda_act=-1,
+                        max_act=-1, adhesion=-1, fixed=-1,
+                        lambda_chemotaxis=-1, lambda_persistence=-1,
+                        persistence_diffusion=-1, persistence_time=-1,
+                        set_adhesion_symmetric=1, stickiness=-1):
+        """Set per-type Hamiltonian parameters (src/python_wrapper.cpp:55-129).
+
+        A group is applied only when all of its fields differ from -1, as in
+        the reference.  Groups of terms outside this engine raise CpmError.
+        """
+        ct = int(cell_type)
+        unsupported = []
+        if fixed not in (-1, 0):
+            unsupported.append("fixed")
+        if lambda_chemotaxis != -1:
+            unsupported.append("lambda_chemotaxis")
+        if (lambda_persistence != -1 and persistence_diffusion != -1
+                and persistence_time != -1):
+            unsupported.append("persistence")
+        if lambda_act != -1 and max_act != -1:
+            unsupported.append("act")
+        if other_cell_type != -1 and stickiness != -1:
+            unsupported.append("stickiness")
+        if unsupported:
+            raise CpmError(CPM_ERR_UNSUPPORTED,
+                           "terms not modelled by this engine: " + ", ".join(unsupported))
+        if lambda_perimeter != -1 and target_perimeter != -1:
+            self._call("cpm_set_perimeter", ct, int(target_perimeter), float(lambda_perimeter))
+        if lambda_area != -1 and target_area != -1:
+            self._call("cpm_set_area", ct, int(target_area), float(lambda_area))
+        if other_cell_type != -1 and adhesion != -1:
+            self._call("cpm_set_adhesion", ct, int(other_cell_type), float(adhesion),
+                       1 if set_adhesion_symmetric else 0)
+
+    def set_temperature(self, temperature):
+        self._call("cpm_set_temperature", float(temperature))
+
+    def add_cell(self, type, x, y, z=-1):  # noqa: A002 - reference's keyword
+        """Seed the next cell id of `type` at one site (src/cpm.cu:160-174)."""
+        if self.dimensionality == 3 and z == -1:
+            raise CpmError(CPM_ERR_INVALID, "add_cell needs z on a 3D lattice")
+        self._call("cpm_add_cell", int(type), int(x), int(y), int(z if z != -1 else 0))
+
+    def run(self, cell_sync, block_sync, global_sync, threads_per_block,
+            positions_per_thread, positions_per_checkerboard,
+            updates_per_checkerboard_switch, updates_per_barrier, iterations,
+            inner_iterations, shared=0, partial_dispatch=0,
+            centroid_tracking=0):
+        """Run (iterations // inner_iterations) * inner_iterations MCS.
+
+        Same arguments as the reference (src/python_wrapper.cpp:182-227).
+        The launch-geometry, synchronisation and dispatch knobs have no
+        meaning for this engine's schedule and are accepted for
+        compatibility.  Asynchronous, like the reference's 2D run.
+        """
+        for name, v in (("cell_sync", cell_sync), ("block_sync", block_sync),
+                        ("global_sync", global_sync),
+                        ("threads_per_block", threads_per_block),
+                        ("positions_per_thread", positions_per_thread),
+                        ("positions_per_checkerboard", positions_per_checkerboard),
+                        ("updates_per_checkerboard_switch", updates_per_checkerboard_switch),
+                        ("updates_per_barrier", updates_per_barrier),
+                        ("iterations", iterations), ("inner_iterations", inner_iterations)):
+            if not isinstance(v, (int, np.integer)) or isinstance(v, bool):
+                raise TypeError(f"{name} must be an int")
+        inner = int(inner_iterations)
+        if inner <= 0:
+            raise CpmError(CPM_ERR_INVALID, "inner_iterations must be positive")
+        total = (int(iterations) // inner) * inner
+        if total > 0:
+            self.run_mcs(total)
+
+    def get_state(self):
+        """Writable int32 view of the host lattice, shape (D, D[, D]),
+        indexed [y, x] / [z, y, x]; values are id | type << 24."""
+        return self._host_view(0, self._shape)
+
+    def get_centroids(self):
+        """(n, d) float64 mean coordinates of the cells made by add_cell."""
+        n = ctypes.c_int()
+        self._call("cpm_get_centroids", None, 0, ctypes.byref(n))
+        out = np.empty((n.value, self.dimensionality), np.float64)
+        if n.value:
+            self._call("cpm_get_centroids", out.ctypes.data, n.value, ctypes.byref(n))
+        return out
+
+    def get_act_state(self):
+        return np.zeros(self._shape, np.int32)
+
+    def get_field(self):
+        return np.zeros((self.dimensionality,) + self._shape, np.float64)
+
+
+class Batch(_Engine):
+    """Many independent replicas advanced by one persistent launch.
+
+    sizes: list of (nx, ny) in 2D or (nx, ny, nz) in 3D; ncells: list of
+    cell counts.  Parameters are set per replica with the *_r setters.
+    """
+
+    def __init__(self, dimensionality, sizes, ncells):
+        lib = library()
+        n = len(sizes)
+        if n == 0 or len(ncells) != n:
+            raise CpmError(CPM_ERR_INVALID, "sizes and ncells must have equal, non-zero length")
+        nx = _int_array([s[0] for s in sizes])
+        ny = _int_array([s[1] for s in sizes])
+        nz = _int_array([s[2] if dimensionality == 3 else 1 for s in sizes])
+        nc = _int_array(ncells)
+        h = ctypes.c_void_p()
+        _check(lib.cpm_create_batch(n, int(dimensionality), nx, ny, nz, nc,
+                                    ctypes.byref(h)), None)
+        super().__init__(h)
+        self.sizes = [tuple(int(v) for v in s) for s in sizes]
+        self.ncells = [int(c) for c in ncells]
+
+    def _ncells(self, replica):
+        return self.ncells[replica]
+
+    def lattice(self, replica):
+        """Writable host view of one replica's lattice ([y, x] / [z, y, x])."""
+        return self._host_view(replica, tuple(reversed(self.sizes[replica])))
+
+    def set_temperature(self, replica, temperature):
+        self._call("cpm_set_temperature_r", int(replica), float(temperature))
+
+    def set_area(self, replica, cell_type, target, lam):
+        self._call("cpm_set_area_r", int(replica), int(cell_type), int(target), float(lam))
+
+    def set_perimeter(self, replica, cell_type, target, lam):
+        self._call("cpm_set_perimeter_r", int(replica), int(cell_type), int(target), float(lam))
+
+    def set_adhesion(self, replica, cell_type, other, J, symmetric=True):
+        self._call("cpm_set_adhesion_r", int(replica), int(cell_type), int(other), float(J),
+                   1 if symmetric else 0)
+
+
+def set_device(device):
+    """CUDA device that engines created later by this thread live on."""
+    _check(library().cpm_set_device(int(device)), None)
+
+
+def barrier_timeout_selftest(timeout_ns=50_000_000):
+    """Status produced by a grid barrier that can never complete (expects
+    CPM_ERR_TIMEOUT after about timeout_ns); the CUDA context stays usable."""
+    st = ctypes.c_int()
+    _check(library().cpm_debug_barrier_timeout(int(timeout_ns), ctypes.byref(st)), None)
+    return st.value
+
+
+def create_box(nx, ny, nz, dimensionality, number_of_cells, temperature):
+    """A single lattice of any box shape (nz = 1 in 2D), as a Batch of one."""
+    lib = library()
+    h = ctypes.c_void_p()
+    _check(lib.cpm_create_box(int(nx), int(ny), int(nz), int(dimensionality),
+                              int(number_of_cells), float(temperature),
+                              ctypes.byref(h)), None)
+    b = Batch.__new__(Batch)
+    _Engine.__init__(b, h)
+    b.sizes = [(int(nx), int(ny)) if dimensionality == 2 else (int(nx), int(ny), int(nz))]
+    b.ncells = [int(number_of_cells)]
+    return b

@@ -1,0 +1,212 @@
+/*
+ * gpucpm.h — C-ABI of the GB300 Cellular Potts engine (libgpucpm_gb300.so).
+ *
+ * The reference (shabaz/gpu-cpm) has no C-ABI: its boundary is the CPython
+ * type `gpucpm.Cpm` (src/python_wrapper.cpp) wrapping the C++ class `Cpm`
+ * (src/cpm.h:78-151, src/cpm.cu).  Every entry point below replaces one
+ * method of that type / class; the citation names the reference code it
+ * stands in for.  The Python module `gpucpm` shipped with this library binds
+ * these symbols with ctypes and reproduces the reference's method set.
+ *
+ * Conventions
+ *   - Plain C types only.  Every function returns an int status (CPM_OK = 0).
+ *   - A handle is single-threaded: callers serialise calls on one handle.
+ *   - Lattice sites hold `id | (type << 24)` (src/cpm.cu:163,171); id 0 with
+ *     type 0 is the medium.  Layout is row-major: index = (z*ny + y)*nx + x.
+ *   - Work is enqueued on the handle's own CUDA stream; cpm_run() returns
+ *     before the sweep finishes (as Cpm::run does for 2D, src/cpm.cu:291).
+ *     cpm_synchronize() waits and reports any device-side error.
+ */
+#ifndef GPUCPM_H_
+#define GPUCPM_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define CPM_OK 0
+#define CPM_ERR_INVALID 1     /* bad argument or bad lattice contents      */
+#define CPM_ERR_CUDA 2        /* a CUDA runtime call failed                 */
+#define CPM_ERR_ALLOC 3       /* host or device allocation failed          */
+#define CPM_ERR_STATE 4       /* call out of order (e.g. run before push)  */
+#define CPM_ERR_TIMEOUT 5     /* a bounded grid barrier gave up            */
+#define CPM_ERR_UNSUPPORTED 6 /* feature outside this engine's scope       */
+
+/* Largest number of cell types with parameters (the reference has 20,
+ * src/settings.h:4; this engine accepts up to 32). */
+#define CPM_MAX_TYPES 32
+
+typedef struct cpm_handle cpm_handle;
+
+/* Counters of one run, summed over all replicas (see cpm_get_counters). */
+typedef struct {
+    uint64_t attempts;  /* copy attempts made (one per site per MCS)       */
+    uint64_t evaluated; /* attempts whose source id differs from target's  */
+    uint64_t accepted;  /* attempts that copied the source id              */
+} cpm_counters;
+
+/* ---- lifetime --------------------------------------------------------- */
+
+/* Replaces Cpm::Cpm (src/cpm.cu:176-261) as reached through PyCpm_init
+ * (src/python_wrapper.cpp:27-41).  Argument order follows the Python
+ * constructor (dimension, dimensionality, number_of_cells, temperature).
+ * `flags` is reserved (has_field / has_act are out-of-scope terms) and must
+ * be 0.  Allocates the device lattice and the cell tables for ids
+ * 0..number_of_cells on the current CUDA device. */
+int cpm_create(int dimension, int dimensionality, int number_of_cells,
+               float temperature, int flags, cpm_handle** out);
+
+/* Same as cpm_create for a non-cubic box nx*ny(*nz); nz must be 1 in 2D.
+ * No counterpart in the reference (square/cubic only, src/cpm.cu:182-184). */
+int cpm_create_box(int nx, int ny, int nz, int dimensionality,
+                   int number_of_cells, float temperature, cpm_handle** out);
+
+/* Batched engine: `n` independent replicas (2D or 3D) with their own box
+ * sizes, cell counts and parameters, advanced together by one persistent
+ * launch.  nx/ny/nz/ncells are arrays of length n.  Replica r is addressed
+ * with the *_r entry points below.  No counterpart in the reference. */
+int cpm_create_batch(int n, int dimensionality, const int* nx, const int* ny,
+                     const int* nz, const int* ncells, cpm_handle** out);
+
+/* Replaces Cpm::~Cpm (src/cpm.cu:263-285). */
+int cpm_destroy(cpm_handle* h);
+
+/* Select the CUDA device later cpm_create* calls of this thread allocate
+ * on (the reference always uses device 0, src/cpm.cu:366).  A handle keeps
+ * the device it was created on for all its later calls. */
+int cpm_set_device(int device);
+
+/* Human-readable description of the last error on this handle (or of the
+ * last failed cpm_create* when h is NULL).  Never returns NULL. */
+const char* cpm_last_error(const cpm_handle* h);
+
+/* ---- parameters (src/cpm.cu:57-158, kwargs of PyCpm_setConstraints,
+ *      src/python_wrapper.cpp:55-129).  Applied to every replica; the *_r
+ *      forms address one replica of a batch. ----------------------------- */
+
+/* Replaces Cpm::setTemperature (src/cpm.cu:57-60).  The reference stores an
+ * int (src/settings.h:30); this engine uses float. */
+int cpm_set_temperature(cpm_handle* h, float temperature);
+int cpm_set_temperature_r(cpm_handle* h, int replica, float temperature);
+
+/* Replaces Cpm::setArea (src/cpm.cu:125-129). */
+int cpm_set_area(cpm_handle* h, int type, int target, float lambda);
+int cpm_set_area_r(cpm_handle* h, int replica, int type, int target,
+                   float lambda);
+
+/* Replaces Cpm::setPerimeter (src/cpm.cu:119-123). */
+int cpm_set_perimeter(cpm_handle* h, int type, int target, float lambda);
+int cpm_set_perimeter_r(cpm_handle* h, int replica, int type, int target,
+                        float lambda);
+
+/* Replaces Cpm::setAdhesion (src/cpm.cu:137-143).  J is float here (the
+ * reference stores short, src/settings.h:20).  symmetric != 0 also sets
+ * J[other][type]. */
+int cpm_set_adhesion(cpm_handle* h, int type, int other, float J,
+                     int symmetric);
+int cpm_set_adhesion_r(cpm_handle* h, int replica, int type, int other,
+                       float J, int symmetric);
+
+/* ---- lattice ---------------------------------------------------------- */
+
+/* Replaces Cpm::addCell (src/cpm.cu:160-174): the next id (1, 2, ...) of
+ * `type` is written at (x, y[, z]) of the host lattice.  z is ignored in 2D.
+ * Cells added this way are the ones cpm_get_centroids reports. */
+int cpm_add_cell(cpm_handle* h, int type, int x, int y, int z);
+
+/* Replaces Cpm::getCellIds (src/cpm.cu:519-521) behind get_state
+ * (src/python_wrapper.cpp:292-308): the host lattice buffer of replica 0
+ * (pinned memory owned by the handle; valid until cpm_destroy). */
+int cpm_host_lattice(cpm_handle* h, uint32_t** ptr, int64_t* nsites);
+int cpm_host_lattice_r(cpm_handle* h, int replica, uint32_t** ptr,
+                       int64_t* nsites);
+
+/* Device lattice of a replica (row-major uint32), for zero-copy readers. */
+int cpm_device_lattice_r(cpm_handle* h, int replica, uint32_t** dptr);
+
+/* Replaces Cpm::moveCellIdsToGpu (src/cpm.cu:541-597): copies every host
+ * lattice to the device and recomputes area, perimeter and centroid sums of
+ * every cell.  Fails with CPM_ERR_INVALID (and leaves the tables unusable)
+ * if a site holds an id above number_of_cells, a type >= CPM_MAX_TYPES, a
+ * non-zero type on id 0, or one id with two types.  Synchronous. */
+int cpm_push(cpm_handle* h);
+
+/* Replaces Cpm::retreiveCellIdsFromGpu (src/cpm.cu:531-540): copies every
+ * device lattice back into the host buffers.  Synchronous. */
+int cpm_pull(cpm_handle* h);
+
+/* ---- sweeps ----------------------------------------------------------- */
+
+/* Replaces Cpm::run (src/cpm.cu:291-517): `mcs` Monte Carlo steps of the
+ * checkerboard Metropolis sweep on every replica.  One MCS makes one copy
+ * attempt per lattice site.  Asynchronous; the launch geometry knobs of the
+ * reference's run() have no meaning here (the engine sizes its own grid). */
+int cpm_run(cpm_handle* h, int mcs);
+
+/* Replaces Cpm::synchronize (src/cpm.cu:653-655).  Waits for the handle's
+ * stream and reports device-side errors (CPM_ERR_TIMEOUT, CPM_ERR_CUDA). */
+int cpm_synchronize(cpm_handle* h);
+
+/* Enqueue the handle's work on `stream` (a cudaStream_t of the same device,
+ * owned by the caller, e.g. a torch.cuda.Stream) instead of its own stream;
+ * NULL switches back to the handle's own stream.  The reference always uses
+ * the legacy default stream. */
+int cpm_set_stream(cpm_handle* h, void* stream);
+
+/* Random stream: the sweep draws Philox4x32-10 numbers keyed by `seed` with
+ * counter (site, phase, stream_id).  Replica r of a batch uses stream
+ * stream_id + r.  Default seed 0, stream 0.  (The reference reseeds from
+ * std::random_device on every run, src/cpm.cu:347-350.) */
+int cpm_set_seed(cpm_handle* h, uint64_t seed, uint32_t stream_id);
+
+/* Monte Carlo time: number of MCS run since creation (Cpm::_mcs,
+ * src/cpm.cu:484).  Together with the lattice and the seed it is a complete
+ * resume point. */
+int cpm_get_tick(const cpm_handle* h, uint64_t* tick);
+int cpm_set_tick(cpm_handle* h, uint64_t tick);
+
+/* ---- readback --------------------------------------------------------- */
+
+/* Replaces Cpm::get2dCentroids / get3dCentroids (src/cpm.cu:68-110): mean
+ * coordinate of cells 1..n_added (the cells made by cpm_add_cell) of replica
+ * 0, `dimensionality` doubles per cell, each in [0, side).  `out` holds
+ * `capacity` cells; *n_out receives n_added.  Synchronous. */
+int cpm_get_centroids(cpm_handle* h, double* out, int capacity, int* n_out);
+
+/* Cell tables of one replica for ids 0..number_of_cells: area, perimeter
+ * (number of (site, Moore neighbour) pairs with the site in the cell and the
+ * neighbour not), and the exact int64 coordinate sums, `dimensionality` per
+ * cell (periodic images chosen nearest the cell's running mean).  Any
+ * pointer may be NULL.  Synchronous.  No counterpart in the reference. */
+int cpm_get_tables_r(cpm_handle* h, int replica, int32_t* area,
+                     int32_t* perimeter, int64_t* centroid_sums);
+
+/* Attempt / evaluation / acceptance counts accumulated since the last
+ * cpm_reset_counters (summed over replicas, or of one replica). */
+int cpm_get_counters(cpm_handle* h, cpm_counters* out);
+int cpm_get_counters_r(cpm_handle* h, int replica, cpm_counters* out);
+int cpm_reset_counters(cpm_handle* h);
+
+/* Engine information: number of replicas, dimensionality, CUDA grid size of
+ * the sweep launch, and the number of kernel launches enqueued so far. */
+int cpm_info(const cpm_handle* h, int* n_replicas, int* dimensionality,
+             int* sweep_grid, uint64_t* kernel_launches);
+
+/* ---- diagnostics ------------------------------------------------------ */
+
+/* Failure-detection self-test: launches a two-block cooperative kernel whose
+ * grid barrier can never complete and whose wait limit is `timeout_ns`, and
+ * stores in *status the status that limit produced (CPM_ERR_TIMEOUT when the
+ * bounded wait ran out, as it must).  Touches no engine state.  No
+ * counterpart in the reference, whose grid.sync() waits without a limit
+ * (src/kernels2d.cu:175,193). */
+int cpm_debug_barrier_timeout(uint64_t timeout_ns, int* status);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GPUCPM_H_ */

@@ -1,0 +1,141 @@
+"""CPU oracle of the checkerboard Cellular Potts sweep.
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, never by the product.  See cpm_oracle.cpp for
+the algorithm, its reference citations and its parity status (bit-level
+parity with the reference is unpinned by golden vectors; the reference has
+none and is nondeterministic).
+"""
+import ctypes
+
+import numpy as np
+
+from .build import LIB_PATH, build
+
+MAX_TYPES = 32
+
+
+class Params(ctypes.Structure):
+    _fields_ = [
+        ("ndim", ctypes.c_int), ("nx", ctypes.c_int), ("ny", ctypes.c_int),
+        ("nz", ctypes.c_int), ("ncells", ctypes.c_int),
+        ("J", ctypes.c_float * (MAX_TYPES * MAX_TYPES)),
+        ("lam_area", ctypes.c_float * MAX_TYPES),
+        ("tgt_area", ctypes.c_int * MAX_TYPES),
+        ("lam_perim", ctypes.c_float * MAX_TYPES),
+        ("tgt_perim", ctypes.c_int * MAX_TYPES),
+        ("temperature", ctypes.c_float),
+        ("seed", ctypes.c_uint64),
+        ("stream", ctypes.c_uint32),
+    ]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = build()
+        l = ctypes.CDLL(str(path))
+        u32p = ctypes.POINTER(ctypes.c_uint32)
+        l.orc_philox4x32_10.argtypes = [u32p, u32p, u32p]
+        l.orc_exp_neg.argtypes = [ctypes.c_float]
+        l.orc_exp_neg.restype = ctypes.c_float
+        l.orc_init_tables.argtypes = [ctypes.POINTER(Params), ctypes.c_void_p,
+                                      ctypes.c_void_p, ctypes.c_void_p,
+                                      ctypes.c_void_p]
+        l.orc_run.argtypes = [ctypes.POINTER(Params), ctypes.c_void_p,
+                              ctypes.c_void_p, ctypes.c_void_p,
+                              ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int,
+                              ctypes.c_int, ctypes.c_void_p]
+        _lib = l
+    return _lib
+
+
+def philox4x32_10(ctr, key):
+    c = (ctypes.c_uint32 * 4)(*ctr)
+    k = (ctypes.c_uint32 * 2)(*key)
+    o = (ctypes.c_uint32 * 4)()
+    lib().orc_philox4x32_10(c, k, o)
+    return [int(v) for v in o]
+
+
+def exp_neg(x: float) -> float:
+    return float(lib().orc_exp_neg(float(x)))
+
+
+class OracleSim:
+    """One lattice plus its cell tables, advanced by the CPU oracle.
+
+    `lattice` is a uint32 array of shape (ny, nx) or (nz, ny, nx) holding
+    id | type << 24.  Parameters follow the engine's conventions: J[a][b] is
+    the adhesion seen by a site of type a next to a site of type b.
+    """
+
+    def __init__(self, lattice, ncells, J, lam_area, tgt_area,
+                 lam_perim=None, tgt_perim=None, temperature=1.0, seed=0,
+                 stream=0):
+        lat = np.ascontiguousarray(lattice, dtype=np.uint32).copy()
+        self.ndim = lat.ndim
+        self.lattice = lat
+        self.ncells = int(ncells)
+        p = Params()
+        p.ndim = self.ndim
+        if self.ndim == 2:
+            p.nz, (p.ny, p.nx) = 1, lat.shape
+        else:
+            p.nz, p.ny, p.nx = lat.shape
+        p.ncells = self.ncells
+        Jm = np.zeros((MAX_TYPES, MAX_TYPES), np.float32)
+        Jin = np.asarray(J, np.float32)
+        Jm[:Jin.shape[0], :Jin.shape[1]] = Jin
+        p.J[:] = Jm.ravel().tolist()
+
+        def fill(dst, src, dt):
+            arr = np.zeros(MAX_TYPES, dt)
+            if src is not None:
+                s = np.asarray(src, dt).ravel()
+                arr[:s.size] = s
+            dst[:] = arr.tolist()
+        fill(p.lam_area, lam_area, np.float32)
+        fill(p.tgt_area, tgt_area, np.int32)
+        fill(p.lam_perim, lam_perim, np.float32)
+        fill(p.tgt_perim, tgt_perim, np.int32)
+        p.temperature = float(temperature)
+        p.seed = int(seed)
+        p.stream = int(stream)
+        self.params = p
+        n1 = self.ncells + 1
+        self.area = np.zeros(n1, np.int32)
+        self.perim = np.zeros(n1, np.int32)
+        self.csum = np.zeros((n1, self.ndim), np.int64)
+        self.tick = 0
+        self.counters = np.zeros(3, np.uint64)
+        err = lib().orc_init_tables(ctypes.byref(p), self.lattice.ctypes.data,
+                                    self.area.ctypes.data,
+                                    self.perim.ctypes.data,
+                                    self.csum.ctypes.data)
+        if err:
+            raise ValueError(f"invalid lattice (oracle error bits {err})")
+
+    def run(self, mcs: int, nthreads: int = 0):
+        lib().orc_run(ctypes.byref(self.params), self.lattice.ctypes.data,
+                      self.area.ctypes.data, self.perim.ctypes.data,
+                      self.csum.ctypes.data, self.tick, int(mcs),
+                      int(nthreads), self.counters.ctypes.data)
+        self.tick += int(mcs)
+        return self
+
+    def recount(self):
+        """Tables recomputed from scratch from the current lattice."""
+        n1 = self.ncells + 1
+        area = np.zeros(n1, np.int32)
+        perim = np.zeros(n1, np.int32)
+        csum = np.zeros((n1, self.ndim), np.int64)
+        err = lib().orc_init_tables(ctypes.byref(self.params),
+                                    self.lattice.ctypes.data, area.ctypes.data,
+                                    perim.ctypes.data, csum.ctypes.data)
+        if err:
+            raise ValueError(f"invalid lattice (oracle error bits {err})")
+        return area, perim, csum

@@ -1,0 +1,409 @@
+// cpm_oracle.cpp — CPU oracle of the checkerboard Cellular Potts sweep.
+//
+// TEST INFRASTRUCTURE ONLY.  Nothing in the product links or calls this file:
+// it is loaded by tests/, by __graft_entry__.smoke() and by bench.py's CPU
+// baseline, as the checker the CUDA engine is compared against bit for bit.
+//
+// Parity status: bit-level parity with the reference is unpinned by golden
+// vectors — the reference (shabaz/gpu-cpm) ships no tests or fixtures and is
+// nondeterministic (std::random_device seed per run, src/cpm.cu:347-350; racy
+// area reads, src/kernels2d.cu:297-298).  This file restates the reference's
+// per-attempt algorithm on a deterministic schedule; the restatement is
+// checked against the reference's own CUDA build statistically on the GPU.
+//
+// What follows the reference, function by function:
+//   * site pick / neighbour pick:  src/kernels2d.cu:199-243 (target and a
+//     uniformly random Moore neighbour as source, as in the shared-memory
+//     branch :212-226), 3D src/kernels3d.cu:203-243
+//   * early out when source id == target id: src/kernels2d.cu:276
+//   * adhesion, perimeter, area dH:  src/kernels2d.cu:346-519,
+//     src/kernels3d.cu:368-541 (same term order: adhesion, perimeter source,
+//     perimeter target, area source, area target)
+//   * Metropolis test `dH < 0 || r < exp(-dH/T)`: src/kernels2d.cu:522-525
+//   * commit + area / perimeter bookkeeping: src/kernels2d.cu:544-569
+//   * centroid add / subtract with periodic unwrapping about the running
+//     mean: src/kernels.cu:63-119 (kept as exact int64 sums here)
+//   * table initialisation (area, Moore interface count, centroid):
+//     src/kernels2d.cu:5-41, src/kernels3d.cu:3-47
+//
+// Deterministic schedule (the engine's, not the reference's):
+//   * Sites are coloured by (x mod 2, y mod 2[, z mod 2]); on an axis of odd
+//     length the last coordinate gets a third class 2.  Slot
+//     (cz, cy, cx) in lexicographic order is one phase; an MCS runs every
+//     non-empty slot once, so each site is the target of exactly one attempt
+//     per MCS.  Two targets of one phase are >= 2 apart on every axis (with
+//     wrap), so no attempt reads another attempt's target.
+//   * Every attempt of a phase reads the cell tables as they were when the
+//     phase began; integer deltas are summed after the phase.
+//   * The random numbers of an attempt are Philox4x32-10 (Salmon et al.,
+//     SC'11, "Parallel random numbers: as easy as 1, 2, 3") of counter
+//     (site, phase lo, stream, phase hi) under key (seed lo, seed hi), with
+//     phase = tick * 3^d + slot.  Word 0 picks the neighbour (mulhi by the
+//     neighbour count); word 1 gives the uniform ((w1 >> 8) | 1) * 2^-24.
+//   * dH is FP32: adhesion summed in neighbour order, then each constraint
+//     added with one fused multiply-add of lambda and an exact integer.
+//     exp is computed by exp_neg() below, an own Cody-Waite + Taylor kernel.
+//
+// Build: oracle/build.py (g++ -O2 -ffp-contract=off -fopenmp).  Contraction
+// must stay off so that no a*b+c is fused behind the code's back.
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+#include <omp.h>
+
+namespace {
+
+constexpr int kMaxTypes = 32;
+
+struct Params {
+  int ndim, nx, ny, nz, ncells;
+  float J[kMaxTypes * kMaxTypes];  // J[own type][neighbour type]
+  float lam_area[kMaxTypes];
+  int tgt_area[kMaxTypes];
+  float lam_perim[kMaxTypes];
+  int tgt_perim[kMaxTypes];
+  float temperature;
+  uint64_t seed;
+  uint32_t stream;
+};
+
+// ---- Philox4x32-10 --------------------------------------------------------
+inline void philox_round(uint32_t c[4], uint32_t k0, uint32_t k1) {
+  const uint64_t p0 = (uint64_t)0xD2511F53u * c[0];
+  const uint64_t p1 = (uint64_t)0xCD9E8D57u * c[2];
+  const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+  const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+  const uint32_t n0 = hi1 ^ c[1] ^ k0;
+  const uint32_t n2 = hi0 ^ c[3] ^ k1;
+  c[0] = n0;
+  c[1] = lo1;
+  c[2] = n2;
+  c[3] = lo0;
+}
+
+inline void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
+  for (int r = 0; r < 10; ++r) {
+    if (r) {
+      k0 += 0x9E3779B9u;
+      k1 += 0xBB67AE85u;
+    }
+    philox_round(c, k0, k1);
+  }
+}
+
+// ---- exp(x) for x <= 0 in FP32 --------------------------------------------
+// Cody-Waite reduction x = k ln2 + r, |r| <= ln2/2, with ln2 split into its
+// FP32 rounding and the remainder; exp(r) by the degree-7 Taylor polynomial
+// (1/n! coefficients) in Horner form; 2^k applied by building the exponent.
+// Below x = -20 the result is 0: every uniform used by the sweep is at least
+// 2^-24 > exp(-20), so the Metropolis test rejects there either way.
+inline float exp_neg(float x) {
+  if (x < -20.0f) return 0.0f;
+  const float kf = std::nearbyint(x * 0x1.715476p+0f);  // x * log2(e)
+  float r = std::fma(-kf, 0x1.62e430p-1f, x);           // ln2 (FP32)
+  r = std::fma(-kf, -0x1.05c610p-29f, r);               // ln2 - FP32(ln2)
+  float p = 0x1.a01a02p-13f;                            // 1/7!
+  p = std::fma(p, r, 0x1.6c16c2p-10f);                  // 1/6!
+  p = std::fma(p, r, 0x1.111112p-7f);                   // 1/5!
+  p = std::fma(p, r, 0x1.555556p-5f);                   // 1/4!
+  p = std::fma(p, r, 0x1.555556p-3f);                   // 1/3!
+  p = std::fma(p, r, 0x1.000000p-1f);                   // 1/2!
+  p = std::fma(p, r, 1.0f);
+  p = std::fma(p, r, 1.0f);
+  const int k = (int)kf;  // in [-29, 0]
+  uint32_t bits = (uint32_t)(k + 127) << 23;
+  float scale;
+  std::memcpy(&scale, &bits, 4);
+  return p * scale;
+}
+
+// ---- schedule helpers -------------------------------------------------------
+inline int class_count(int n, int c) {
+  if (n == 1) return c == 0 ? 1 : 0;
+  if (c < 2) return n / 2;
+  return n & 1;
+}
+inline int class_coord(int n, int c, int i) {
+  if (n == 1) return 0;
+  return c < 2 ? 2 * i + c : n - 1;
+}
+inline int wrap(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
+
+// Periodic image of coordinate xc nearest to mean S/a (a >= 1).
+inline int64_t image(int xc, int n, int64_t a, int64_t S) {
+  const int64_t d = (int64_t)xc * a - S;
+  if (2 * d > (int64_t)n * a) return (int64_t)xc - n;
+  if (2 * d < -(int64_t)n * a) return (int64_t)xc + n;
+  return xc;
+}
+
+struct Accepted {
+  uint32_t s, t;  // full site values (id | type << 24)
+  int dps, dpt;
+  int64_t img_s[3], img_t[3];
+};
+
+struct Tables {
+  int32_t* area;
+  int32_t* perim;
+  int64_t* csum;
+};
+
+// One copy attempt at target (x, y, z).  Returns 0 for a no-op, 1 for an
+// evaluated and rejected attempt, 2 for an accepted one (lattice written,
+// *acc filled).
+inline int attempt(const Params& p, uint32_t* lat, const Tables& tb, int x,
+                   int y, int z, uint64_t phase, bool perim_on,
+                   Accepted* acc) {
+  const int nx = p.nx, ny = p.ny, nz = p.nz;
+  const int N = p.ndim == 2 ? 8 : 26;
+  uint32_t nb[26];
+  int m = 0;
+  const int zlo = p.ndim == 3 ? -1 : 0, zhi = p.ndim == 3 ? 1 : 0;
+  for (int dz = zlo; dz <= zhi; ++dz)
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dx = -1; dx <= 1; ++dx) {
+        if (!dz && !dy && !dx) continue;
+        const int xx = wrap(x + dx, nx), yy = wrap(y + dy, ny),
+                  zz = p.ndim == 3 ? wrap(z + dz, nz) : 0;
+        nb[m++] = lat[((int64_t)zz * ny + yy) * nx + xx];
+      }
+  const int64_t site = ((int64_t)z * ny + y) * nx + x;
+  const uint32_t t = lat[site];
+  bool interior = true;
+  for (int k = 0; k < N; ++k) interior &= (nb[k] == t);
+  if (interior) return 0;
+
+  uint32_t r[4] = {(uint32_t)site, (uint32_t)phase, p.stream,
+                   (uint32_t)(phase >> 32)};
+  philox4x32_10(r, (uint32_t)p.seed, (uint32_t)(p.seed >> 32));
+  const int kdir = (int)(((uint64_t)r[0] * (uint64_t)N) >> 32);
+  const uint32_t s = nb[kdir];
+  if (s == t) return 0;
+
+  const int ts = (int)(s >> 24), tt = (int)(t >> 24);
+  float e_old = 0.0f, e_new = 0.0f;
+  int cnt_s = 0, cnt_t = 0;
+  for (int k = 0; k < N; ++k) {
+    const int tn = (int)(nb[k] >> 24);
+    if (nb[k] != t) e_old = e_old + p.J[tt * kMaxTypes + tn];
+    if (nb[k] != s) e_new = e_new + p.J[ts * kMaxTypes + tn];
+    cnt_s += nb[k] == s;
+    cnt_t += nb[k] == t;
+  }
+  float dH = e_new - e_old;
+  const int dps = N - 2 * cnt_s;  // source cell gains the target site
+  const int dpt = 2 * cnt_t - N;  // target cell loses it
+  const uint32_t is = s & 0xFFFFFFu, it = t & 0xFFFFFFu;
+  if (perim_on) {
+    if (s != 0) {
+      const int64_t P = tb.perim[is];
+      const int64_t q = (int64_t)dps * (2 * (P - p.tgt_perim[ts]) + dps);
+      dH = std::fma(p.lam_perim[ts], (float)q, dH);
+    }
+    if (t != 0) {
+      const int64_t P = tb.perim[it];
+      const int64_t q = (int64_t)dpt * (2 * (P - p.tgt_perim[tt]) + dpt);
+      dH = std::fma(p.lam_perim[tt], (float)q, dH);
+    }
+  }
+  if (s != 0) {
+    const int64_t q = 1 + 2 * ((int64_t)tb.area[is] - p.tgt_area[ts]);
+    dH = std::fma(p.lam_area[ts], (float)q, dH);
+  }
+  if (t != 0) {
+    const int64_t q = 1 - 2 * ((int64_t)tb.area[it] - p.tgt_area[tt]);
+    dH = std::fma(p.lam_area[tt], (float)q, dH);
+  }
+
+  bool ok;
+  if (dH < 0.0f) {
+    ok = true;
+  } else if (!(p.temperature > 0.0f)) {
+    ok = false;
+  } else {
+    const float u = (float)((r[1] >> 8) | 1u) * 0x1p-24f;
+    ok = u < exp_neg(-dH / p.temperature);
+  }
+  if (!ok) return 1;
+
+  lat[site] = s;
+  acc->s = s;
+  acc->t = t;
+  acc->dps = dps;
+  acc->dpt = dpt;
+  const int coord[3] = {x, y, z};
+  const int dims[3] = {nx, ny, nz};
+  for (int a = 0; a < p.ndim; ++a) {
+    acc->img_s[a] = s ? image(coord[a], dims[a], tb.area[is],
+                              tb.csum[(int64_t)is * p.ndim + a])
+                      : 0;
+    acc->img_t[a] = t ? image(coord[a], dims[a], tb.area[it],
+                              tb.csum[(int64_t)it * p.ndim + a])
+                      : 0;
+  }
+  return 2;
+}
+
+bool perimeter_enabled(const Params& p) {
+  for (int k = 0; k < kMaxTypes; ++k)
+    if (p.lam_perim[k] != 0.0f) return true;
+  return false;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Parameter block shared with oracle/__init__.py (ctypes.Structure).
+typedef Params orc_params;
+
+// Philox4x32-10 of one counter block (known-answer tests).
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2],
+                       uint32_t out[4]) {
+  uint32_t c[4] = {ctr[0], ctr[1], ctr[2], ctr[3]};
+  philox4x32_10(c, key[0], key[1]);
+  std::memcpy(out, c, sizeof c);
+}
+
+float orc_exp_neg(float x) { return exp_neg(x); }
+
+// Recompute every table from the lattice.  Returns 0, or a bit set of
+// 1: id above ncells, 2: type >= 32, 4: non-zero type on id 0,
+// 8: one id carries two types.
+int orc_init_tables(const orc_params* pp, const uint32_t* lat, int32_t* area,
+                    int32_t* perim, int64_t* csum) {
+  const Params& p = *pp;
+  const int nx = p.nx, ny = p.ny, nz = p.ndim == 3 ? p.nz : 1;
+  const int64_t nsites = (int64_t)nx * ny * nz;
+  const int64_t ncell1 = (int64_t)p.ncells + 1;
+  std::vector<int64_t> first(ncell1, -1);
+  std::vector<int> type(ncell1, -1);
+  int err = 0;
+  for (int64_t i = 0; i < nsites; ++i) {
+    const uint32_t v = lat[i];
+    const uint32_t id = v & 0xFFFFFFu;
+    const int ty = (int)(v >> 24);
+    if (id > (uint32_t)p.ncells) { err |= 1; continue; }
+    if (ty >= kMaxTypes) err |= 2;
+    if (id == 0 && ty != 0) err |= 4;
+    if (type[id] < 0) type[id] = ty;
+    else if (type[id] != ty) err |= 8;
+    if (first[id] < 0) first[id] = i;
+  }
+  if (err) return err;
+  std::memset(area, 0, sizeof(int32_t) * ncell1);
+  std::memset(perim, 0, sizeof(int32_t) * ncell1);
+  std::memset(csum, 0, sizeof(int64_t) * ncell1 * p.ndim);
+  const int dims[3] = {nx, ny, nz};
+  for (int z = 0; z < nz; ++z)
+    for (int y = 0; y < ny; ++y)
+      for (int x = 0; x < nx; ++x) {
+        const int64_t i = ((int64_t)z * ny + y) * nx + x;
+        const uint32_t v = lat[i];
+        const uint32_t id = v & 0xFFFFFFu;
+        if (id == 0) continue;
+        int foreign = 0;
+        const int zlo = p.ndim == 3 ? -1 : 0, zhi = p.ndim == 3 ? 1 : 0;
+        for (int dz = zlo; dz <= zhi; ++dz)
+          for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+              if (!dz && !dy && !dx) continue;
+              const int xx = wrap(x + dx, nx), yy = wrap(y + dy, ny),
+                        zz = p.ndim == 3 ? wrap(z + dz, nz) : 0;
+              foreign += lat[((int64_t)zz * ny + yy) * nx + xx] != v;
+            }
+        area[id] += 1;
+        perim[id] += foreign;
+        const int64_t f = first[id];
+        const int anchor[3] = {(int)(f % nx), (int)((f / nx) % ny),
+                               (int)(f / ((int64_t)nx * ny))};
+        const int c[3] = {x, y, z};
+        for (int a = 0; a < p.ndim; ++a)
+          csum[(int64_t)id * p.ndim + a] += image(c[a], dims[a], 1, anchor[a]);
+      }
+  return 0;
+}
+
+// Run `mcs` Monte Carlo steps from tick `tick0` in place.  counters[0..2]
+// receive attempts, evaluated and accepted counts (added to).  `nthreads`
+// <= 0 uses every OpenMP thread; the result does not depend on it.
+int orc_run(const orc_params* pp, uint32_t* lat, int32_t* area, int32_t* perim,
+            int64_t* csum, uint64_t tick0, int mcs, int nthreads,
+            uint64_t* counters) {
+  const Params& p = *pp;
+  const int nx = p.nx, ny = p.ny, nz = p.ndim == 3 ? p.nz : 1;
+  const int nslots = p.ndim == 2 ? 9 : 27;
+  const bool perim_on = perimeter_enabled(p);
+  Tables tb{area, perim, csum};
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+  std::vector<std::vector<Accepted>> logs(nthreads);
+  uint64_t n_att = 0, n_eval = 0, n_acc = 0;
+  for (int m = 0; m < mcs; ++m) {
+    const uint64_t tick = tick0 + (uint64_t)m;
+    for (int cz = 0; cz < (p.ndim == 3 ? 3 : 1); ++cz)
+      for (int cy = 0; cy < 3; ++cy)
+        for (int cx = 0; cx < 3; ++cx) {
+          const int ncx = class_count(nx, cx), ncy = class_count(ny, cy),
+                    ncz = class_count(nz, cz);
+          if (!ncx || !ncy || !ncz) continue;
+          const int slot = (cz * 3 + cy) * 3 + cx;
+          const uint64_t phase = tick * (uint64_t)nslots + (uint64_t)slot;
+          const int64_t nrows = (int64_t)ncy * ncz;
+          uint64_t e = 0, a = 0;
+#pragma omp parallel num_threads(nthreads) reduction(+ : e, a)
+          {
+            std::vector<Accepted>& log = logs[omp_get_thread_num()];
+            log.clear();
+#pragma omp for schedule(static)
+            for (int64_t row = 0; row < nrows; ++row) {
+              const int z = class_coord(nz, cz, (int)(row / ncy));
+              const int y = class_coord(ny, cy, (int)(row % ncy));
+              for (int i = 0; i < ncx; ++i) {
+                const int x = class_coord(nx, cx, i);
+                Accepted acc;
+                const int res = attempt(p, lat, tb, x, y, z, phase, perim_on,
+                                        &acc);
+                if (res >= 1) ++e;
+                if (res == 2) {
+                  ++a;
+                  log.push_back(acc);
+                }
+              }
+            }
+          }
+          n_att += (uint64_t)ncx * ncy * ncz;
+          n_eval += e;
+          n_acc += a;
+          // Apply the phase's deltas; integer sums, so order is irrelevant.
+          for (auto& log : logs)
+            for (const Accepted& c : log) {
+              if (c.s) {
+                const uint32_t is = c.s & 0xFFFFFFu;
+                area[is] += 1;
+                perim[is] += c.dps;
+                for (int d = 0; d < p.ndim; ++d)
+                  csum[(int64_t)is * p.ndim + d] += c.img_s[d];
+              }
+              if (c.t) {
+                const uint32_t it = c.t & 0xFFFFFFu;
+                area[it] -= 1;
+                perim[it] += c.dpt;
+                for (int d = 0; d < p.ndim; ++d)
+                  csum[(int64_t)it * p.ndim + d] -= c.img_t[d];
+              }
+            }
+          for (auto& log : logs) log.clear();
+        }
+  }
+  if (counters) {
+    counters[0] += n_att;
+    counters[1] += n_eval;
+    counters[2] += n_acc;
+  }
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,45 @@
+"""CPU tests of the C-ABI library: it builds for sm_103a, loads, and exports
+every function include/gpucpm.h declares.  No compute call is made."""
+import ctypes
+import pathlib
+import re
+
+ROOT = pathlib.Path(__file__).resolve().parents[1]
+
+
+def declared_functions():
+    text = (ROOT / "include" / "gpucpm.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(cpm_\w+)\s*\(", text)))
+
+
+def test_header_declares_the_boundary():
+    names = declared_functions()
+    for required in ("cpm_create", "cpm_destroy", "cpm_push", "cpm_pull", "cpm_run",
+                     "cpm_synchronize", "cpm_add_cell", "cpm_set_adhesion",
+                     "cpm_set_area", "cpm_set_perimeter", "cpm_get_centroids",
+                     "cpm_host_lattice", "cpm_last_error", "cpm_create_batch"):
+        assert required in names
+
+
+def test_library_exports_every_declared_symbol(engine_lib):
+    missing = [n for n in declared_functions() if not hasattr(engine_lib, n)]
+    assert not missing, missing
+
+
+def test_create_failure_reports_message_without_gpu(engine_lib):
+    import torch
+    if torch.cuda.is_available():
+        return  # covered by the GPU tests
+    h = ctypes.c_void_p()
+    rc = engine_lib.cpm_create(64, 2, 10, 10.0, 0, ctypes.byref(h))
+    assert rc != 0 and not h.value
+    assert engine_lib.cpm_last_error(None)
+
+
+def test_invalid_arguments_rejected_before_touching_cuda(engine_lib):
+    h = ctypes.c_void_p()
+    assert engine_lib.cpm_create(64, 4, 10, 10.0, 0, ctypes.byref(h)) == 1
+    assert b"dimensionality" in engine_lib.cpm_last_error(None)
+    assert engine_lib.cpm_create(64, 2, 10, 10.0, 1, ctypes.byref(h)) == 6
+    assert engine_lib.cpm_create(2, 2, 10, 10.0, 0, ctypes.byref(h)) == 1

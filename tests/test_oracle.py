@@ -1,0 +1,241 @@
+"""CPU tests of the oracle: known-answer vectors, exp error bound, table
+recount on hand-computed lattices, hand-computed dH against the reference's
+formula, invariants after sweeps and thread-count independence."""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+from gpucpm import workloads as W
+
+
+# Philox4x32-10 known-answer vectors (Random123 kat_vectors, philox4x32_10).
+KAT = [
+    ([0, 0, 0, 0], [0, 0], [0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8]),
+    ([0xffffffff] * 4, [0xffffffff] * 2,
+     [0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd]),
+    ([0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344], [0xa4093822, 0x299f31d0],
+     [0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1]),
+]
+
+
+@pytest.mark.parametrize("ctr,key,want", KAT)
+def test_philox_known_answers(ctr, key, want):
+    assert oracle.philox4x32_10(ctr, key) == want
+
+
+def test_exp_neg_error_bound():
+    xs = np.concatenate([np.linspace(-20.0, 0.0, 40001, dtype=np.float32),
+                         np.float32(-np.logspace(-8, np.log10(20), 2000))])
+    worst = 0.0
+    for x in xs:
+        got = oracle.exp_neg(float(x))
+        ref = math.exp(float(x))
+        worst = max(worst, abs(got - ref) / float(np.spacing(np.float32(ref))))
+    assert worst <= 1.0, worst  # at most 1 ulp of FP32 over [-20, 0]
+    assert oracle.exp_neg(0.0) == 1.0
+    assert oracle.exp_neg(-20.5) == 0.0
+
+
+def _sim(lat, ncells, J=None, **kw):
+    if J is None:
+        J = np.zeros((3, 3), np.float32)
+    kw.setdefault("lam_area", [0, 1, 1])
+    kw.setdefault("tgt_area", [0, 9, 9])
+    return oracle.OracleSim(np.asarray(lat, np.uint32), ncells, J, **kw)
+
+
+def test_recount_single_square_2d():
+    lat = np.zeros((8, 8), np.uint32)
+    lat[2:5, 3:6] = 1 | (1 << 24)
+    s = _sim(lat, 1)
+    # 3x3 block in medium: 4 corners x 5 + 4 edges x 3 foreign Moore neighbours
+    assert s.area[1] == 9 and s.perim[1] == 32
+    assert list(s.csum[1]) == [3 * (3 + 4 + 5), 3 * (2 + 3 + 4)]
+
+
+def test_recount_wrapped_cell_uses_nearest_images():
+    lat = np.zeros((10, 10), np.uint32)
+    lat[4, [9, 0, 1]] = 1 | (1 << 24)  # straddles the periodic x boundary
+    s = _sim(lat, 1)
+    assert s.area[1] == 3
+    # anchor is the first site in raster order (x=0); x=9 maps to -1
+    assert s.csum[1][0] == -1 + 0 + 1 and s.csum[1][1] == 12
+
+
+def test_recount_3d_cube():
+    lat = np.zeros((6, 6, 6), np.uint32)
+    lat[1:3, 1:3, 1:3] = 1 | (2 << 24)
+    s = _sim(lat, 1)
+    # each site of a 2x2x2 cube has 7 same-cell and 19 foreign neighbours
+    assert s.area[1] == 8 and s.perim[1] == 8 * 19
+
+
+def test_invalid_lattices_rejected():
+    lat = np.zeros((6, 6), np.uint32)
+    lat[0, 0] = 5 | (1 << 24)
+    with pytest.raises(ValueError):
+        _sim(lat, 3)  # id above ncells
+    lat[0, 0] = 1 << 24
+    with pytest.raises(ValueError):
+        _sim(lat, 3)  # medium with a type
+    lat[0, 0] = 1 | (1 << 24)
+    lat[0, 1] = 1 | (2 << 24)
+    with pytest.raises(ValueError):
+        _sim(lat, 3)  # one id, two types
+
+
+def _reference_dh(lat, ax, ay, sx, sy, area, perim, J, lam_a, tgt_a, lam_p, tgt_p):
+    """dH of copying (sx, sy) into (ax, ay), restated from the reference
+    (src/kernels2d.cu:346-519): integer adhesion sums, double lambda terms."""
+    n = lat.shape[0]
+    s, t = int(lat[sy, sx]), int(lat[ay, ax])
+    ts, tt = s >> 24, t >> 24
+    e_old = e_new = 0
+    ops = nps = opt = npt = 0
+    for j in (-1, 0, 1):
+        for i in (-1, 0, 1):
+            if i == 0 and j == 0:
+                continue
+            v = int(lat[(ay + j) % n, (ax + i) % n])
+            tv = v >> 24
+            if t != v:
+                e_old += J[tt][tv]
+            if s != v:
+                e_new += J[ts][tv]
+            ops += v == s
+            nps += v != s
+            opt += v != t
+            npt += v == t
+    e = float(e_new - e_old)
+    if s:
+        P = perim[s & 0xFFFFFF]
+        Pn = P - ops + nps
+        e += lam_p[ts] * ((Pn - tgt_p[ts]) ** 2 - (P - tgt_p[ts]) ** 2)
+    if t:
+        P = perim[t & 0xFFFFFF]
+        Pn = P - opt + npt
+        e += lam_p[tt] * ((Pn - tgt_p[tt]) ** 2 - (P - tgt_p[tt]) ** 2)
+    if s:
+        e += lam_a[ts] * (1 + 2 * area[s & 0xFFFFFF] - 2 * tgt_a[ts])
+    if t:
+        e += lam_a[tt] * (1 - 2 * area[t & 0xFFFFFF] + 2 * tgt_a[tt])
+    return e
+
+
+def test_first_mcs_matches_reference_dh_formula():
+    """Replay one MCS in Python with the reference's dH formula and the same
+    Philox draws, and compare the result with the oracle."""
+    w = W.random_small((16, 16), 10, seed=11, temperature=6.0)
+    J = np.rint(w.J).astype(int)            # integer J: both sides exact
+    lam_a = [1.0] * 3
+    lam_p = [0.5] * 3
+    tgt_a, tgt_p = [0, 20, 20], [0, 18, 18]
+    T = 6.0
+    sim = oracle.OracleSim(w.lattice, w.ncells, J.astype(np.float32), lam_a, tgt_a,
+                           lam_p, tgt_p, temperature=T, seed=7)
+    lat = w.lattice.copy()
+    area, perim = sim.area.copy(), sim.perim.copy()
+    n = 16
+    accepted = 0
+    for cy in (0, 1):
+        for cx in (0, 1):
+            slot = cy * 3 + cx
+            changes = []
+            for y in range(cy, n, 2):
+                for x in range(cx, n, 2):
+                    t = int(lat[y, x])
+                    nbs = [(x + i, y + j) for j in (-1, 0, 1) for i in (-1, 0, 1)
+                           if (i, j) != (0, 0)]
+                    vals = [int(lat[b % n, a % n]) for a, b in nbs]
+                    if all(v == t for v in vals):
+                        continue
+                    r = oracle.philox4x32_10([y * n + x, slot, 0, 0], [7, 0])
+                    k = (r[0] * 8) >> 32
+                    if vals[k] == t:
+                        continue
+                    sx, sy = nbs[k][0] % n, nbs[k][1] % n
+                    dH = _reference_dh(lat, x, y, sx, sy, area, perim, J, lam_a,
+                                       tgt_a, lam_p, tgt_p)
+                    u = ((r[1] >> 8) | 1) * 2.0 ** -24
+                    if dH < 0 or u < math.exp(-dH / T):
+                        changes.append((x, y, vals[k], t, vals))
+            for x, y, s, t, vals in changes:
+                lat[y, x] = s
+                accepted += 1
+                if s:
+                    area[s & 0xFFFFFF] += 1
+                    perim[s & 0xFFFFFF] += 8 - 2 * sum(v == s for v in vals)
+                if t:
+                    area[t & 0xFFFFFF] -= 1
+                    perim[t & 0xFFFFFF] += 2 * sum(v == t for v in vals) - 8
+    sim.run(1)
+    assert accepted > 5
+    assert int(sim.counters[2]) == accepted
+    np.testing.assert_array_equal(sim.lattice, lat)
+    np.testing.assert_array_equal(sim.area, area)
+    np.testing.assert_array_equal(sim.perim, perim)
+
+
+@pytest.mark.parametrize("shape,ncells", [((64, 64), 40), ((37, 41), 30),
+                                          ((12, 10, 14), 25), ((9, 13, 11), 20)])
+def test_tables_match_recount_after_sweeps(shape, ncells):
+    w = W.random_small(shape, ncells, seed=len(shape) * 7 + ncells)
+    s = oracle.OracleSim(w.lattice, w.ncells, **w.oracle_kwargs(), seed=3)
+    s.run(30 if len(shape) == 2 else 10)
+    a, p, c = s.recount()
+    np.testing.assert_array_equal(a, s.area)
+    np.testing.assert_array_equal(p, s.perim)
+    dims = np.array(shape[::-1])
+    assert ((c - s.csum) % dims == 0).all()
+    assert int(s.area[1:].sum()) == int(((s.lattice & 0xFFFFFF) != 0).sum())
+
+
+def test_thread_count_does_not_change_result():
+    w = W.random_small((48, 52), 35, seed=4)
+    a = oracle.OracleSim(w.lattice, w.ncells, **w.oracle_kwargs(), seed=9).run(20, 1)
+    b = oracle.OracleSim(w.lattice, w.ncells, **w.oracle_kwargs(), seed=9).run(20, 5)
+    np.testing.assert_array_equal(a.lattice, b.lattice)
+    np.testing.assert_array_equal(a.csum, b.csum)
+    np.testing.assert_array_equal(a.counters, b.counters)
+
+
+def test_run_is_resumable_by_tick():
+    w = W.random_small((32, 32), 20, seed=8)
+    a = oracle.OracleSim(w.lattice, w.ncells, **w.oracle_kwargs(), seed=2).run(12)
+    b = oracle.OracleSim(w.lattice, w.ncells, **w.oracle_kwargs(), seed=2).run(5).run(7)
+    np.testing.assert_array_equal(a.lattice, b.lattice)
+
+
+def test_zero_temperature_accepts_only_downhill():
+    w = W.random_small((32, 32), 20, seed=12, temperature=0.0)
+    s = oracle.OracleSim(w.lattice, w.ncells, **w.oracle_kwargs())
+    e0 = _total_energy(s)
+    s.run(5)
+    assert _total_energy(s) <= e0
+
+
+def _total_energy(s):
+    lat = s.lattice.astype(np.int64)
+    J = np.asarray(s.params.J).reshape(32, 32)
+    e = 0.0
+    n0, n1 = lat.shape
+    for j in (-1, 0, 1):
+        for i in (-1, 0, 1):
+            if (i, j) == (0, 0):
+                continue
+            nb = np.roll(np.roll(lat, -j, 0), -i, 1)
+            diff = nb != lat
+            e += J[lat >> 24, nb >> 24][diff].sum()
+    e /= 2
+    la = np.asarray(s.params.lam_area)
+    ta = np.asarray(s.params.tgt_area)
+    ids = np.arange(1, s.ncells + 1)
+    ty = np.zeros(s.ncells + 1, int)
+    ty[lat.ravel() & 0xFFFFFF] = lat.ravel() >> 24
+    e += (la[ty[ids]] * (s.area[ids] - ta[ty[ids]]) ** 2).sum()
+    lp = np.asarray(s.params.lam_perim)
+    tp = np.asarray(s.params.tgt_perim)
+    e += (lp[ty[ids]] * (s.perim[ids] - tp[ty[ids]]) ** 2).sum()
+    return e
