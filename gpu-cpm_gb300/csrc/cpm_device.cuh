@@ -94,36 +94,50 @@ __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
   return v;
 }
 
+__device__ __forceinline__ void st_release_gpu(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v)
+               : "memory");
+}
+
 // Grid-wide barrier of a cooperative launch (all blocks co-resident).  The
-// counter ctl[kCtlBarrier] is zeroed before the launch and only grows; the
-// e-th barrier of the launch completes when it reaches gridDim.x * (e + 1).
-// The wait is bounded: after kBarrierTimeoutNs the block sets kErrTimeout
-// and every block returns false at its next barrier, so a lost block ends
-// the kernel with an error status instead of a hang.  Block-uniform result.
+// arrival counter ctl[kCtlBarrier] and the release flag ctl[kCtlFlag] are
+// zeroed before the launch and only grow.  At the e-th barrier (e = 1, 2,
+// ...) each block adds 1 to the counter; the block that brings it to
+// gridDim.x * e publishes e in the flag, which the others poll with backoff.
+// The wait is bounded: after `timeout_ns` the block sets kErrTimeout and
+// every block returns false at its next barrier, so a lost block ends the
+// kernel with an error status instead of a hang.  Block-uniform result.
 constexpr unsigned long long kBarrierTimeoutNs = 2000000000ull;
 
 __device__ __forceinline__ bool grid_barrier(
-    uint32_t* ctl, unsigned target, int* s_ok,
+    uint32_t* ctl, unsigned episode, int* s_ok,
     unsigned long long timeout_ns = kBarrierTimeoutNs) {
   __syncthreads();
   if (threadIdx.x == 0) {
-    __threadfence();
-    atomicAdd(&ctl[kCtlBarrier], 1u);
-    const unsigned long long t0 = global_timer_ns();
-    unsigned spins = 0;
     int ok = 1;
-    while (ld_acquire_gpu(&ctl[kCtlBarrier]) < target) {
-      if (ld_acquire_gpu(&ctl[kCtlErr]) & kErrTimeout) {
-        ok = 0;
-        break;
+    __threadfence();
+    const unsigned arrived = atomicAdd(&ctl[kCtlBarrier], 1u) + 1u;
+    if (arrived == gridDim.x * episode) {
+      __threadfence();
+      st_release_gpu(&ctl[kCtlFlag], episode);
+    } else {
+      const unsigned long long t0 = global_timer_ns();
+      unsigned spins = 0, nap = 32;
+      while (ld_acquire_gpu(&ctl[kCtlFlag]) < episode) {
+        if ((++spins & 15u) == 0) {
+          if (ld_acquire_gpu(&ctl[kCtlErr]) & kErrTimeout) {
+            ok = 0;
+            break;
+          }
+          if (global_timer_ns() - t0 > timeout_ns) {
+            atomicOr((int*)&ctl[kCtlErr], kErrTimeout);
+            ok = 0;
+            break;
+          }
+        }
+        __nanosleep(nap);
+        if (nap < 256) nap <<= 1;
       }
-      if ((++spins & 63u) == 0 &&
-          global_timer_ns() - t0 > timeout_ns) {
-        atomicOr((int*)&ctl[kCtlErr], kErrTimeout);
-        ok = 0;
-        break;
-      }
-      __nanosleep(32);
     }
     __threadfence();
     *s_ok = ok;

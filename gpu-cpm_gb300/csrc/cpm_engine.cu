@@ -48,11 +48,11 @@ struct cpm_handle {
 
   uint32_t* h_lat = nullptr;  // pinned, all replicas back to back
   uint32_t* d_lat = nullptr;
-  int2* d_ap = nullptr;
-  long long* d_cs = nullptr;
-  int2* d_dap = nullptr;
-  long long* d_dcs = nullptr;
-  uint32_t* d_dflag = nullptr;
+  unsigned long long* d_ap[2] = {nullptr, nullptr};  // packed (area, perimeter)
+  long long* d_cs[2] = {nullptr, nullptr};
+  unsigned long long* d_dap[2] = {nullptr, nullptr};
+  long long* d_dcs[2] = {nullptr, nullptr};
+  uint32_t* d_dflag[2] = {nullptr, nullptr};
   uint32_t* d_dlist = nullptr;
   uint32_t* d_ctl = nullptr;
   unsigned long long* d_counters = nullptr;
@@ -65,6 +65,7 @@ struct cpm_handle {
   cudaStream_t stream = nullptr;      // stream work is enqueued on
   cudaStream_t own_stream = nullptr;  // created with the handle
   int grid = 1;
+  long long list_cap = 0;
   std::vector<int> task_prefix;  // [27][nrep + 1]
   std::vector<int> active_slots;
   std::vector<unsigned long long> attempts;  // per replica, host-counted
@@ -117,11 +118,13 @@ void free_all(cpm_handle* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   cudaFreeHost(h->h_lat);
   cudaFree(h->d_lat);
-  cudaFree(h->d_ap);
-  cudaFree(h->d_cs);
-  cudaFree(h->d_dap);
-  cudaFree(h->d_dcs);
-  cudaFree(h->d_dflag);
+  for (int b = 0; b < 2; ++b) {
+    cudaFree(h->d_ap[b]);
+    cudaFree(h->d_cs[b]);
+    cudaFree(h->d_dap[b]);
+    cudaFree(h->d_dcs[b]);
+    cudaFree(h->d_dflag[b]);
+  }
   cudaFree(h->d_dlist);
   cudaFree(h->d_ctl);
   cudaFree(h->d_counters);
@@ -214,12 +217,13 @@ int build_engine(int n, int ndim, const int* nx, const int* ny, const int* nz,
     if (e == cudaSuccess) e = cudaMalloc(p, bytes ? bytes : 1);
   };
   al((void**)&h->d_lat, sizeof(uint32_t) * sites);
-  al((void**)&h->d_ap, sizeof(int2) * rows);
-  al((void**)&h->d_cs, sizeof(long long) * rows * ndim);
-  al((void**)&h->d_dap, sizeof(int2) * rows);
-  al((void**)&h->d_dcs, sizeof(long long) * rows * ndim);
-  al((void**)&h->d_dflag, sizeof(uint32_t) * rows);
-  al((void**)&h->d_dlist, sizeof(uint32_t) * rows * 2);
+  for (int b = 0; b < 2; ++b) {
+    al((void**)&h->d_ap[b], sizeof(unsigned long long) * rows);
+    al((void**)&h->d_cs[b], sizeof(long long) * rows * ndim);
+    al((void**)&h->d_dap[b], sizeof(unsigned long long) * rows);
+    al((void**)&h->d_dcs[b], sizeof(long long) * rows * ndim);
+    al((void**)&h->d_dflag[b], sizeof(uint32_t) * rows);
+  }
   al((void**)&h->d_ctl, sizeof(uint32_t) * kCtlWords);
   al((void**)&h->d_counters, sizeof(unsigned long long) * 2 * n);
   al((void**)&h->d_first, sizeof(unsigned long long) * rows);
@@ -236,7 +240,10 @@ int build_engine(int n, int ndim, const int* nx, const int* ny, const int* nz,
   }
   std::memset(h->h_lat, 0, sizeof(uint32_t) * sites);
 
-  // Block tasks per slot and replica (prefix over replicas).
+  // Sweep tiles per slot and replica (prefix over replicas).
+  const int tcx = ndim == 2 ? TileGeom<2>::CX : TileGeom<3>::CX;
+  const int tcy = ndim == 2 ? TileGeom<2>::CY : TileGeom<3>::CY;
+  const int tcz = ndim == 2 ? TileGeom<2>::CZ : TileGeom<3>::CZ;
   h->task_prefix.assign(27 * (n + 1), 0);
   long long max_tasks = 1;
   for (int slot = 0; slot < 27; ++slot) {
@@ -248,8 +255,8 @@ int build_engine(int n, int ndim, const int* nx, const int* ny, const int* nz,
       if (ndim == 2 && cz != 0) continue;
       const long long ncx = class_count_h(R.nx, cx), ncy = class_count_h(R.ny, cy),
                       ncz = class_count_h(R.nz, cz);
-      const long long segs = ncy * ncz * ((ncx + 31) / 32);
-      acc += (segs + kWarpsPerBlock - 1) / kWarpsPerBlock;
+      if (!ncx || !ncy || !ncz) continue;
+      acc += ((ncx + tcx - 1) / tcx) * ((ncy + tcy - 1) / tcy) * ((ncz + tcz - 1) / tcz);
     }
     if (acc >= (1LL << 31)) {
       g_create_error = "batch too large for one launch";
@@ -272,8 +279,23 @@ int build_engine(int n, int ndim, const int* nx, const int* ny, const int* nz,
     delete h;
     return CPM_ERR_CUDA;
   }
-  h->grid = (int)std::min<long long>((long long)per_sm * sms, max_tasks);
+  // One block per SM (fewer if the largest slot has fewer warp tiles).
+  const long long blocks_needed = (max_tasks + kSweepWarps - 1) / kSweepWarps;
+  h->grid = (int)std::min<long long>((long long)per_sm * sms, blocks_needed);
   h->grid = std::max(h->grid, 1);
+  // Per-block dirty lists (two per block, for the running and the previous
+  // phase): a warp works at most ceil(tiles / warps) tiles per slot, each
+  // attempt touching at most two table rows.
+  const long long warps = (long long)h->grid * kSweepWarps;
+  h->list_cap = 2LL * sweep_tile_targets(ndim) * kSweepWarps *
+                ((max_tasks + warps - 1) / warps);
+  e = cudaMalloc((void**)&h->d_dlist, sizeof(uint32_t) * h->list_cap * 2 * h->grid);
+  if (e != cudaSuccess) {
+    g_create_error = std::string("dirty-list allocation failed: ") + cudaGetErrorString(e);
+    free_all(h);
+    delete h;
+    return e == cudaErrorMemoryAllocation ? CPM_ERR_ALLOC : CPM_ERR_CUDA;
+  }
 
   e = cudaMemcpyAsync(h->d_reps, h->reps.data(), sizeof(DevReplica) * n,
                       cudaMemcpyHostToDevice, h->stream);
@@ -488,18 +510,25 @@ int cpm_push(cpm_handle* h) {
   h->pushed = false;
   CPM_CUDA(h, cudaMemcpyAsync(h->d_lat, h->h_lat, sizeof(uint32_t) * h->total_sites,
                               cudaMemcpyHostToDevice, h->stream));
-  CPM_CUDA(h, cudaMemsetAsync(h->d_ap, 0, sizeof(int2) * h->rows, h->stream));
-  CPM_CUDA(h, cudaMemsetAsync(h->d_cs, 0, sizeof(long long) * h->rows * h->ndim, h->stream));
-  CPM_CUDA(h, cudaMemsetAsync(h->d_dap, 0, sizeof(int2) * h->rows, h->stream));
-  CPM_CUDA(h, cudaMemsetAsync(h->d_dcs, 0, sizeof(long long) * h->rows * h->ndim, h->stream));
-  CPM_CUDA(h, cudaMemsetAsync(h->d_dflag, 0, sizeof(uint32_t) * h->rows, h->stream));
+  for (int b = 0; b < 2; ++b) {
+    CPM_CUDA(h, cudaMemsetAsync(h->d_ap[b], 0, sizeof(unsigned long long) * h->rows, h->stream));
+    CPM_CUDA(h, cudaMemsetAsync(h->d_cs[b], 0, sizeof(long long) * h->rows * h->ndim, h->stream));
+    CPM_CUDA(h, cudaMemsetAsync(h->d_dap[b], 0, sizeof(unsigned long long) * h->rows, h->stream));
+    CPM_CUDA(h, cudaMemsetAsync(h->d_dcs[b], 0, sizeof(long long) * h->rows * h->ndim, h->stream));
+    CPM_CUDA(h, cudaMemsetAsync(h->d_dflag[b], 0, sizeof(uint32_t) * h->rows, h->stream));
+  }
   CPM_CUDA(h, cudaMemsetAsync(h->d_first, 0xFF, sizeof(unsigned long long) * h->rows, h->stream));
   CPM_CUDA(h, cudaMemsetAsync(h->d_ctype, 0xFF, sizeof(int) * h->rows, h->stream));
   CPM_CUDA(h, cudaMemsetAsync(h->d_ctl, 0, sizeof(uint32_t) * kCtlWords, h->stream));
   CPM_CUDA(h, launch_init(h->ndim, h->d_lat, h->d_reps, h->nrep, h->total_sites,
-                          h->d_ap, h->d_cs, h->d_first, h->d_ctype, h->d_ctl,
+                          h->d_ap[0], h->d_cs[0], h->d_first, h->d_ctype, h->d_ctl,
                           h->stream));
   h->launches += 2;
+  // Both table copies start equal (the sweep keeps them equal between runs).
+  CPM_CUDA(h, cudaMemcpyAsync(h->d_ap[1], h->d_ap[0], sizeof(unsigned long long) * h->rows,
+                              cudaMemcpyDeviceToDevice, h->stream));
+  CPM_CUDA(h, cudaMemcpyAsync(h->d_cs[1], h->d_cs[0], sizeof(long long) * h->rows * h->ndim,
+                              cudaMemcpyDeviceToDevice, h->stream));
   uint32_t w = 0;
   if (int rc = read_error_word(h, &w)) return rc;
   if (w) {
@@ -537,18 +566,20 @@ int cpm_run(cpm_handle* h, int mcs) {
   SweepArgs a;
   std::memset(&a, 0, sizeof a);
   a.lat = h->d_lat;
-  a.ap = h->d_ap;
-  a.cs = h->d_cs;
-  a.dap = h->d_dap;
-  a.dcs = h->d_dcs;
-  a.dflag = h->d_dflag;
+  for (int b = 0; b < 2; ++b) {
+    a.ap[b] = h->d_ap[b];
+    a.cs[b] = h->d_cs[b];
+    a.dap[b] = h->d_dap[b];
+    a.dcs[b] = h->d_dcs[b];
+    a.dflag[b] = h->d_dflag[b];
+  }
   a.dlist = h->d_dlist;
+  a.list_cap = h->list_cap;
   a.ctl = h->d_ctl;
   a.counters = h->d_counters;
   a.reps = h->d_reps;
   a.params = h->d_params;
   a.task_prefix = h->d_task_prefix;
-  a.rows = h->rows;
   a.seed = h->seed;
   a.nrep = h->nrep;
   a.stream0 = h->stream_id;
@@ -627,17 +658,18 @@ int cpm_get_tables_r(cpm_handle* h, int r, int32_t* area, int32_t* perimeter,
   const DevReplica& R = h->reps[r];
   const long long n1 = (long long)R.ncells + 1;
   if (area || perimeter) {
-    std::vector<int2> ap(n1);
-    CPM_CUDA(h, cudaMemcpyAsync(ap.data(), h->d_ap + R.cell_off, sizeof(int2) * n1,
-                                cudaMemcpyDeviceToHost, h->stream));
+    std::vector<unsigned long long> ap(n1);
+    CPM_CUDA(h, cudaMemcpyAsync(ap.data(), h->d_ap[0] + R.cell_off,
+                                sizeof(unsigned long long) * n1, cudaMemcpyDeviceToHost,
+                                h->stream));
     CPM_CUDA(h, cudaStreamSynchronize(h->stream));
     for (long long c = 0; c < n1; ++c) {
-      if (area) area[c] = ap[c].x;
-      if (perimeter) perimeter[c] = ap[c].y;
+      if (area) area[c] = unpack_area(ap[c]);
+      if (perimeter) perimeter[c] = unpack_perim(ap[c]);
     }
   }
   if (centroid_sums) {
-    CPM_CUDA(h, cudaMemcpyAsync(centroid_sums, h->d_cs + R.cell_off * h->ndim,
+    CPM_CUDA(h, cudaMemcpyAsync(centroid_sums, h->d_cs[0] + R.cell_off * h->ndim,
                                 sizeof(long long) * n1 * h->ndim,
                                 cudaMemcpyDeviceToHost, h->stream));
     CPM_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -653,17 +685,18 @@ int cpm_get_centroids(cpm_handle* h, double* out, int capacity, int* n_out) {
   const DevReplica& R = h->reps[0];
   const int d = h->ndim;
   const int m = std::min(n, capacity);
-  std::vector<int2> ap(m);
+  std::vector<unsigned long long> ap(m);
   std::vector<long long> cs((size_t)m * d);
-  CPM_CUDA(h, cudaMemcpyAsync(ap.data(), h->d_ap + R.cell_off + 1, sizeof(int2) * m,
-                              cudaMemcpyDeviceToHost, h->stream));
-  CPM_CUDA(h, cudaMemcpyAsync(cs.data(), h->d_cs + (R.cell_off + 1) * d,
+  CPM_CUDA(h, cudaMemcpyAsync(ap.data(), h->d_ap[0] + R.cell_off + 1,
+                              sizeof(unsigned long long) * m, cudaMemcpyDeviceToHost,
+                              h->stream));
+  CPM_CUDA(h, cudaMemcpyAsync(cs.data(), h->d_cs[0] + (R.cell_off + 1) * d,
                               sizeof(long long) * m * d, cudaMemcpyDeviceToHost, h->stream));
   CPM_CUDA(h, cudaStreamSynchronize(h->stream));
   const int dims[3] = {R.nx, R.ny, R.nz};
   for (int c = 0; c < m; ++c)
     for (int k = 0; k < d; ++k) {
-      double v = (double)cs[(size_t)c * d + k] / (double)ap[c].x;
+      double v = (double)cs[(size_t)c * d + k] / (double)unpack_area(ap[c]);
       if (std::isfinite(v)) v -= dims[k] * std::floor(v / dims[k]);
       out[(size_t)c * d + k] = v;
     }

@@ -3,18 +3,25 @@
 //
 // Device memory layout of one engine (a batch of R replicas; a plain
 // gpucpm.Cpm is a batch of one):
-//   lat  : uint32  [sum_r sites_r]        replica r at reps[r].lat_off,
-//                                         row-major (z*ny + y)*nx + x
-//   ap   : int2    [sum_r (ncells_r+1)]   (area, perimeter), replica r's id
-//                                         c at row reps[r].cell_off + c
-//   cs   : int64   [rows * ndim]          exact centroid coordinate sums
-//   dap, dcs                              deltas of the running phase
-//   dflag: uint32  [rows]                 row is on the phase's dirty list
-//   dlist: uint32  [2 * rows]             two alternating dirty lists
-//   ctl  : uint32  [8]                    barrier counter, 2 dirty counts,
-//                                         sticky error bits
-// The tables are small next to the lattice (4096^2 at 100 sites per cell:
-// 67 MB of lattice, 4 MB of tables) and stay L2-resident through a run.
+//   lat    : uint32 [sum_r sites_r]      replica r at reps[r].lat_off,
+//                                        row-major (z*ny + y)*nx + x
+//   ap[2]  : uint64 [rows]               packed (area | perimeter << 32) of
+//                                        replica r's id c at row
+//                                        reps[r].cell_off + c; two copies
+//   cs[2]  : int64  [rows * ndim]        exact centroid coordinate sums,
+//                                        two copies
+//   dap[2], dcs[2]                       deltas of one phase (two phases in
+//                                        flight alternate)
+//   dflag[2]: uint32 [rows]              row is on a dirty list of a phase
+//   dlist  : uint32 [grid * 2 * list_cap] two dirty lists per sweep block
+//   ctl    : uint32 [64]                 barrier counter / release flag,
+//                                        sticky error bits
+// Table double buffering: phase k reads copy k % 2 and adds its deltas both
+// into the other copy and into dap/dcs[k % 2]; phase k + 1 replays those
+// deltas into copy k % 2, which missed them.  So every phase reads tables as
+// they stood when it began, with one grid barrier per phase.  The tables are
+// small next to the lattice (4096^2 at 100 sites per cell: 67 MB of lattice,
+// 4 MB per table copy) and stay L2-resident through a run.
 #pragma once
 
 #include <cstdint>
@@ -23,15 +30,31 @@
 namespace gpucpm {
 
 constexpr int kMaxTypes = 32;
-constexpr int kWarpsPerBlock = 8;
-constexpr int kSweepThreads = 32 * kWarpsPerBlock;
+constexpr int kSweepWarps = 24;  // warps per sweep block, one block per SM
+constexpr int kSweepThreads = 32 * kSweepWarps;
 constexpr int kInitThreads = 256;
 
-// ctl[] word indices
+// Warp tile: CX x CY x CZ targets of one slot, staged with their one-site
+// halo in the warp's own shared memory.  2D: 32 x 8 targets (66 x 17
+// sites); 3D: 32 x 2 x 2 targets (66 x 5 x 5 sites).
+template <int NDIM>
+struct TileGeom;
+template <>
+struct TileGeom<2> {
+  static constexpr int CX = 32, CY = 8, CZ = 1;
+};
+template <>
+struct TileGeom<3> {
+  static constexpr int CX = 32, CY = 2, CZ = 2;
+};
+
+// ctl[] word indices (the barrier counter and its release flag sit in
+// different 128-byte lines so that waiting blocks do not slow down arriving
+// ones)
 constexpr int kCtlBarrier = 0;
-constexpr int kCtlDirty0 = 1;  // dirty counts at kCtlDirty0 + (step & 1)
-constexpr int kCtlErr = 3;
-constexpr int kCtlWords = 8;
+constexpr int kCtlFlag = 32;
+constexpr int kCtlErr = 48;  // words [0, kCtlErr) are zeroed before a launch
+constexpr int kCtlWords = 64;
 
 // error bits in ctl[kCtlErr]
 constexpr int kErrTimeout = 1;      // a grid barrier waited too long
@@ -40,8 +63,8 @@ constexpr int kErrBadType = 4;      // type >= kMaxTypes
 constexpr int kErrMediumType = 8;   // id 0 with a non-zero type
 constexpr int kErrTypeConflict = 16;  // one id with two types
 
-// Per-replica parameters, kept in global memory and staged into shared
-// memory by each block for the replica it is working on.
+// Per-replica parameters, kept in global memory (read through the
+// read-only cache; a replica's few hundred used bytes stay L1-resident).
 struct DevParams {
   float J[kMaxTypes * kMaxTypes];  // J[own type][neighbour type]
   float lam_area[kMaxTypes];
@@ -59,21 +82,34 @@ struct DevReplica {
   long long cell_off;  // table row of the replica's id 0
 };
 
+// (area, perimeter) packed in one 64-bit word: area in the low 32 bits (it
+// never goes below zero), perimeter in the high 32 bits.  A signed 64-bit
+// addition of pack_delta(da, dp) updates both fields exactly.
+__host__ __device__ inline unsigned long long pack_delta(int da, int dp) {
+  return (unsigned long long)((long long)dp * 4294967296LL + (long long)da);
+}
+__host__ __device__ inline int unpack_area(unsigned long long w) {
+  return (int)(uint32_t)w;
+}
+__host__ __device__ inline int unpack_perim(unsigned long long w) {
+  return (int)(uint32_t)(w >> 32);
+}
+
 // Arguments of the persistent sweep kernel.
 struct SweepArgs {
   uint32_t* lat;
-  int2* ap;
-  long long* cs;
-  int2* dap;
-  long long* dcs;
-  uint32_t* dflag;
+  unsigned long long* ap[2];
+  long long* cs[2];
+  unsigned long long* dap[2];
+  long long* dcs[2];
+  uint32_t* dflag[2];
   uint32_t* dlist;
   uint32_t* ctl;
   unsigned long long* counters;  // [nrep][2]: evaluated, accepted
   const DevReplica* reps;
   const DevParams* params;
-  const int* task_prefix;  // [27][nrep + 1] block tasks per slot, prefix
-  long long rows;          // total table rows (dirty list capacity)
+  const int* task_prefix;  // [27][nrep + 1] warp tiles per slot, prefix
+  long long list_cap;      // entries of one dirty list of one block
   unsigned long long tick0;
   unsigned long long seed;
   int nrep;
@@ -84,13 +120,15 @@ struct SweepArgs {
 };
 
 // Launchers (cpm_kernels.cu).  Each returns the cudaError_t of its launch.
+cudaError_t sweep_prepare(int ndim, bool perim);
 cudaError_t launch_sweep(int ndim, bool perim, const SweepArgs& a, int grid,
                          cudaStream_t s);
 int sweep_max_blocks_per_sm(int ndim, bool perim);
+int sweep_tile_targets(int ndim);
 cudaError_t launch_barrier_probe(uint32_t* ctl, unsigned long long timeout_ns,
                                  cudaStream_t s);
 cudaError_t launch_init(int ndim, const uint32_t* lat, const DevReplica* reps,
-                        int nrep, long long total_sites, int2* ap,
+                        int nrep, long long total_sites, unsigned long long* ap,
                         long long* cs, unsigned long long* first, int* ctype,
                         uint32_t* ctl, cudaStream_t s);
 

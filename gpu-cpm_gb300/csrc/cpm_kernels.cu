@@ -15,17 +15,28 @@
 // and one MCS runs every non-empty slot in lexicographic (cz, cy, cx) order.
 // All targets of a slot are >= 2 apart on each axis, so an attempt never
 // reads a site another attempt of the same slot may write; the cell tables
-// are read as they stood when the slot began and the integer deltas of the
-// slot are folded in after a grid barrier.  The result is independent of
-// thread, block and replica order, which is what makes the CPU oracle
-// (oracle/cpm_oracle.cpp) reproduce it bit for bit.
+// are read as they stood when the slot began (double-buffered, see
+// cpm_internal.h) and the integer deltas are exact and order-free.  The
+// result is independent of thread, block and replica order, which is what
+// makes the CPU oracle (oracle/cpm_oracle.cpp) reproduce it bit for bit.
 //
-// Work decomposition.  A warp owns a segment of 32 consecutive targets of
-// one target row of one replica; a block task is kWarpsPerBlock segments of
-// one replica, so the block stages that replica's J / lambda / target tables
-// in shared memory once per task switch.  Block tasks of a slot are
-// flattened over replicas (prefix table per slot) and dealt out
-// grid-stride, which balances ragged batches by work, not by replica.
+// Work decomposition.  One block of kSweepWarps warps per SM, one grid
+// barrier per slot.  The unit of work is a warp tile: CX x CY (x CZ)
+// targets of one slot of one replica, staged with a one-site halo in the
+// warp's own shared memory (periodic wrap resolved while loading; even and
+// odd lattice columns kept in separate halves so that 32 consecutive
+// targets read 32 consecutive words).  A warp then works its tile in three
+// compacted passes, so lanes stay busy although most attempts end early:
+//   1. boundary test: a target whose Moore neighbours all carry its own id
+//      cannot change; the others are queued;
+//   2. Philox draw and source pick for the queued targets; attempts whose
+//      source id equals the target's are dropped, the rest are queued with
+//      their direction and uniform;
+//   3. dH, Metropolis test, lattice write and table deltas.
+// A warp never waits for another warp inside a slot, so the 24 warps of an
+// SM hide each other's load latencies.  Tiles of a slot are flattened over
+// replicas (prefix table per slot) and dealt out warp-strided over the
+// grid, which balances ragged batches by work.
 //
 // Memory.  Mutable data (lattice, tables, deltas, dirty lists) is read with
 // ld.global.cg so that no SM serves a stale L1 line after a barrier; the
@@ -36,6 +47,8 @@
 
 namespace gpucpm {
 namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
 
 __device__ __forceinline__ int find_task_replica(const int* pre, int nrep,
                                                  int task) {
@@ -65,228 +78,398 @@ __device__ __forceinline__ int find_site_replica(const DevReplica* reps,
   return lo;
 }
 
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// Shared-memory layout of a staged warp tile.  Logical column c of a staged
+// row lives at (c & 1) * HALF + (c >> 1): target columns (odd logical
+// columns) in the upper half, their left / right neighbours in the lower.
 template <int NDIM>
-__device__ __forceinline__ void add_delta(const SweepArgs& a, long long row,
-                                          int darea, int dperim,
-                                          const long long* img, int sign,
-                                          uint32_t* dlist, uint32_t* dcount) {
-  atomicAdd(&a.dap[row].x, darea);
-  atomicAdd(&a.dap[row].y, dperim);
+struct Stage {
+  using G = TileGeom<NDIM>;
+  static constexpr int HALF = G::CX + 1;
+  static constexpr int SXP = 2 * HALF;
+  static constexpr int SY = 2 * G::CY + 1;
+  static constexpr int SZ = NDIM == 3 ? 2 * G::CZ + 1 : 1;
+  static constexpr int WORDS = SXP * SY * SZ;
+  static constexpr int NT = G::CX * G::CY * G::CZ;
+  static constexpr int NB = NDIM == 2 ? 8 : 26;
+
+  // shared-memory index of target q's own site (qx = q % CX is the lane)
+  __device__ static __forceinline__ int center(int q) {
+    const int qx = q % G::CX, qy = (q / G::CX) % G::CY, qz = q / (G::CX * G::CY);
+    const int zz = NDIM == 3 ? 2 * qz + 1 : 0;
+    return (zz * SY + 2 * qy + 1) * SXP + HALF + qx;
+  }
+  // offset of neighbour (dz, dy, dx) from a target's own site
+  __host__ __device__ static constexpr int offset(int dz, int dy, int dx) {
+    return (dz * SY + dy) * SXP + (dx == 0 ? 0 : (dx < 0 ? -HALF : 1 - HALF));
+  }
+  // offset of the k-th neighbour in (dz, dy, dx) lexicographic order
+  __device__ static __forceinline__ int nb_offset(int k) {
+    if (NDIM == 2) {
+      const int m = k + (k >= 4);
+      return offset(0, m / 3 - 1, m % 3 - 1);
+    }
+    const int m = k + (k >= 13);
+    return offset(m / 9 - 1, (m / 3) % 3 - 1, m % 3 - 1);
+  }
+};
+
+template <int NDIM>
+struct WarpSmem {
+  uint2 qb[Stage<NDIM>::NT];                // (q | dir << 16, uniform word)
+  uint32_t tile[Stage<NDIM>::WORDS];
+  uint16_t qa[Stage<NDIM>::NT];
+};
+
+template <int NDIM>
+constexpr size_t sweep_smem_bytes() {
+  return sizeof(WarpSmem<NDIM>) * kSweepWarps;
+}
+
+// Per-phase view of the double-buffered tables.
+template <int NDIM>
+struct PhaseTables {
+  const unsigned long long* rap;  // read copy (tables at phase start)
+  const long long* rcs;
+  unsigned long long* wap;        // other copy: receives this phase's deltas
+  long long* wcs;
+  unsigned long long* dap;        // this phase's deltas (replayed next phase)
+  long long* dcs;
+  uint32_t* dflag;
+  uint32_t* list;                 // this block's dirty list for the phase
+  unsigned* cnt;                  // its length (shared memory)
+};
+
+// One accepted copy's change of one table row: added to the other table
+// copy and to the phase delta table.  The first block to touch the row in
+// the phase (dflag 0 -> 1) puts it on its own dirty list; that block
+// replays the row's delta into the read copy during the next phase.
+template <int NDIM>
+__device__ __forceinline__ void add_delta(const PhaseTables<NDIM>& pt,
+                                          long long row, int darea, int dperim,
+                                          const long long* img, long long sign) {
+  const unsigned long long pd = pack_delta(darea, dperim);
+  atomicAdd(pt.wap + row, pd);
+  atomicAdd(pt.dap + row, pd);
 #pragma unroll
-  for (int k = 0; k < NDIM; ++k)
-    atomicAdd(reinterpret_cast<unsigned long long*>(&a.dcs[row * NDIM + k]),
-              (unsigned long long)(sign * img[k]));
-  if (atomicExch(&a.dflag[row], 1u) == 0u) {
-    const uint32_t pos = atomicAdd(dcount, 1u);
-    dlist[pos] = (uint32_t)row;
+  for (int k = 0; k < NDIM; ++k) {
+    const unsigned long long v = (unsigned long long)(sign * img[k]);
+    atomicAdd(reinterpret_cast<unsigned long long*>(pt.wcs + row * NDIM + k), v);
+    atomicAdd(reinterpret_cast<unsigned long long*>(pt.dcs + row * NDIM + k), v);
+  }
+  if (atomicExch(pt.dflag + row, 1u) == 0u) {
+    const unsigned pos = atomicAdd(pt.cnt, 1u);
+    pt.list[pos] = (uint32_t)row;
+  }
+}
+
+// Replays the deltas of the rows on a block's dirty list into `ap`/`cs`
+// and clears them (delta, flag), strided over the block's threads.
+template <int NDIM>
+__device__ __forceinline__ void replay(const uint32_t* list, unsigned n,
+                                       unsigned long long* dap, long long* dcs,
+                                       uint32_t* dflag, unsigned long long* ap,
+                                       long long* cs) {
+  for (unsigned j = threadIdx.x; j < n; j += blockDim.x) {
+    const uint32_t row = __ldcg(list + j);
+    const unsigned long long d = __ldcg(dap + row);
+    if (d) atomicAdd(ap + row, d);
+    dap[row] = 0ull;
+#pragma unroll
+    for (int k = 0; k < NDIM; ++k) {
+      const long long idx = (long long)row * NDIM + k;
+      const long long dc = __ldcg(dcs + idx);
+      if (dc) atomicAdd(reinterpret_cast<unsigned long long*>(cs + idx),
+                        (unsigned long long)dc);
+      dcs[idx] = 0;
+    }
+    dflag[row] = 0u;
   }
 }
 
 template <int NDIM, bool PERIM>
-__global__ void __launch_bounds__(kSweepThreads)
+__global__ void __launch_bounds__(kSweepThreads, 1)
     sweep_kernel(const SweepArgs a) {
-  constexpr int NB = NDIM == 2 ? 8 : 26;
+  using G = TileGeom<NDIM>;
+  using S = Stage<NDIM>;
+  constexpr int NB = S::NB;
+  constexpr int NT = S::NT;
   constexpr unsigned long long NSLOTS = NDIM == 2 ? 9 : 27;
-  __shared__ DevParams sp;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_ok;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t k0 = (uint32_t)a.seed, k1 = (uint32_t)(a.seed >> 32);
-  const unsigned nblk = gridDim.x;
-  int* err = reinterpret_cast<int*>(&a.ctl[kCtlErr]);
-  int cur_rep = -1;
-  unsigned episode = 0;
-  int step = 0;
+  __shared__ unsigned s_cnt[2];
 
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  WarpSmem<NDIM>& ws = reinterpret_cast<WarpSmem<NDIM>*>(smem_raw)[warp];
+  const int gwarp = blockIdx.x * kSweepWarps + warp;
+  const int nwarps = gridDim.x * kSweepWarps;
+  const uint32_t k0 = (uint32_t)a.seed, k1 = (uint32_t)(a.seed >> 32);
+  int* err = reinterpret_cast<int*>(&a.ctl[kCtlErr]);
+  // (kernel-parameter arrays are selected with ?: rather than indexed with
+  // a runtime value, which would copy the parameter block to local memory)
+  auto blist = [&](int b) { return a.dlist + (2LL * blockIdx.x + b) * a.list_cap; };
+  unsigned episode = 0;
+  int cnt_rep = -1;
+  unsigned long long n_eval = 0, n_acc = 0;  // warp-uniform
+  if (tid < 2) s_cnt[tid] = 0;
+  __syncthreads();
+
+  int step = 0;
   for (int m = 0; m < a.mcs; ++m) {
     const unsigned long long tick = a.tick0 + (unsigned long long)m;
-    for (int si = 0; si < a.nslot_active; ++si) {
+    for (int si = 0; si < a.nslot_active; ++si, ++step) {
+      const int cur = step & 1, prv = cur ^ 1;
+      PhaseTables<NDIM> pt;
+      pt.rap = cur ? a.ap[1] : a.ap[0];
+      pt.rcs = cur ? a.cs[1] : a.cs[0];
+      pt.wap = cur ? a.ap[0] : a.ap[1];
+      pt.wcs = cur ? a.cs[0] : a.cs[1];
+      pt.dap = cur ? a.dap[1] : a.dap[0];
+      pt.dcs = cur ? a.dcs[1] : a.dcs[0];
+      pt.dflag = cur ? a.dflag[1] : a.dflag[0];
+      pt.list = blist(cur);
+      pt.cnt = &s_cnt[cur];
+
+      // Replay the previous phase's deltas into the copy that phase read.
+      if (step > 0)
+        replay<NDIM>(blist(prv), s_cnt[prv], cur ? a.dap[0] : a.dap[1],
+                     cur ? a.dcs[0] : a.dcs[1], cur ? a.dflag[0] : a.dflag[1],
+                     pt.wap, pt.wcs);
+
       const int slot = a.slots[si];
       const int cx = slot % 3, cy = (slot / 3) % 3, cz = slot / 9;
       const unsigned long long phase = tick * NSLOTS + (unsigned long long)slot;
       const int* pre = a.task_prefix + slot * (a.nrep + 1);
-      const int ntasks = __ldg(pre + a.nrep);
-      const int lst = step & 1;
-      uint32_t* dcount = &a.ctl[kCtlDirty0 + lst];
-      uint32_t* dlist = a.dlist + (long long)lst * a.rows;
+      const int ntiles = __ldg(pre + a.nrep);
 
-      for (int task = blockIdx.x; task < ntasks; task += gridDim.x) {
+      for (int task = gwarp; task < ntiles; task += nwarps) {
         const int r = find_task_replica(pre, a.nrep, task);
-        if (r != cur_rep) {  // block-uniform
-          __syncthreads();
-          const int* src = reinterpret_cast<const int*>(a.params + r);
-          int* dst = reinterpret_cast<int*>(&sp);
-          for (int i = threadIdx.x; i < (int)(sizeof(DevParams) / 4);
-               i += blockDim.x)
-            dst[i] = __ldg(src + i);
-          __syncthreads();
-          cur_rep = r;
+        if (r != cnt_rep) {
+          if (lane == 0 && cnt_rep >= 0) {
+            if (n_eval) atomicAdd(&a.counters[2 * cnt_rep], n_eval);
+            if (n_acc) atomicAdd(&a.counters[2 * cnt_rep + 1], n_acc);
+          }
+          n_eval = n_acc = 0;
+          cnt_rep = r;
         }
+        const DevParams* P = a.params + r;
         const int nx = __ldg(&a.reps[r].nx), ny = __ldg(&a.reps[r].ny),
                   nz = __ldg(&a.reps[r].nz), ncells = __ldg(&a.reps[r].ncells);
         const long long lat_off = __ldg(&a.reps[r].lat_off);
         const long long cell_off = __ldg(&a.reps[r].cell_off);
         const int ncx = class_count(nx, cx), ncy = class_count(ny, cy),
                   ncz = class_count(nz, cz);
-        const int spr = (ncx + 31) >> 5;
-        const long long nseg = (long long)ncy * ncz * spr;
-        const long long seg =
-            (long long)(task - __ldg(pre + r)) * kWarpsPerBlock + warp;
-        if (seg >= nseg) continue;  // warp-uniform
-
-        const int row = (int)(seg / spr);
-        const int i = (int)(seg - (long long)row * spr) * 32 + lane;
-        const bool valid = i < ncx;
-        const int x = class_coord(nx, cx, valid ? i : ncx - 1);
-        const int y = class_coord(ny, cy, row % ncy);
-        const int z = class_coord(nz, cz, row / ncy);
+        const int tnx = (ncx + G::CX - 1) / G::CX;
+        const int tny = (ncy + G::CY - 1) / G::CY;
+        const int local = task - __ldg(pre + r);
+        const int tx = local % tnx, rest = local / tnx;
+        const int ty = rest % tny, tz = rest / tny;
+        const int i0 = tx * G::CX, j0 = ty * G::CY, l0 = tz * G::CZ;
+        const int cntx = min(G::CX, ncx - i0), cnty = min(G::CY, ncy - j0),
+                  cntz = min(G::CZ, ncz - l0);
+        const int xorig = class_coord(nx, cx, i0) - 1;
+        const int yorig = class_coord(ny, cy, j0) - 1;
+        const int zorig = NDIM == 3 ? class_coord(nz, cz, l0) - 1 : 0;
+        const int ux = 2 * cntx + 1, uy = 2 * cnty + 1,
+                  uz = NDIM == 3 ? 2 * cntz + 1 : 1;
         uint32_t* L = a.lat + lat_off;
 
-        // Neighbourhood in (dz, dy, dx) lexicographic order, centre skipped.
-        const int xs[3] = {x == 0 ? nx - 1 : x - 1, x, x == nx - 1 ? 0 : x + 1};
-        const int ys[3] = {y == 0 ? ny - 1 : y - 1, y, y == ny - 1 ? 0 : y + 1};
-        int zs[3] = {0, 0, 0};
-        if (NDIM == 3) {
-          zs[0] = z == 0 ? nz - 1 : z - 1;
-          zs[1] = z;
-          zs[2] = z == nz - 1 ? 0 : z + 1;
+        // ---- stage the tile and its halo (periodic wrap applied here) ----
+        int gx[3];
+#pragma unroll
+        for (int u = 0; u < 3; ++u) {
+          int v = xorig + lane + 32 * u;
+          gx[u] = v < 0 ? v + nx : (v >= nx ? v - nx : v);
         }
-        uint32_t nb[NB];
-        {
-          int k = 0;
+        for (int zz = 0; zz < uz; ++zz) {
+          int gz = zorig + zz;
+          gz = gz < 0 ? gz + nz : (gz >= nz ? gz - nz : gz);
+#pragma unroll 4
+          for (int yy = 0; yy < uy; ++yy) {
+            int gy = yorig + yy;
+            gy = gy < 0 ? gy + ny : (gy >= ny ? gy - ny : gy);
+            const uint32_t* src = L + ((long long)gz * ny + gy) * nx;
+            uint32_t* dst = ws.tile + (zz * S::SY + yy) * S::SXP;
 #pragma unroll
-          for (int dz = (NDIM == 3 ? 0 : 1); dz < (NDIM == 3 ? 3 : 2); ++dz)
-#pragma unroll
-            for (int dy = 0; dy < 3; ++dy)
-#pragma unroll
-              for (int dx = 0; dx < 3; ++dx) {
-                if (dz == 1 && dy == 1 && dx == 1) continue;
-                nb[k++] = __ldcg(
-                    L + ((long long)zs[dz] * ny + ys[dy]) * nx + xs[dx]);
-              }
-        }
-        const long long site = ((long long)z * ny + y) * nx + x;
-        const uint32_t t = __ldcg(L + site);
-        bool boundary = false;
-#pragma unroll
-        for (int k = 0; k < NB; ++k) boundary |= nb[k] != t;
-
-        bool evaluated = false, accepted = false;
-        if (valid && boundary) {
-          uint32_t c0 = (uint32_t)site, c1 = (uint32_t)phase,
-                   c2 = a.stream0 + (uint32_t)r, c3 = (uint32_t)(phase >> 32);
-          philox4x32_10(c0, c1, c2, c3, k0, k1);
-          const int kdir = (int)__umulhi(c0, (unsigned)NB);
-          uint32_t s = nb[0];
-#pragma unroll
-          for (int k = 1; k < NB; ++k)
-            if (k == kdir) s = nb[k];
-          const uint32_t is = s & 0xFFFFFFu, it = t & 0xFFFFFFu;
-          if (s != t && (is > (uint32_t)ncells || it > (uint32_t)ncells)) {
-            atomicOr(err, kErrBadId);
-          } else if (s != t) {
-            evaluated = true;
-            const int ts = (int)(s >> 24) & (kMaxTypes - 1);
-            const int tt = (int)(t >> 24) & (kMaxTypes - 1);
-            float e_old = 0.0f, e_new = 0.0f;
-            int cnt_s = 0, cnt_t = 0;
-#pragma unroll
-            for (int k = 0; k < NB; ++k) {
-              const int tn = (int)(nb[k] >> 24) & (kMaxTypes - 1);
-              if (nb[k] != t) e_old = __fadd_rn(e_old, sp.J[tt * kMaxTypes + tn]);
-              if (nb[k] != s) e_new = __fadd_rn(e_new, sp.J[ts * kMaxTypes + tn]);
-              cnt_s += nb[k] == s;
-              cnt_t += nb[k] == t;
-            }
-            float dH = __fsub_rn(e_new, e_old);
-            const int dps = NB - 2 * cnt_s;
-            const int dpt = 2 * cnt_t - NB;
-            const long long rs = cell_off + is, rt = cell_off + it;
-            const int2 aps = s ? __ldcg(a.ap + rs) : make_int2(0, 0);
-            const int2 apt = t ? __ldcg(a.ap + rt) : make_int2(0, 0);
-            if (PERIM && sp.perim_on) {
-              if (s) {
-                const long long q =
-                    (long long)dps * (2LL * (aps.y - sp.tgt_perim[ts]) + dps);
-                dH = __fmaf_rn(sp.lam_perim[ts], __ll2float_rn(q), dH);
-              }
-              if (t) {
-                const long long q =
-                    (long long)dpt * (2LL * (apt.y - sp.tgt_perim[tt]) + dpt);
-                dH = __fmaf_rn(sp.lam_perim[tt], __ll2float_rn(q), dH);
-              }
-            }
-            if (s) {
-              const long long q = 1 + 2LL * (aps.x - sp.tgt_area[ts]);
-              dH = __fmaf_rn(sp.lam_area[ts], __ll2float_rn(q), dH);
-            }
-            if (t) {
-              const long long q = 1 - 2LL * (apt.x - sp.tgt_area[tt]);
-              dH = __fmaf_rn(sp.lam_area[tt], __ll2float_rn(q), dH);
-            }
-            const float T = sp.temperature;
-            bool ok;
-            if (dH < 0.0f) {
-              ok = true;
-            } else if (!(T > 0.0f)) {
-              ok = false;
-            } else {
-              const float u = __fmul_rn(__uint2float_rn((c1 >> 8) | 1u), 0x1p-24f);
-              ok = u < exp_neg(__fdiv_rn(-dH, T));
-            }
-            if (ok) {
-              accepted = true;
-              L[site] = s;
-              const int crd[3] = {x, y, z};
-              const int dim[3] = {nx, ny, nz};
-              long long img[NDIM];
-              if (s) {
-#pragma unroll
-                for (int k = 0; k < NDIM; ++k)
-                  img[k] = nearest_image(crd[k], dim[k], aps.x,
-                                         __ldcg(a.cs + rs * NDIM + k));
-                add_delta<NDIM>(a, rs, 1, dps, img, 1, dlist, dcount);
-              }
-              if (t) {
-#pragma unroll
-                for (int k = 0; k < NDIM; ++k)
-                  img[k] = nearest_image(crd[k], dim[k], apt.x,
-                                         __ldcg(a.cs + rt * NDIM + k));
-                add_delta<NDIM>(a, rt, -1, dpt, img, -1, dlist, dcount);
-              }
+            for (int u = 0; u < 3; ++u) {
+              const int c = lane + 32 * u;
+              if (c < ux) dst[(c & 1) * S::HALF + (c >> 1)] = __ldcg(src + gx[u]);
             }
           }
         }
-        const unsigned be = __ballot_sync(0xffffffffu, evaluated);
-        const unsigned ba = __ballot_sync(0xffffffffu, accepted);
-        if (lane == 0 && be) {
-          atomicAdd(&a.counters[2 * r], (unsigned long long)__popc(be));
-          if (ba) atomicAdd(&a.counters[2 * r + 1], (unsigned long long)__popc(ba));
+        __syncwarp();
+
+        // ---- pass 1: boundary test ---------------------------------------
+        int na = 0;
+#pragma unroll
+        for (int it = 0; it < NT / 32; ++it) {
+          const int q = it * 32 + lane;
+          const int qy = it % G::CY, qz = it / G::CY;
+          bool bnd = false;
+          if (lane < cntx && qy < cnty && qz < cntz) {
+            const int c = S::center(q);
+            const uint32_t t = ws.tile[c];
+#pragma unroll
+            for (int k = 0; k < NB; ++k) bnd |= ws.tile[c + S::nb_offset(k)] != t;
+          }
+          const unsigned ball = __ballot_sync(kFull, bnd);
+          if (bnd) ws.qa[na + __popc(ball & lanemask_lt())] = (uint16_t)q;
+          na += __popc(ball);
         }
+        __syncwarp();
+
+        // ---- pass 2: random draw and source pick -------------------------
+        int nb = 0;
+        for (int base = 0; base < na; base += 32) {
+          const int j = base + lane;
+          bool keep = false;
+          uint2 entry = make_uint2(0u, 0u);
+          if (j < na) {
+            const int q = ws.qa[j];
+            const int qx = q % G::CX, qy = (q / G::CX) % G::CY,
+                      qz = q / (G::CX * G::CY);
+            const int x = class_coord(nx, cx, i0 + qx);
+            const int y = class_coord(ny, cy, j0 + qy);
+            const int z = NDIM == 3 ? class_coord(nz, cz, l0 + qz) : 0;
+            const long long site = ((long long)z * ny + y) * nx + x;
+            uint32_t c0 = (uint32_t)site, c1 = (uint32_t)phase,
+                     c2 = a.stream0 + (uint32_t)r, c3 = (uint32_t)(phase >> 32);
+            philox4x32_10(c0, c1, c2, c3, k0, k1);
+            const int kdir = (int)__umulhi(c0, (unsigned)NB);
+            const int c = S::center(q);
+            keep = ws.tile[c + S::nb_offset(kdir)] != ws.tile[c];
+            entry = make_uint2((uint32_t)q | ((uint32_t)kdir << 16), c1);
+          }
+          const unsigned ball = __ballot_sync(kFull, keep);
+          if (keep) ws.qb[nb + __popc(ball & lanemask_lt())] = entry;
+          nb += __popc(ball);
+        }
+        __syncwarp();
+
+        // ---- pass 3: dH, Metropolis test, commit -------------------------
+        for (int base = 0; base < nb; base += 32) {
+          const int j = base + lane;
+          bool accepted = false;
+          if (j < nb) {
+            const uint2 entry = ws.qb[j];
+            const int q = (int)(entry.x & 0xFFFFu), kdir = (int)(entry.x >> 16);
+            const int c = S::center(q);
+            const uint32_t t = ws.tile[c];
+            const uint32_t s = ws.tile[c + S::nb_offset(kdir)];
+            const uint32_t is = s & 0xFFFFFFu, it = t & 0xFFFFFFu;
+            if (is > (uint32_t)ncells || it > (uint32_t)ncells) {
+              atomicOr(err, kErrBadId);
+            } else {
+              const int ts = (int)(s >> 24) & (kMaxTypes - 1);
+              const int tt = (int)(t >> 24) & (kMaxTypes - 1);
+              const long long rs = cell_off + is, rt = cell_off + it;
+              const unsigned long long aps = s ? __ldcg(pt.rap + rs) : 0ull;
+              const unsigned long long apt = t ? __ldcg(pt.rap + rt) : 0ull;
+              float e_old = 0.0f, e_new = 0.0f;
+              int cnt_s = 0, cnt_t = 0;
+#pragma unroll
+              for (int k = 0; k < NB; ++k) {
+                const uint32_t v = ws.tile[c + S::nb_offset(k)];
+                const int tn = (int)(v >> 24) & (kMaxTypes - 1);
+                if (v != t) e_old = __fadd_rn(e_old, __ldg(&P->J[tt * kMaxTypes + tn]));
+                if (v != s) e_new = __fadd_rn(e_new, __ldg(&P->J[ts * kMaxTypes + tn]));
+                cnt_s += v == s;
+                cnt_t += v == t;
+              }
+              float dH = __fsub_rn(e_new, e_old);
+              const int dps = NB - 2 * cnt_s;
+              const int dpt = 2 * cnt_t - NB;
+              if (PERIM && __ldg(&P->perim_on)) {
+                if (s) {
+                  const long long qv = (long long)dps *
+                      (2LL * (unpack_perim(aps) - __ldg(&P->tgt_perim[ts])) + dps);
+                  dH = __fmaf_rn(__ldg(&P->lam_perim[ts]), __ll2float_rn(qv), dH);
+                }
+                if (t) {
+                  const long long qv = (long long)dpt *
+                      (2LL * (unpack_perim(apt) - __ldg(&P->tgt_perim[tt])) + dpt);
+                  dH = __fmaf_rn(__ldg(&P->lam_perim[tt]), __ll2float_rn(qv), dH);
+                }
+              }
+              if (s) {
+                const long long qv =
+                    1 + 2LL * (unpack_area(aps) - __ldg(&P->tgt_area[ts]));
+                dH = __fmaf_rn(__ldg(&P->lam_area[ts]), __ll2float_rn(qv), dH);
+              }
+              if (t) {
+                const long long qv =
+                    1 - 2LL * (unpack_area(apt) - __ldg(&P->tgt_area[tt]));
+                dH = __fmaf_rn(__ldg(&P->lam_area[tt]), __ll2float_rn(qv), dH);
+              }
+              const float T = __ldg(&P->temperature);
+              bool ok;
+              if (dH < 0.0f) {
+                ok = true;
+              } else if (!(T > 0.0f)) {
+                ok = false;
+              } else {
+                const float u =
+                    __fmul_rn(__uint2float_rn((entry.y >> 8) | 1u), 0x1p-24f);
+                ok = u < exp_neg(__fdiv_rn(-dH, T));
+              }
+              if (ok) {
+                accepted = true;
+                const int qx = q % G::CX, qy = (q / G::CX) % G::CY,
+                          qz = q / (G::CX * G::CY);
+                const int x = class_coord(nx, cx, i0 + qx);
+                const int y = class_coord(ny, cy, j0 + qy);
+                const int z = NDIM == 3 ? class_coord(nz, cz, l0 + qz) : 0;
+                L[((long long)z * ny + y) * nx + x] = s;
+                const int crd[3] = {x, y, z};
+                const int dim[3] = {nx, ny, nz};
+                long long img[NDIM];
+                if (s) {
+#pragma unroll
+                  for (int k = 0; k < NDIM; ++k)
+                    img[k] = nearest_image(crd[k], dim[k], unpack_area(aps),
+                                           __ldcg(pt.rcs + rs * NDIM + k));
+                  add_delta<NDIM>(pt, rs, 1, dps, img, 1);
+                }
+                if (t) {
+#pragma unroll
+                  for (int k = 0; k < NDIM; ++k)
+                    img[k] = nearest_image(crd[k], dim[k], unpack_area(apt),
+                                           __ldcg(pt.rcs + rt * NDIM + k));
+                  add_delta<NDIM>(pt, rt, -1, dpt, img, -1);
+                }
+              }
+            }
+          }
+          n_acc += __popc(__ballot_sync(kFull, accepted));
+        }
+        n_eval += nb;
+        __syncwarp();  // the tile buffers are rewritten by the next tile
       }
 
-      // All attempts of the slot have read the tables: fold the deltas.
-      if (!grid_barrier(a.ctl, nblk * ++episode, &s_ok)) return;
-      const uint32_t n = __ldcg(dcount);
-      for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n;
-           j += gridDim.x * blockDim.x) {
-        const uint32_t row = __ldcg(dlist + j);
-        const int2 d = __ldcg(a.dap + row);
-        const int2 v = __ldcg(a.ap + row);
-        a.ap[row] = make_int2(v.x + d.x, v.y + d.y);
-        a.dap[row] = make_int2(0, 0);
-#pragma unroll
-        for (int k = 0; k < NDIM; ++k) {
-          const long long idx = (long long)row * NDIM + k;
-          a.cs[idx] = __ldcg(a.cs + idx) + __ldcg(a.dcs + idx);
-          a.dcs[idx] = 0;
-        }
-        a.dflag[row] = 0u;
-      }
-      if (blockIdx.x == 0 && threadIdx.x == 0)
-        a.ctl[kCtlDirty0 + (lst ^ 1)] = 0u;
-      if (!grid_barrier(a.ctl, nblk * ++episode, &s_ok)) return;
-      ++step;
+      // The replayed list is consumed; every attempt of the slot is done
+      // once all blocks pass the barrier.
+      __syncthreads();
+      if (tid == 0) s_cnt[prv] = 0;
+      if (!grid_barrier(a.ctl, ++episode, &s_ok)) return;
     }
+  }
+
+  // Final replay: the last phase's deltas into the copy it read, so that
+  // both copies agree when the kernel ends.
+  if (step > 0) {
+    const int last = (step - 1) & 1;
+    replay<NDIM>(blist(last), s_cnt[last], last ? a.dap[1] : a.dap[0],
+                 last ? a.dcs[1] : a.dcs[0], last ? a.dflag[1] : a.dflag[0],
+                 last ? a.ap[1] : a.ap[0], last ? a.cs[1] : a.cs[0]);
+  }
+  if (lane == 0 && cnt_rep >= 0) {
+    if (n_eval) atomicAdd(&a.counters[2 * cnt_rep], n_eval);
+    if (n_acc) atomicAdd(&a.counters[2 * cnt_rep + 1], n_acc);
   }
 }
 
@@ -325,8 +508,8 @@ template <int NDIM>
 __global__ void __launch_bounds__(kInitThreads)
     init_pass2(const uint32_t* __restrict__ lat,
                const DevReplica* __restrict__ reps, int nrep, long long total,
-               const unsigned long long* __restrict__ first, int2* ap,
-               long long* cs) {
+               const unsigned long long* __restrict__ first,
+               unsigned long long* ap, long long* cs) {
   for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
        g < total; g += (long long)gridDim.x * blockDim.x) {
     const int r = find_site_replica(reps, nrep, g);
@@ -354,8 +537,7 @@ __global__ void __launch_bounds__(kInitThreads)
           foreign += L[((long long)zz * R.ny + yy) * R.nx + xx] != v;
         }
     const long long row = R.cell_off + id;
-    atomicAdd(&ap[row].x, 1);
-    atomicAdd(&ap[row].y, foreign);
+    atomicAdd(ap + row, pack_delta(1, foreign));
     const long long f = (long long)first[row];
     const int anchor[3] = {(int)(f % R.nx), (int)((f / R.nx) % R.ny),
                            (int)(f / ((long long)R.nx * R.ny))};
@@ -368,12 +550,12 @@ __global__ void __launch_bounds__(kInitThreads)
   }
 }
 
-// Failure-detection probe: every block waits at a barrier that needs one
-// block more than the grid has, so the bounded wait runs out and the error
-// word records kErrTimeout.  No memory beyond ctl[] is touched.
+// Failure-detection probe: every block waits at a barrier episode that
+// needs twice the blocks the grid has, so the bounded wait runs out and the
+// error word records kErrTimeout.  No memory beyond ctl[] is touched.
 __global__ void barrier_probe(uint32_t* ctl, unsigned long long timeout_ns) {
   __shared__ int s_ok;
-  grid_barrier(ctl, gridDim.x + 1, &s_ok, timeout_ns);
+  grid_barrier(ctl, 2u, &s_ok, timeout_ns);
 }
 
 const void* sweep_fn(int ndim, bool perim) {
@@ -384,22 +566,37 @@ const void* sweep_fn(int ndim, bool perim) {
                : (const void*)sweep_kernel<3, false>;
 }
 
+size_t sweep_smem(int ndim) {
+  return ndim == 2 ? sweep_smem_bytes<2>() : sweep_smem_bytes<3>();
+}
+
 }  // namespace
+
+cudaError_t sweep_prepare(int ndim, bool perim) {
+  return cudaFuncSetAttribute(sweep_fn(ndim, perim),
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)sweep_smem(ndim));
+}
 
 int sweep_max_blocks_per_sm(int ndim, bool perim) {
   int n = 0;
+  if (sweep_prepare(ndim, perim) != cudaSuccess) return 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sweep_fn(ndim, perim),
-                                                    kSweepThreads, 0) !=
-      cudaSuccess)
+                                                    kSweepThreads,
+                                                    sweep_smem(ndim)) != cudaSuccess)
     return 0;
   return n;
+}
+
+int sweep_tile_targets(int ndim) {
+  return ndim == 2 ? Stage<2>::NT : Stage<3>::NT;
 }
 
 cudaError_t launch_sweep(int ndim, bool perim, const SweepArgs& a, int grid,
                          cudaStream_t s) {
   void* args[] = {const_cast<SweepArgs*>(&a)};
   return cudaLaunchCooperativeKernel(sweep_fn(ndim, perim), dim3(grid),
-                                     dim3(kSweepThreads), args, 0, s);
+                                     dim3(kSweepThreads), args, sweep_smem(ndim), s);
 }
 
 cudaError_t launch_barrier_probe(uint32_t* ctl, unsigned long long timeout_ns,
@@ -410,7 +607,7 @@ cudaError_t launch_barrier_probe(uint32_t* ctl, unsigned long long timeout_ns,
 }
 
 cudaError_t launch_init(int ndim, const uint32_t* lat, const DevReplica* reps,
-                        int nrep, long long total_sites, int2* ap,
+                        int nrep, long long total_sites, unsigned long long* ap,
                         long long* cs, unsigned long long* first, int* ctype,
                         uint32_t* ctl, cudaStream_t s) {
   int dev = 0, sms = 0;
