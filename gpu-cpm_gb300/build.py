@@ -21,7 +21,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "--fmad=false",
            "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
            f"-I{INCLUDE}", f"-I{CSRC}"]
-SOURCES = ["cpm_engine.cu", "cpm_kernels.cu"]
+SOURCES = ["cpm_engine.cu", "cpm_kernels.cu", "cpm_static.cu"]
 HEADERS = ["cpm_internal.h", "cpm_device.cuh"]
 
 

@@ -36,6 +36,8 @@ constexpr int kMaxMcsPerLaunch = 1 << 16;
 
 }  // namespace
 
+void gpucpm::set_thread_error(const char* message) { g_create_error = message; }
+
 struct cpm_handle {
   int ndim = 2;
   int nrep = 0;

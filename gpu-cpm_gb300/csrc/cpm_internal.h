@@ -119,6 +119,9 @@ struct SweepArgs {
   int slots[27];
 };
 
+// Message returned by cpm_last_error(NULL) for calls without a handle.
+void set_thread_error(const char* message);
+
 // Launchers (cpm_kernels.cu).  Each returns the cudaError_t of its launch.
 cudaError_t sweep_prepare(int ndim, bool perim);
 cudaError_t launch_sweep(int ndim, bool perim, const SweepArgs& a, int grid,

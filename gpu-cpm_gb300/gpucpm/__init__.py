@@ -55,6 +55,16 @@ class _Counters(ctypes.Structure):
                 ("accepted", ctypes.c_uint64)]
 
 
+class StaticParams(ctypes.Structure):
+    """cpm_static_params of include/gpucpm.h (parameters of sweep_static)."""
+    _fields_ = [("J", ctypes.c_float * (MAX_TYPES * MAX_TYPES)),
+                ("lambda_area", ctypes.c_float * MAX_TYPES),
+                ("target_area", ctypes.c_int * MAX_TYPES),
+                ("lambda_perimeter", ctypes.c_float * MAX_TYPES),
+                ("target_perimeter", ctypes.c_int * MAX_TYPES),
+                ("temperature", ctypes.c_float)]
+
+
 _lib = None
 
 
@@ -114,6 +124,10 @@ def library():
         fn = getattr(L, name)
         fn.argtypes = args
         fn.restype = ctypes.c_int
+    L.cpm_sweep_static.argtypes = [ctypes.c_int] * 5 + [ctypes.c_void_p] * 4 + [
+        ctypes.c_int, ctypes.POINTER(StaticParams), ctypes.c_uint64, ctypes.c_uint32,
+        ctypes.c_uint64, ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]
+    L.cpm_sweep_static.restype = ctypes.c_int
     L.cpm_set_device.argtypes = [ctypes.c_int]
     L.cpm_set_device.restype = ctypes.c_int
     L.cpm_debug_barrier_timeout.argtypes = [ctypes.c_uint64, ip]
@@ -393,6 +407,30 @@ class Batch(_Engine):
     def set_adhesion(self, replica, cell_type, other, J, symmetric=True):
         self._call("cpm_set_adhesion_r", int(replica), int(cell_type), int(other), float(J),
                    1 if symmetric else 0)
+
+
+def sweep_static(dimensionality, shape, number_of_cells, lattice_ptr, area_ptr,
+                 perimeter_ptr, centroid_sums_ptr, params, seed=0, stream_id=0,
+                 tick=0, mcs=1, recount=False, stream=None):
+    """Run `mcs` MCS on caller-owned device buffers without allocating.
+
+    For callers that cannot allocate device memory (a framework-owned memory
+    pool, a loop that must not allocate after start-up): the lattice and the
+    tables are device pointers the caller owns, all other working memory is a
+    fixed array inside the library (see cpm_sweep_static in
+    include/gpucpm.h for the size limits).  `shape` is (nx, ny) or
+    (nx, ny, nz); `params` a StaticParams.  Returns (evaluated, accepted).
+    Synchronous; calls must not overlap on the GPU.
+    """
+    nx, ny = int(shape[0]), int(shape[1])
+    nz = int(shape[2]) if dimensionality == 3 else 1
+    c = (ctypes.c_uint64 * 2)()
+    _check(library().cpm_sweep_static(
+        int(dimensionality), nx, ny, nz, int(number_of_cells), lattice_ptr, area_ptr,
+        perimeter_ptr, centroid_sums_ptr, 1 if recount else 0, ctypes.byref(params),
+        int(seed), int(stream_id), int(tick), int(mcs),
+        ctypes.c_void_p(int(stream) if stream else None), c), None)
+    return int(c[0]), int(c[1])
 
 
 def set_device(device):

@@ -195,6 +195,59 @@ int cpm_reset_counters(cpm_handle* h);
 int cpm_info(const cpm_handle* h, int* n_replicas, int* dimensionality,
              int* sweep_grid, uint64_t* kernel_launches);
 
+/* ---- sweep without allocation ------------------------------------------ */
+
+/* Size limits of cpm_sweep_static (its working memory is a fixed array). */
+#define CPM_STATIC_MAX_SITES (1 << 18)
+#define CPM_STATIC_MAX_CELLS 16383
+
+/* Parameters of cpm_sweep_static, in the conventions of the setters above:
+ * J[a * CPM_MAX_TYPES + b] is the adhesion a site of type a feels from a
+ * neighbour of type b; index 0 of the per-type arrays is the medium. */
+typedef struct {
+    float J[CPM_MAX_TYPES * CPM_MAX_TYPES];
+    float lambda_area[CPM_MAX_TYPES];
+    int target_area[CPM_MAX_TYPES];
+    float lambda_perimeter[CPM_MAX_TYPES];
+    int target_perimeter[CPM_MAX_TYPES];
+    float temperature;
+} cpm_static_params;
+
+/* No counterpart in the reference.  Runs `mcs` Monte Carlo steps of the same
+ * sweep as cpm_run on one lattice that lives entirely in caller-owned device
+ * memory, and allocates nothing: no cudaMalloc, no cudaFree, no handle.  It
+ * is meant for callers that cannot allocate device memory themselves: code
+ * running inside a framework that owns the device memory pool, a pre-sized
+ * real-time or embedded loop that must not allocate after start-up, or a
+ * host that hands this library fixed buffers only.
+ *
+ * Buffers (device pointers, all in/out): lattice[nx*ny*nz] (id | type << 24,
+ * row-major), area[n+1], perimeter[n+1], centroid_sums[(n+1)*dimensionality]
+ * with n = number_of_cells.  With recount != 0 the tables are first
+ * recomputed from the lattice (their input contents are ignored); with
+ * recount == 0 they must describe the lattice, e.g. as left by an earlier
+ * call.  Random stream and time as in cpm_set_seed / cpm_set_tick: the
+ * result equals a handle's cpm_run from tick `tick` with the same seed and
+ * stream id.
+ *
+ * Working memory is one fixed array compiled into the library (about 6.5 MB,
+ * held on every GPU that loads the library until the process exits), which
+ * bounds the sizes: nx*ny*nz <= CPM_STATIC_MAX_SITES and number_of_cells <=
+ * CPM_STATIC_MAX_CELLS; larger requests fail with CPM_ERR_INVALID before any
+ * GPU work.  The first call on a device looks the array's address up on
+ * that device (make that call before capturing a CUDA graph on it).  Every
+ * call shares the one array: calls must not overlap on the GPU (two host
+ * threads calling at once on different streams would race).  The call works
+ * on `stream` (NULL: the default stream) and returns after that work has
+ * finished, with the status of the sweep; counters_out, if not NULL,
+ * receives {evaluated, accepted} of this call. */
+int cpm_sweep_static(int dimensionality, int nx, int ny, int nz,
+                     int number_of_cells, uint32_t* lattice, int32_t* area,
+                     int32_t* perimeter, int64_t* centroid_sums, int recount,
+                     const cpm_static_params* params, uint64_t seed,
+                     uint32_t stream_id, uint64_t tick, int mcs, void* stream,
+                     uint64_t* counters_out);
+
 /* ---- diagnostics ------------------------------------------------------ */
 
 /* Failure-detection self-test: launches a two-block cooperative kernel whose
