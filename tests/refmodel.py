@@ -1,0 +1,120 @@
+"""Python restatement of the reference's sequential copy-attempt algorithm.
+
+Used by the tests to pin the engine's semantics against the reference's own
+outputs.  With one thread (threads_per_block = 1, positions_per_thread =
+positions_per_checkerboard = D) the reference sweep src/kernels2d.cu:44-583
+is an ordinary sequential Cellular Potts model driven by its Park-Miller
+generator, and therefore deterministic for a given seed.  `sequential_run`
+repeats that run step by step:
+  seed mixing          src/kernels2d.cu:99
+  site pick            :199-202 (a = r % ppc, b = r % ppc)
+  neighbour pick       :232-241 and src/random.cu:22-28 (dx = r % 3 - 1,
+                       wrap with & (D - 1), redraw while it is the site)
+  dH                   :346-519 via reference_dh()
+  Metropolis test      :522-525 (r = seed / (2^31 - 1))
+  commit + tables      :548-569
+"""
+import math
+
+import numpy as np
+
+M = 2147483647
+
+
+def next_random(seed):
+    """Park-Miller step of src/random.cu:5-12 (exact in integers)."""
+    return (seed * 16807) % M
+
+
+def reference_dh(lat, ax, ay, sx, sy, area, perim, J, lam_a, tgt_a, lam_p, tgt_p,
+                 perimeter_on=True):
+    """dH of copying (sx, sy) into (ax, ay) as src/kernels2d.cu:346-519
+    computes it: integer adhesion sums, double lambda terms."""
+    n = lat.shape[0]
+    s, t = int(lat[sy, sx]), int(lat[ay, ax])
+    ts, tt = s >> 24, t >> 24
+    e_old = e_new = 0
+    ops = nps = opt = npt = 0
+    for j in (-1, 0, 1):
+        for i in (-1, 0, 1):
+            if i == 0 and j == 0:
+                continue
+            v = int(lat[(ay + j) % n, (ax + i) % n])
+            tv = v >> 24
+            if t != v:
+                e_old += J[tt][tv]
+            if s != v:
+                e_new += J[ts][tv]
+            ops += v == s
+            nps += v != s
+            opt += v != t
+            npt += v == t
+    e = float(e_new - e_old)
+    if perimeter_on:
+        if s:
+            P = int(perim[s & 0xFFFFFF])
+            Pn = P - ops + nps
+            e += lam_p[ts] * ((Pn - tgt_p[ts]) ** 2 - (P - tgt_p[ts]) ** 2)
+        if t:
+            P = int(perim[t & 0xFFFFFF])
+            Pn = P - opt + npt
+            e += lam_p[tt] * ((Pn - tgt_p[tt]) ** 2 - (P - tgt_p[tt]) ** 2)
+    if s:
+        e += lam_a[ts] * (1 + 2 * int(area[s & 0xFFFFFF]) - 2 * tgt_a[ts])
+    if t:
+        e += lam_a[tt] * (1 - 2 * int(area[t & 0xFFFFFF]) + 2 * tgt_a[tt])
+    return e, (nps - ops), (npt - opt)
+
+
+def sequential_run(lat, area, perim, J, lam_a, tgt_a, lam_p, tgt_p, T, seed, mcs,
+                   perimeter_on=True):
+    """The reference's one-thread run (in place); returns the accept count."""
+    D = lat.shape[0]
+    seed = next_random(0 + seed)  # calculateIndex(0, 0) + seed
+    accepted = 0
+    for _ in range(mcs):
+        for _ in range(D * D):
+            seed = next_random(seed)
+            x = seed % D
+            seed = next_random(seed)
+            y = seed % D
+            while True:
+                seed = next_random(seed)
+                nx = (x + seed % 3 - 1) & (D - 1)
+                seed = next_random(seed)
+                ny = (y + seed % 3 - 1) & (D - 1)
+                if not (nx == x and ny == y):
+                    break
+            s, t = int(lat[y, x]), int(lat[ny, nx])
+            if s == t:
+                continue
+            dH, dps, dpt = reference_dh(lat, nx, ny, x, y, area, perim, J, lam_a, tgt_a,
+                                        lam_p, tgt_p, perimeter_on)
+            e = np.float32(dH)
+            seed = next_random(seed)
+            r = np.float32(seed / M)
+            if e < 0 or (T > 0 and r < np.float32(math.exp(-float(e) / T))):
+                lat[ny, nx] = s
+                accepted += 1
+                if s:
+                    area[s & 0xFFFFFF] += 1
+                    if perimeter_on:
+                        perim[s & 0xFFFFFF] += dps
+                if t:
+                    area[t & 0xFFFFFF] -= 1
+                    if perimeter_on:
+                        perim[t & 0xFFFFFF] += dpt
+    return accepted
+
+
+def heterotypic_fraction(lat):
+    """Fraction of Moore-8 neighbour pairs of two different non-medium cells
+    whose types differ (the sorting order parameter)."""
+    lat = np.asarray(lat).astype(np.int64)
+    hetero = total = 0
+    for dy, dx in ((0, 1), (1, -1), (1, 0), (1, 1)):
+        nb = np.roll(np.roll(lat, -dy, 0), -dx, 1)
+        both = ((lat & 0xFFFFFF) != 0) & ((nb & 0xFFFFFF) != 0) & (lat != nb)
+        total += int(both.sum())
+        hetero += int((both & ((lat >> 24) != (nb >> 24))).sum())
+    return hetero / max(total, 1)

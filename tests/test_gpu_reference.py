@@ -1,0 +1,171 @@
+"""Parity with the reference's own CUDA build (oracle/_ref, built from the
+reference sources by oracle/ref_gpu/build.py and driven by ref_driver.cpp).
+
+1. Table recount: the reference's calculateAreasAndCircumferences and this
+   engine's push compute identical area and perimeter tables.
+2. A one-thread reference run (deterministic for a given seed) equals
+   tests/refmodel.py's restatement of the reference's sequential algorithm,
+   bit for bit.  That restatement's dH is the one tests/test_oracle.py
+   replays against the oracle, so the oracle's dH is pinned to the
+   reference's outputs through it.
+3. Statistics of the sorting workload after 1000 MCS (the reference's own
+   example geometry, racy updates and Park-Miller draws, against this
+   engine's deterministic schedule): mean area, area spread, perimeter,
+   surviving cells, heterotypic boundary fraction and site activity agree
+   within the tolerances below.
+"""
+import json
+import pathlib
+
+import numpy as np
+import pytest
+
+import refmodel
+from gpucpm import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+ref_gpu = pytest.importorskip("oracle.ref_gpu")
+if not ref_gpu.available():
+    pytest.skip("reference cubin not built (needs the reference checkout)",
+                allow_module_level=True)
+
+REPORT = pathlib.Path(__file__).resolve().parents[1] / "gpurun_out"
+
+
+def _ours(w, seed=0, stream=0):
+    import gpucpm
+    n = w.lattice.shape[0]
+    e = gpucpm.Cpm(n, w.ndim, w.ncells, w.temperature, False)
+    e.get_state()[...] = w.lattice.view(np.int32)
+    w.apply(e)
+    e.set_seed(seed, stream)
+    e.push_to_gpu()
+    return e
+
+
+def _ref(w):
+    r = ref_gpu.RefGpu(w.lattice.shape[0], w.ndim, w.ncells, w.temperature)
+    r.apply(w)
+    r.push(w.lattice)
+    return r
+
+
+@pytest.mark.parametrize("case", ["sorting256", "tissue2d", "tissue3d"])
+def test_table_recount_matches_reference(engine_lib, case):
+    if case == "sorting256":
+        w = W.sorting_2d(n=256, ncells=655)
+    elif case == "tissue2d":
+        w = W.tissue_2d(n=512, area=100)
+    else:
+        w = W.tissue_3d(n=64, volume=500)
+    ours = _ours(w)
+    area, perim, _ = ours.tables()
+    ra, rp = _ref(w).tables()
+    np.testing.assert_array_equal(area, ra.astype(np.int32))
+    np.testing.assert_array_equal(perim, rp.astype(np.int32))
+
+
+@pytest.mark.parametrize("D,perimeter,seed", [(16, False, 12345), (16, True, 777),
+                                              (32, True, 31337)])
+def test_one_thread_reference_run_equals_restatement(engine_lib, D, perimeter, seed):
+    w = W.random_small((D, D), D * D // 20, seed=D + seed % 97, temperature=6.0,
+                       perim=perimeter)
+    J = np.rint(w.J).astype(int)
+    lam_a = [0.0, 1.0, 1.0]
+    tgt_a = [0, 20, 20]
+    lam_p = [0.0, 0.5, 0.5] if perimeter else [0.0, 0.0, 0.0]
+    tgt_p = [0, 18, 18]
+    wi = W.Workload("one_thread", w.lattice, w.ncells, J.astype(np.float32),
+                    np.array(lam_a, np.float32), np.array(tgt_a, np.int32),
+                    np.array(lam_p, np.float32), np.array(tgt_p, np.int32), 6.0, 0)
+    ref = _ref(wi)
+    a0, p0 = ref.tables()
+    mcs = 3
+    ref.run(mcs, threads_per_block=1, positions_per_thread=D, positions_per_checkerboard=D,
+            seed=seed)
+    ref.synchronize()
+    got = ref.pull()
+    ra, rp = ref.tables()
+
+    lat = w.lattice.copy()
+    area, perim = a0.astype(np.int64), p0.astype(np.int64)
+    acc = refmodel.sequential_run(lat, area, perim, J, lam_a, tgt_a, lam_p, tgt_p, 6.0,
+                                  seed, mcs, perimeter_on=perimeter)
+    assert acc > 10
+    np.testing.assert_array_equal(got, lat)
+    np.testing.assert_array_equal(ra.astype(np.int64), area)
+    if perimeter:
+        np.testing.assert_array_equal(rp.astype(np.int64), perim)
+
+
+def _observables(lat, prev):
+    ids = (lat & 0xFFFFFF).astype(np.int64)
+    areas = np.bincount(ids.ravel())[1:]
+    alive = areas[areas > 0]
+    lat64 = lat.astype(np.int64)
+    per = np.zeros_like(areas)
+    for dy in (-1, 0, 1):
+        for dx in (-1, 0, 1):
+            if dy == 0 and dx == 0:
+                continue
+            nb = np.roll(np.roll(lat64, -dy, 0), -dx, 1)
+            diff = (nb != lat64) & (ids > 0)
+            per += np.bincount(ids[diff], minlength=len(areas) + 1)[1:]
+    return {"mean_area": float(alive.mean()), "sd_area": float(alive.std()),
+            "mean_perimeter": float(per[areas > 0].mean()), "cells": int(len(alive)),
+            "heterotypic": refmodel.heterotypic_fraction(lat),
+            "activity": float((lat != prev).mean())}
+
+
+def test_sorting_statistics_match_reference(engine_lib):
+    """The sorting recipe at 256^2 (655 cells of 5x5, J_ll=14 J_dd=2 J_ld=11
+    J_lm=J_dm=16, A=25, lambda=1, T=10) after 1000 MCS, 6 seeds each.  The
+    reference runs its own examples/sorting.py geometry (32x32 threads, 4x4
+    sites per thread, 2x2 checkerboard squares, grid sync per attempt)."""
+    w = W.sorting_2d(n=256, ncells=655)
+    mcs, tail = 1000, 10
+    ours, refs = [], []
+    for seed in range(1, 7):
+        e = _ours(w, seed=seed)
+        e.run_mcs(mcs - tail)
+        e.synchronize()
+        e.pull_from_gpu()
+        prev = e.get_state().view(np.uint32).copy()
+        e.run_mcs(tail)
+        e.synchronize()
+        e.pull_from_gpu()
+        ours.append(_observables(e.get_state().view(np.uint32), prev))
+
+        r = _ref(w)
+        kw = dict(threads_per_block=32, positions_per_thread=4, positions_per_checkerboard=2)
+        r.run(mcs - tail, seed=seed, **kw)
+        r.synchronize()
+        prev = r.pull()
+        r.run(tail, seed=seed + 1000, **kw)
+        r.synchronize()
+        refs.append(_observables(r.pull(), prev))
+
+    summary = {}
+    for k in ours[0]:
+        a = np.array([o[k] for o in ours], float)
+        b = np.array([o[k] for o in refs], float)
+        summary[k] = {"ours_mean": a.mean(), "ours_sd": a.std(ddof=1),
+                      "ref_mean": b.mean(), "ref_sd": b.std(ddof=1)}
+    REPORT.mkdir(exist_ok=True)
+    (REPORT / "reference_sorting_stats.json").write_text(json.dumps(summary, indent=1))
+    # Stated tolerances (relative to the reference's mean over seeds):
+    #   mean area, mean perimeter          5 %
+    #   sorting order parameter           10 %
+    #   area spread, site activity        15 %
+    #   surviving cells                   10 %
+    # Cells shrink and die in this workload (655 -> ~340).  Reading area
+    # from a per-phase snapshot lets a shrinking cell lose several sites in
+    # one phase at a slightly too small area penalty, which costs about 5 %
+    # more cells by MCS 1000 than the reference's live reads; the oracle
+    # with tables updated after every attempt instead reproduces the
+    # reference's survival.
+    for k, tol in (("mean_area", 0.05), ("sd_area", 0.15), ("mean_perimeter", 0.05),
+                   ("cells", 0.10), ("heterotypic", 0.10), ("activity", 0.15)):
+        o, r = summary[k]["ours_mean"], summary[k]["ref_mean"]
+        assert abs(o - r) <= tol * abs(r), (k, summary[k])
