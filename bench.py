@@ -55,7 +55,9 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--workload", default="tissue_2d",
-                   choices=["tissue_2d", "tissue_2d_8192", "tissue_3d", "sorting_2d"])
+                   choices=["tissue_2d", "tissue_2d_8192", "tissue_3d", "sorting_2d",
+                            "ensemble"])
+    p.add_argument("--replicas", type=int, default=256, help="replicas of --workload ensemble")
     p.add_argument("--mcs", type=int, default=None, help="MCS per step")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -431,11 +433,123 @@ def run_ours(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def run_ensemble(args, world, rank, local):
+    """Ragged ensemble: all replicas in one graph-captured persistent launch
+    (batched) against the same replicas as a per-replica launch loop.
+
+    Each rank runs its own ensemble (replica stream ids offset by rank).  The
+    total lattice (~193 MB for 256 replicas) exceeds L2, so no flush is
+    needed between steps.
+    """
+    import numpy as np
+    import torch
+
+    import gpucpm
+    from gpucpm import workloads as W
+
+    torch.cuda.set_device(local)
+    gpucpm.set_device(local)
+    nrep = args.replicas
+    ws = W.ensemble_2d(nrep=nrep, seed=3)
+    mcs = args.mcs or 500
+    sizes = [w.lattice.shape[::-1] for w in ws]
+    stream = torch.cuda.Stream()
+
+    b = gpucpm.Batch(2, sizes, [w.ncells for w in ws])
+    for r, w in enumerate(ws):
+        b.lattice(r)[...] = w.lattice.view(np.int32)
+        w.apply(b, replica=r)
+    b.set_seed(0, rank * nrep)
+    b.set_stream(stream.cuda_stream)
+    b.push_to_gpu()
+    variant, tuned_ms = b.autotune(probe_mcs=2)
+    for _ in range(args.warmup):
+        b.run_graph(mcs)
+    b.synchronize()
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    launches0 = b.kernel_launches()
+    dist_barrier(world)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            starts[i].record(stream)
+            b.run_graph(mcs)
+            ends[i].record(stream)
+    b.synchronize()
+    torch.cuda.synchronize()
+    dist_barrier(world)
+    launches = b.kernel_launches() - launches0
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    dev_s = dist_max(world, sum(step_ms) / 1e3)
+    sites = sum(w.nsites for w in ws)
+    value = sites * mcs * args.steps * world / dev_s
+    batched_ms = dev_s / args.steps * 1e3
+
+    # The same replicas as a per-replica launch loop: one single-lattice
+    # engine per replica, launched back to back on one stream.
+    engines = []
+    for r, w in enumerate(ws):
+        n = w.lattice.shape
+        e = gpucpm.create_box(n[1], n[0], 1, 2, w.ncells, w.temperature)
+        e.lattice(0)[...] = w.lattice.view(np.int32)
+        w.apply(e, replica=0)
+        e.set_seed(0, rank * nrep + r)
+        e.set_stream(stream.cuda_stream)
+        e.push_to_gpu()
+        engines.append(e)
+    for e in engines:
+        e.run_mcs(2)  # warm-up
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        t0.record(stream)
+        for e in engines:
+            e.run_mcs(mcs)
+        t1.record(stream)
+    for e in engines:
+        e.synchronize()
+    torch.cuda.synchronize()
+    loop_ms = dist_max(world, t0.elapsed_time(t1) / 1e3) * 1e3
+
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peak_hbm()
+    achieved = BYTES_PER_ATTEMPT * sites * mcs / (batched_ms / 1e3) / 1e9
+    side = [s[0] for s in sizes]
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": batched_ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u32+f32", "data": "synthetic (seeded Voronoi replicas)",
+            "config": {"workload": f"ensemble_2d {nrep} replicas, side log-uniform "
+                                   f"[64,1024] ({min(side)}..{max(side)}), cells = side^2/50, "
+                                   "per-replica J~U[2,20], lambda~U[0.5,2], T~U[5,30]",
+                       "sites": sites, "mcs_per_step": mcs, "tile_variant": variant,
+                       "l2": "inputs larger than L2 (no flush)", "seed": 0},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak,
+                         "peak_source": f"{peak_kind} HBM copy (burst)", "traffic": None,
+                         "algorithmic_bytes_per_launch": BYTES_PER_ATTEMPT * sites * mcs,
+                         "kernel": "sweep_kernel (one graph-captured launch per step)"},
+            "gpu_launches": int(launches),
+            "batched_vs_loop": {"batched_ms": batched_ms, "loop_ms": loop_ms,
+                                "speedup": loop_ms / batched_ms,
+                                "loop": "one single-lattice engine per replica, "
+                                        "launched back to back on one stream"},
+            "autotune": {"variant": variant, "probe_ms_per_mcs": tuned_ms},
+            "step_ms": step_ms, "e2e": None}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.workload == "ensemble":
+        run_ensemble(args, world, rank, local)
     else:
         run_ours(args, world, rank, local)
     if world > 1:

@@ -66,11 +66,25 @@ struct cpm_handle {
 
   cudaStream_t stream = nullptr;      // stream work is enqueued on
   cudaStream_t own_stream = nullptr;  // created with the handle
-  int grid = 1;
-  long long list_cap = 0;
-  std::vector<int> task_prefix;  // [27][nrep + 1]
-  std::vector<int> active_slots;
+  // One launch configuration per tile variant; `variant` is the one runs use
+  // (0 until cpm_autotune picks another).
+  struct Config {
+    SweepShape shape;
+    int grid = 1;
+    long long list_cap = 0;
+    std::vector<int> task_prefix;  // [27][nrep + 1] warp tiles per slot
+    std::vector<int> active_slots;
+  } cfg[kTileVariants];
+  int variant = 0;
   std::vector<unsigned long long> attempts;  // per replica, host-counted
+
+  // Graph-captured run (cpm_run_graph): the captured launch reads and
+  // advances the device copy of the tick.
+  unsigned long long* d_tick = nullptr;
+  bool d_tick_stale = true;
+  cudaGraphExec_t graph_exec = nullptr;
+  int graph_mcs = 0, graph_variant = -1;
+  cudaStream_t graph_stream = nullptr;
 
   uint64_t seed = 0;
   uint32_t stream_id = 0;
@@ -135,6 +149,8 @@ void free_all(cpm_handle* h) {
   cudaFree(h->d_reps);
   cudaFree(h->d_params);
   cudaFree(h->d_task_prefix);
+  cudaFree(h->d_tick);
+  if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
 }
 
@@ -232,7 +248,8 @@ int build_engine(int n, int ndim, const int* nx, const int* ny, const int* nz,
   al((void**)&h->d_ctype, sizeof(int) * rows);
   al((void**)&h->d_reps, sizeof(DevReplica) * n);
   al((void**)&h->d_params, sizeof(DevParams) * n);
-  al((void**)&h->d_task_prefix, sizeof(int) * 27 * (n + 1));
+  al((void**)&h->d_task_prefix, sizeof(int) * kTileVariants * 27 * (n + 1));
+  al((void**)&h->d_tick, sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMallocHost((void**)&h->h_lat, sizeof(uint32_t) * (sites ? sites : 1));
   if (e != cudaSuccess) {
     g_create_error = std::string("device/pinned allocation failed: ") + cudaGetErrorString(e);
@@ -242,56 +259,59 @@ int build_engine(int n, int ndim, const int* nx, const int* ny, const int* nz,
   }
   std::memset(h->h_lat, 0, sizeof(uint32_t) * sites);
 
-  // Sweep tiles per slot and replica (prefix over replicas).
-  const int tcx = ndim == 2 ? TileGeom<2>::CX : TileGeom<3>::CX;
-  const int tcy = ndim == 2 ? TileGeom<2>::CY : TileGeom<3>::CY;
-  const int tcz = ndim == 2 ? TileGeom<2>::CZ : TileGeom<3>::CZ;
-  h->task_prefix.assign(27 * (n + 1), 0);
-  long long max_tasks = 1;
-  for (int slot = 0; slot < 27; ++slot) {
-    const int cx = slot % 3, cy = (slot / 3) % 3, cz = slot / 9;
-    long long acc = 0;
-    for (int r = 0; r < n; ++r) {
-      h->task_prefix[slot * (n + 1) + r] = (int)acc;
-      const DevReplica& R = h->reps[r];
-      if (ndim == 2 && cz != 0) continue;
-      const long long ncx = class_count_h(R.nx, cx), ncy = class_count_h(R.ny, cy),
-                      ncz = class_count_h(R.nz, cz);
-      if (!ncx || !ncy || !ncz) continue;
-      acc += ((ncx + tcx - 1) / tcx) * ((ncy + tcy - 1) / tcy) * ((ncz + tcz - 1) / tcz);
-    }
-    if (acc >= (1LL << 31)) {
-      g_create_error = "batch too large for one launch";
-      free_all(h);
-      delete h;
-      return CPM_ERR_INVALID;
-    }
-    h->task_prefix[slot * (n + 1) + n] = (int)acc;
-    if (acc > 0) h->active_slots.push_back(slot);
-    max_tasks = std::max(max_tasks, acc);
-  }
-
+  // One launch configuration per tile variant: warp tiles per slot and
+  // replica (prefix over replicas), grid, dirty-list capacity.
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
-  int per_sm = sweep_max_blocks_per_sm(ndim, true);
-  per_sm = std::min(per_sm, sweep_max_blocks_per_sm(ndim, false));
-  if (per_sm < 1 || sms < 1) {
-    g_create_error = "cannot place the sweep kernel on this device";
-    free_all(h);
-    delete h;
-    return CPM_ERR_CUDA;
+  long long dlist_entries = 1;
+  for (int v = 0; v < kTileVariants; ++v) {
+    cpm_handle::Config& c = h->cfg[v];
+    c.shape = sweep_shape(ndim, v);
+    c.task_prefix.assign(27 * (n + 1), 0);
+    long long max_tasks = 1;
+    for (int slot = 0; slot < 27; ++slot) {
+      const int cx = slot % 3, cy = (slot / 3) % 3, cz = slot / 9;
+      long long acc = 0;
+      for (int r = 0; r < n; ++r) {
+        c.task_prefix[slot * (n + 1) + r] = (int)acc;
+        const DevReplica& R = h->reps[r];
+        if (ndim == 2 && cz != 0) continue;
+        const long long ncx = class_count_h(R.nx, cx), ncy = class_count_h(R.ny, cy),
+                        ncz = class_count_h(R.nz, cz);
+        if (!ncx || !ncy || !ncz) continue;
+        acc += ((ncx + c.shape.cx - 1) / c.shape.cx) * ((ncy + c.shape.cy - 1) / c.shape.cy) *
+               ((ncz + c.shape.cz - 1) / c.shape.cz);
+      }
+      if (acc >= (1LL << 31)) {
+        g_create_error = "batch too large for one launch";
+        free_all(h);
+        delete h;
+        return CPM_ERR_INVALID;
+      }
+      c.task_prefix[slot * (n + 1) + n] = (int)acc;
+      if (acc > 0) c.active_slots.push_back(slot);
+      max_tasks = std::max(max_tasks, acc);
+    }
+    const int per_sm = std::min(sweep_max_blocks_per_sm(ndim, true, v),
+                                sweep_max_blocks_per_sm(ndim, false, v));
+    if (per_sm < 1 || sms < 1) {
+      g_create_error = "cannot place the sweep kernel on this device";
+      free_all(h);
+      delete h;
+      return CPM_ERR_CUDA;
+    }
+    // One block per SM (fewer if the largest slot has fewer warp tiles).
+    const long long blocks_needed = (max_tasks + c.shape.warps - 1) / c.shape.warps;
+    c.grid = (int)std::max(1LL, std::min<long long>((long long)per_sm * sms, blocks_needed));
+    // Per-block dirty lists (two per block, for the running and the previous
+    // phase): a warp works at most ceil(tiles / warps) tiles per slot, each
+    // attempt touching at most two table rows.
+    const long long warps = (long long)c.grid * c.shape.warps;
+    const long long nt = (long long)c.shape.cx * c.shape.cy * c.shape.cz;
+    c.list_cap = 2LL * nt * c.shape.warps * ((max_tasks + warps - 1) / warps);
+    dlist_entries = std::max(dlist_entries, c.list_cap * 2 * c.grid);
   }
-  // One block per SM (fewer if the largest slot has fewer warp tiles).
-  const long long blocks_needed = (max_tasks + kSweepWarps - 1) / kSweepWarps;
-  h->grid = (int)std::min<long long>((long long)per_sm * sms, blocks_needed);
-  h->grid = std::max(h->grid, 1);
-  // Per-block dirty lists (two per block, for the running and the previous
-  // phase): a warp works at most ceil(tiles / warps) tiles per slot, each
-  // attempt touching at most two table rows.
-  const long long warps = (long long)h->grid * kSweepWarps;
-  h->list_cap = 2LL * sweep_tile_targets(ndim) * kSweepWarps *
-                ((max_tasks + warps - 1) / warps);
-  e = cudaMalloc((void**)&h->d_dlist, sizeof(uint32_t) * h->list_cap * 2 * h->grid);
+  e = cudaMalloc((void**)&h->d_dlist, sizeof(uint32_t) * dlist_entries);
   if (e != cudaSuccess) {
     g_create_error = std::string("dirty-list allocation failed: ") + cudaGetErrorString(e);
     free_all(h);
@@ -301,9 +321,9 @@ int build_engine(int n, int ndim, const int* nx, const int* ny, const int* nz,
 
   e = cudaMemcpyAsync(h->d_reps, h->reps.data(), sizeof(DevReplica) * n,
                       cudaMemcpyHostToDevice, h->stream);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(h->d_task_prefix, h->task_prefix.data(),
-                        sizeof(int) * h->task_prefix.size(),
+  for (int v = 0; v < kTileVariants && e == cudaSuccess; ++v)
+    e = cudaMemcpyAsync(h->d_task_prefix + (size_t)v * 27 * (n + 1),
+                        h->cfg[v].task_prefix.data(), sizeof(int) * 27 * (n + 1),
                         cudaMemcpyHostToDevice, h->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(h->d_ctl, 0, sizeof(uint32_t) * kCtlWords, h->stream);
   if (e == cudaSuccess)
@@ -385,6 +405,58 @@ int read_error_word(cpm_handle* h, uint32_t* word) {
                               cudaMemcpyDeviceToHost, h->stream));
   CPM_CUDA(h, cudaStreamSynchronize(h->stream));
   return CPM_OK;
+}
+
+int upload_params(cpm_handle* h) {
+  if (!h->params_dirty) return CPM_OK;
+  for (auto& p : h->params) p.perim_on = perim_on(p) ? 1 : 0;
+  CPM_CUDA(h, cudaMemcpyAsync(h->d_params, h->params.data(), sizeof(DevParams) * h->nrep,
+                              cudaMemcpyHostToDevice, h->stream));
+  CPM_CUDA(h, cudaStreamSynchronize(h->stream));  // the host copy may change next
+  h->params_dirty = false;
+  return CPM_OK;
+}
+
+bool any_perimeter(const cpm_handle* h) {
+  for (auto& p : h->params)
+    if (p.perim_on) return true;
+  return false;
+}
+
+// Kernel arguments of a sweep with tile variant v (tick0 / mcs filled in by
+// the caller).
+SweepArgs sweep_args(const cpm_handle* h, int v) {
+  SweepArgs a;
+  std::memset(&a, 0, sizeof a);
+  a.lat = h->d_lat;
+  for (int b = 0; b < 2; ++b) {
+    a.ap[b] = h->d_ap[b];
+    a.cs[b] = h->d_cs[b];
+    a.dap[b] = h->d_dap[b];
+    a.dcs[b] = h->d_dcs[b];
+    a.dflag[b] = h->d_dflag[b];
+  }
+  const cpm_handle::Config& c = h->cfg[v];
+  a.dlist = h->d_dlist;
+  a.list_cap = c.list_cap;
+  a.ctl = h->d_ctl;
+  a.counters = h->d_counters;
+  a.reps = h->d_reps;
+  a.params = h->d_params;
+  a.task_prefix = h->d_task_prefix + (size_t)v * 27 * (h->nrep + 1);
+  a.seed = h->seed;
+  a.nrep = h->nrep;
+  a.stream0 = h->stream_id;
+  a.nslot_active = (int)c.active_slots.size();
+  for (int i = 0; i < a.nslot_active; ++i) a.slots[i] = c.active_slots[i];
+  return a;
+}
+
+void count_attempts(cpm_handle* h, int mcs) {
+  for (int r = 0; r < h->nrep; ++r) {
+    const DevReplica& R = h->reps[r];
+    h->attempts[r] += (unsigned long long)R.nx * R.ny * R.nz * (unsigned long long)mcs;
+  }
 }
 
 std::string describe_errors(uint32_t w) {
@@ -555,56 +627,158 @@ int cpm_run(cpm_handle* h, int mcs) {
   if (mcs < 0) return h->fail(CPM_ERR_INVALID, "mcs must be >= 0");
   if (!h->pushed) return h->fail(CPM_ERR_STATE, "run() before a successful push_to_gpu()");
   if (mcs == 0) return CPM_OK;
-  if (h->params_dirty) {
-    for (auto& p : h->params) p.perim_on = perim_on(p) ? 1 : 0;
-    CPM_CUDA(h, cudaMemcpyAsync(h->d_params, h->params.data(),
-                                sizeof(DevParams) * h->nrep,
-                                cudaMemcpyHostToDevice, h->stream));
-    h->params_dirty = false;
-  }
-  bool any_perim = false;
-  for (auto& p : h->params) any_perim |= p.perim_on != 0;
-
-  SweepArgs a;
-  std::memset(&a, 0, sizeof a);
-  a.lat = h->d_lat;
-  for (int b = 0; b < 2; ++b) {
-    a.ap[b] = h->d_ap[b];
-    a.cs[b] = h->d_cs[b];
-    a.dap[b] = h->d_dap[b];
-    a.dcs[b] = h->d_dcs[b];
-    a.dflag[b] = h->d_dflag[b];
-  }
-  a.dlist = h->d_dlist;
-  a.list_cap = h->list_cap;
-  a.ctl = h->d_ctl;
-  a.counters = h->d_counters;
-  a.reps = h->d_reps;
-  a.params = h->d_params;
-  a.task_prefix = h->d_task_prefix;
-  a.seed = h->seed;
-  a.nrep = h->nrep;
-  a.stream0 = h->stream_id;
-  a.nslot_active = (int)h->active_slots.size();
-  for (int i = 0; i < a.nslot_active; ++i) a.slots[i] = h->active_slots[i];
-
+  if (int rc = upload_params(h)) return rc;
+  const bool any_perim = any_perimeter(h);
+  SweepArgs a = sweep_args(h, h->variant);
   int left = mcs;
   while (left > 0) {
     const int chunk = std::min(left, kMaxMcsPerLaunch);
     a.tick0 = h->tick;
     a.mcs = chunk;
-    // Barrier counter and both dirty counts start at zero in every launch;
-    // the sticky error word is left alone until cpm_synchronize reads it.
+    // Barrier counter and release flag start at zero in every launch; the
+    // sticky error word is left alone until cpm_synchronize reads it.
     CPM_CUDA(h, cudaMemsetAsync(h->d_ctl, 0, sizeof(uint32_t) * kCtlErr, h->stream));
-    CPM_CUDA(h, launch_sweep(h->ndim, any_perim, a, h->grid, h->stream));
+    CPM_CUDA(h, launch_sweep(h->ndim, any_perim, h->variant, a, h->cfg[h->variant].grid,
+                             h->stream));
     h->launches += 1;
     h->tick += (uint64_t)chunk;
     left -= chunk;
   }
-  for (int r = 0; r < h->nrep; ++r) {
-    const DevReplica& R = h->reps[r];
-    h->attempts[r] += (unsigned long long)R.nx * R.ny * R.nz * (unsigned long long)mcs;
+  h->d_tick_stale = true;
+  count_attempts(h, mcs);
+  return CPM_OK;
+}
+
+int cpm_run_graph(cpm_handle* h, int mcs) {
+  CPM_BIND(h);
+  if (mcs <= 0 || mcs > kMaxMcsPerLaunch)
+    return h->fail(CPM_ERR_INVALID, "mcs must be in [1, %d] for a graph run", kMaxMcsPerLaunch);
+  if (!h->pushed) return h->fail(CPM_ERR_STATE, "run before a successful push_to_gpu()");
+  if (h->stream == nullptr)
+    return h->fail(CPM_ERR_STATE, "graph runs need a non-default stream");
+  if (int rc = upload_params(h)) return rc;
+  if (!h->graph_exec || h->graph_mcs != mcs || h->graph_variant != h->variant ||
+      h->graph_stream != h->stream) {
+    if (h->graph_exec) {
+      cudaGraphExecDestroy(h->graph_exec);
+      h->graph_exec = nullptr;
+    }
+    // Capture: reset the barrier words, then the persistent sweep reading
+    // its start time from (and advancing) the device tick.
+    SweepArgs a = sweep_args(h, h->variant);
+    a.tick_ptr = h->d_tick;
+    a.mcs = mcs;
+    cudaGraph_t g = nullptr;
+    CPM_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e1 = cudaMemsetAsync(h->d_ctl, 0, sizeof(uint32_t) * kCtlErr, h->stream);
+    cudaError_t e2 = e1 == cudaSuccess
+                         ? launch_sweep(h->ndim, any_perimeter(h), h->variant, a,
+                                        h->cfg[h->variant].grid, h->stream)
+                         : e1;
+    cudaError_t e3 = cudaStreamEndCapture(h->stream, &g);
+    if (e2 != cudaSuccess) return h->cuda_fail(e2, "capture of the sweep launch");
+    if (e3 != cudaSuccess) return h->cuda_fail(e3, "cudaStreamEndCapture");
+    cudaError_t e4 = cudaGraphInstantiate(&h->graph_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e4 != cudaSuccess) return h->cuda_fail(e4, "cudaGraphInstantiate");
+    h->graph_mcs = mcs;
+    h->graph_variant = h->variant;
+    h->graph_stream = h->stream;
   }
+  if (h->d_tick_stale) {
+    const unsigned long long t = h->tick;
+    CPM_CUDA(h, cudaMemcpyAsync(h->d_tick, &t, sizeof t, cudaMemcpyHostToDevice, h->stream));
+    CPM_CUDA(h, cudaStreamSynchronize(h->stream));  // `t` lives on this frame
+    h->d_tick_stale = false;
+  }
+  CPM_CUDA(h, cudaGraphLaunch(h->graph_exec, h->stream));
+  h->launches += 1;
+  h->tick += (uint64_t)mcs;
+  count_attempts(h, mcs);
+  return CPM_OK;
+}
+
+int cpm_autotune(cpm_handle* h, int probe_mcs, int* chosen, float* ms_per_mcs) {
+  CPM_BIND(h);
+  if (!h->pushed) return h->fail(CPM_ERR_STATE, "autotune before a successful push_to_gpu()");
+  if (probe_mcs < 1) probe_mcs = 2;
+  if (int rc = upload_params(h)) return rc;
+  // Work on a saved copy of the state: every variant runs the same MCS from
+  // the same start, and the state (lattice, tables, counters, tick) is put
+  // back afterwards.  The sweep's result does not depend on the variant, so
+  // only the time differs.
+  const size_t lat_b = sizeof(uint32_t) * h->total_sites;
+  const size_t ap_b = sizeof(unsigned long long) * h->rows;
+  const size_t cs_b = sizeof(long long) * h->rows * h->ndim;
+  const size_t cnt_b = sizeof(unsigned long long) * 2 * h->nrep;
+  char* save = nullptr;
+  CPM_CUDA(h, cudaMalloc(&save, lat_b + ap_b + cs_b + cnt_b));
+  auto copy = [&](bool to_save) -> cudaError_t {
+    char* p = save;
+    void* dst[4] = {p, p + lat_b, p + lat_b + ap_b, p + lat_b + ap_b + cs_b};
+    void* src[4] = {h->d_lat, h->d_ap[0], h->d_cs[0], h->d_counters};
+    const size_t n[4] = {lat_b, ap_b, cs_b, cnt_b};
+    for (int i = 0; i < 4; ++i) {
+      cudaError_t e = to_save ? cudaMemcpyAsync(dst[i], src[i], n[i], cudaMemcpyDeviceToDevice, h->stream)
+                              : cudaMemcpyAsync(src[i], dst[i], n[i], cudaMemcpyDeviceToDevice, h->stream);
+      if (e != cudaSuccess) return e;
+    }
+    if (!to_save) {
+      cudaError_t e = cudaMemcpyAsync(h->d_ap[1], h->d_ap[0], ap_b, cudaMemcpyDeviceToDevice, h->stream);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(h->d_cs[1], h->d_cs[0], cs_b, cudaMemcpyDeviceToDevice, h->stream);
+      return e;
+    }
+    return cudaSuccess;
+  };
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  cudaError_t e = cudaEventCreate(&ev[0]);
+  if (e == cudaSuccess) e = cudaEventCreate(&ev[1]);
+  if (e == cudaSuccess) e = copy(true);
+  const uint64_t tick = h->tick;
+  const int keep = h->variant;
+  float best = -1.0f;
+  int best_v = keep;
+  const bool any_perim = any_perimeter(h);
+  for (int v = 0; v < kTileVariants && e == cudaSuccess; ++v) {
+    SweepArgs a = sweep_args(h, v);
+    a.tick0 = tick;
+    a.mcs = probe_mcs;
+    e = copy(false);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->d_ctl, 0, sizeof(uint32_t) * kCtlErr, h->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[0], h->stream);
+    if (e == cudaSuccess) e = launch_sweep(h->ndim, any_perim, v, a, h->cfg[v].grid, h->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[1], h->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
+    float ms = 0.0f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ev[0], ev[1]);
+    h->launches += 1;
+    if (e == cudaSuccess && (best < 0.0f || ms < best)) {
+      best = ms;
+      best_v = v;
+    }
+  }
+  if (e == cudaSuccess) e = copy(false);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  cudaFree(save);
+  if (ev[0]) cudaEventDestroy(ev[0]);
+  if (ev[1]) cudaEventDestroy(ev[1]);
+  if (e != cudaSuccess) return h->cuda_fail(e, "autotune");
+  uint32_t w = 0;
+  if (int rc = read_error_word(h, &w)) return rc;
+  if (w) return h->fail(CPM_ERR_TIMEOUT, "autotune: %s", describe_errors(w).c_str());
+  h->variant = best_v;
+  h->tick = tick;
+  if (chosen) *chosen = best_v;
+  if (ms_per_mcs) *ms_per_mcs = best / (float)probe_mcs;
+  return CPM_OK;
+}
+
+int cpm_set_variant(cpm_handle* h, int variant) {
+  if (!h) return CPM_ERR_INVALID;
+  if (variant < 0 || variant >= kTileVariants)
+    return h->fail(CPM_ERR_INVALID, "tile variant %d out of range [0, %d)", variant, kTileVariants);
+  h->variant = variant;
   return CPM_OK;
 }
 
@@ -650,6 +824,7 @@ int cpm_get_tick(const cpm_handle* h, uint64_t* tick) {
 int cpm_set_tick(cpm_handle* h, uint64_t tick) {
   if (!h) return CPM_ERR_INVALID;
   h->tick = tick;
+  h->d_tick_stale = true;
   return CPM_OK;
 }
 
@@ -741,8 +916,21 @@ int cpm_info(const cpm_handle* h, int* n_replicas, int* dimensionality,
   if (!h) return CPM_ERR_INVALID;
   if (n_replicas) *n_replicas = h->nrep;
   if (dimensionality) *dimensionality = h->ndim;
-  if (sweep_grid) *sweep_grid = h->grid;
+  if (sweep_grid) *sweep_grid = h->cfg[h->variant].grid;
   if (kernel_launches) *kernel_launches = h->launches;
+  return CPM_OK;
+}
+
+int cpm_sweep_config(const cpm_handle* h, int* variant, int* tile_x, int* tile_y,
+                     int* tile_z, int* warps_per_block, int* grid) {
+  if (!h) return CPM_ERR_INVALID;
+  const cpm_handle::Config& c = h->cfg[h->variant];
+  if (variant) *variant = h->variant;
+  if (tile_x) *tile_x = c.shape.cx;
+  if (tile_y) *tile_y = c.shape.cy;
+  if (tile_z) *tile_z = c.shape.cz;
+  if (warps_per_block) *warps_per_block = c.shape.warps;
+  if (grid) *grid = c.grid;
   return CPM_OK;
 }
 

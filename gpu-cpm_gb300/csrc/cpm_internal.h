@@ -30,23 +30,53 @@
 namespace gpucpm {
 
 constexpr int kMaxTypes = 32;
-constexpr int kSweepWarps = 24;  // warps per sweep block, one block per SM
-constexpr int kSweepThreads = 32 * kSweepWarps;
+constexpr int kMaxSweepWarps = 24;  // warps per sweep block (one block per SM)
+constexpr int kSweepThreadsMax = 32 * kMaxSweepWarps;
+constexpr int kSweepSmemMax = 227 * 1024;  // usable shared memory per block
 constexpr int kInitThreads = 256;
 
 // Warp tile: CX x CY x CZ targets of one slot, staged with their one-site
-// halo in the warp's own shared memory.  2D: 32 x 8 targets (66 x 17
-// sites); 3D: 32 x 2 x 2 targets (66 x 5 x 5 sites).
-template <int NDIM>
+// halo in the warp's own shared memory.  Three compiled variants per
+// dimensionality; the autotuner (cpm_autotune) picks one per engine.  The
+// sweep's result does not depend on the variant.
+//   2D  v0 32 x 8 (66 x 17 sites)   v1 32 x 4    v2 32 x 16
+//   3D  v0 32 x 2 x 2 (66 x 5 x 5)  v1 32 x 4 x 2  v2 32 x 4 x 4
+constexpr int kTileVariants = 3;
+template <int NDIM, int V>
 struct TileGeom;
 template <>
-struct TileGeom<2> {
+struct TileGeom<2, 0> {
   static constexpr int CX = 32, CY = 8, CZ = 1;
 };
 template <>
-struct TileGeom<3> {
+struct TileGeom<2, 1> {
+  static constexpr int CX = 32, CY = 4, CZ = 1;
+};
+template <>
+struct TileGeom<2, 2> {
+  static constexpr int CX = 32, CY = 16, CZ = 1;
+};
+template <>
+struct TileGeom<3, 0> {
   static constexpr int CX = 32, CY = 2, CZ = 2;
 };
+template <>
+struct TileGeom<3, 1> {
+  static constexpr int CX = 32, CY = 4, CZ = 2;
+};
+template <>
+struct TileGeom<3, 2> {
+  static constexpr int CX = 32, CY = 4, CZ = 4;
+};
+
+// Launch shape of one sweep configuration.
+struct SweepShape {
+  int variant;      // tile variant
+  int cx, cy, cz;   // its tile extent in targets
+  int warps;        // warps per block (tiles in flight per block)
+  size_t smem;      // dynamic shared memory per block
+};
+SweepShape sweep_shape(int ndim, int variant);
 
 // ctl[] word indices (the barrier counter and its release flag sit in
 // different 128-byte lines so that waiting blocks do not slow down arriving
@@ -110,6 +140,10 @@ struct SweepArgs {
   const DevParams* params;
   const int* task_prefix;  // [27][nrep + 1] warp tiles per slot, prefix
   long long list_cap;      // entries of one dirty list of one block
+  // Monte Carlo time of the first MCS: tick0, or *tick_ptr when tick_ptr is
+  // set (graph replays); in the latter case block 0 advances *tick_ptr by
+  // mcs when the launch ends.
+  unsigned long long* tick_ptr;
   unsigned long long tick0;
   unsigned long long seed;
   int nrep;
@@ -123,11 +157,9 @@ struct SweepArgs {
 void set_thread_error(const char* message);
 
 // Launchers (cpm_kernels.cu).  Each returns the cudaError_t of its launch.
-cudaError_t sweep_prepare(int ndim, bool perim);
-cudaError_t launch_sweep(int ndim, bool perim, const SweepArgs& a, int grid,
-                         cudaStream_t s);
-int sweep_max_blocks_per_sm(int ndim, bool perim);
-int sweep_tile_targets(int ndim);
+cudaError_t launch_sweep(int ndim, bool perim, int variant, const SweepArgs& a,
+                         int grid, cudaStream_t s);
+int sweep_max_blocks_per_sm(int ndim, bool perim, int variant);
 cudaError_t launch_barrier_probe(uint32_t* ctl, unsigned long long timeout_ns,
                                  cudaStream_t s);
 cudaError_t launch_init(int ndim, const uint32_t* lat, const DevReplica* reps,

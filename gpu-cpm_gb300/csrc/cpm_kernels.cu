@@ -20,7 +20,7 @@
 // result is independent of thread, block and replica order, which is what
 // makes the CPU oracle (oracle/cpm_oracle.cpp) reproduce it bit for bit.
 //
-// Work decomposition.  One block of kSweepWarps warps per SM, one grid
+// Work decomposition.  One block of up to 24 warps per SM, one grid
 // barrier per slot.  The unit of work is a warp tile: CX x CY (x CZ)
 // targets of one slot of one replica, staged with a one-site halo in the
 // warp's own shared memory (periodic wrap resolved while loading; even and
@@ -87,9 +87,9 @@ __device__ __forceinline__ unsigned lanemask_lt() {
 // Shared-memory layout of a staged warp tile.  Logical column c of a staged
 // row lives at (c & 1) * HALF + (c >> 1): target columns (odd logical
 // columns) in the upper half, their left / right neighbours in the lower.
-template <int NDIM>
+template <int NDIM, int V>
 struct Stage {
-  using G = TileGeom<NDIM>;
+  using G = TileGeom<NDIM, V>;
   static constexpr int HALF = G::CX + 1;
   static constexpr int SXP = 2 * HALF;
   static constexpr int SY = 2 * G::CY + 1;
@@ -119,16 +119,32 @@ struct Stage {
   }
 };
 
-template <int NDIM>
+template <int NDIM, int V>
 struct WarpSmem {
-  uint2 qb[Stage<NDIM>::NT];                // (q | dir << 16, uniform word)
-  uint32_t tile[Stage<NDIM>::WORDS];
-  uint16_t qa[Stage<NDIM>::NT];
+  uint2 qb[Stage<NDIM, V>::NT];                // (q | dir << 16, uniform word)
+  uint32_t tile[Stage<NDIM, V>::WORDS];
+  uint16_t qa[Stage<NDIM, V>::NT];
 };
 
-template <int NDIM>
-constexpr size_t sweep_smem_bytes() {
-  return sizeof(WarpSmem<NDIM>) * kSweepWarps;
+// Warps per block of a variant: as many warp tiles as fit in shared memory,
+// at most kMaxSweepWarps (the register file's limit at 80 registers).
+template <int NDIM, int V>
+constexpr int variant_warps() {
+  const size_t w = kSweepSmemMax / sizeof(WarpSmem<NDIM, V>);
+  return w < (size_t)kMaxSweepWarps ? (int)w : kMaxSweepWarps;
+}
+
+template <int NDIM, int V>
+SweepShape shape_of() {
+  using G = TileGeom<NDIM, V>;
+  SweepShape s;
+  s.variant = V;
+  s.cx = G::CX;
+  s.cy = G::CY;
+  s.cz = G::CZ;
+  s.warps = variant_warps<NDIM, V>();
+  s.smem = sizeof(WarpSmem<NDIM, V>) * (size_t)s.warps;
+  return s;
 }
 
 // Per-phase view of the double-buffered tables.
@@ -192,22 +208,24 @@ __device__ __forceinline__ void replay(const uint32_t* list, unsigned n,
   }
 }
 
-template <int NDIM, bool PERIM>
-__global__ void __launch_bounds__(kSweepThreads, 1)
+template <int NDIM, bool PERIM, int V>
+__global__ void __launch_bounds__(kSweepThreadsMax, 1)
     sweep_kernel(const SweepArgs a) {
-  using G = TileGeom<NDIM>;
-  using S = Stage<NDIM>;
+  using G = TileGeom<NDIM, V>;
+  using S = Stage<NDIM, V>;
   constexpr int NB = S::NB;
   constexpr int NT = S::NT;
   constexpr unsigned long long NSLOTS = NDIM == 2 ? 9 : 27;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_ok;
   __shared__ unsigned s_cnt[2];
+  __shared__ unsigned long long s_tick0;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  WarpSmem<NDIM>& ws = reinterpret_cast<WarpSmem<NDIM>*>(smem_raw)[warp];
-  const int gwarp = blockIdx.x * kSweepWarps + warp;
-  const int nwarps = gridDim.x * kSweepWarps;
+  const int wpb = blockDim.x >> 5;  // warps (tiles in flight) per block
+  WarpSmem<NDIM, V>& ws = reinterpret_cast<WarpSmem<NDIM, V>*>(smem_raw)[warp];
+  const int gwarp = blockIdx.x * wpb + warp;
+  const int nwarps = gridDim.x * wpb;
   const uint32_t k0 = (uint32_t)a.seed, k1 = (uint32_t)(a.seed >> 32);
   int* err = reinterpret_cast<int*>(&a.ctl[kCtlErr]);
   // (kernel-parameter arrays are selected with ?: rather than indexed with
@@ -217,11 +235,14 @@ __global__ void __launch_bounds__(kSweepThreads, 1)
   int cnt_rep = -1;
   unsigned long long n_eval = 0, n_acc = 0;  // warp-uniform
   if (tid < 2) s_cnt[tid] = 0;
+  // Every block reads *tick_ptr before its first barrier arrival, and block
+  // 0 advances it only after the last barrier, so all blocks see one value.
+  if (tid == 0) s_tick0 = a.tick_ptr ? __ldcg(a.tick_ptr) : a.tick0;
   __syncthreads();
 
   int step = 0;
   for (int m = 0; m < a.mcs; ++m) {
-    const unsigned long long tick = a.tick0 + (unsigned long long)m;
+    const unsigned long long tick = s_tick0 + (unsigned long long)m;
     for (int si = 0; si < a.nslot_active; ++si, ++step) {
       const int cur = step & 1, prv = cur ^ 1;
       PhaseTables<NDIM> pt;
@@ -289,7 +310,7 @@ __global__ void __launch_bounds__(kSweepThreads, 1)
         for (int zz = 0; zz < uz; ++zz) {
           int gz = zorig + zz;
           gz = gz < 0 ? gz + nz : (gz >= nz ? gz - nz : gz);
-#pragma unroll 4
+#pragma unroll
           for (int yy = 0; yy < uy; ++yy) {
             int gy = yorig + yy;
             gy = gy < 0 ? gy + ny : (gy >= ny ? gy - ny : gy);
@@ -471,6 +492,8 @@ __global__ void __launch_bounds__(kSweepThreads, 1)
     if (n_eval) atomicAdd(&a.counters[2 * cnt_rep], n_eval);
     if (n_acc) atomicAdd(&a.counters[2 * cnt_rep + 1], n_acc);
   }
+  if (a.tick_ptr && blockIdx.x == 0 && tid == 0 && a.mcs > 0)
+    *a.tick_ptr = s_tick0 + (unsigned long long)a.mcs;
 }
 
 // ---- table recount ---------------------------------------------------------
@@ -558,45 +581,63 @@ __global__ void barrier_probe(uint32_t* ctl, unsigned long long timeout_ns) {
   grid_barrier(ctl, 2u, &s_ok, timeout_ns);
 }
 
-const void* sweep_fn(int ndim, bool perim) {
-  if (ndim == 2)
-    return perim ? (const void*)sweep_kernel<2, true>
-                 : (const void*)sweep_kernel<2, false>;
-  return perim ? (const void*)sweep_kernel<3, true>
-               : (const void*)sweep_kernel<3, false>;
+template <int NDIM, int V>
+const void* sweep_fn_v(bool perim) {
+  return perim ? (const void*)sweep_kernel<NDIM, true, V>
+               : (const void*)sweep_kernel<NDIM, false, V>;
 }
 
-size_t sweep_smem(int ndim) {
-  return ndim == 2 ? sweep_smem_bytes<2>() : sweep_smem_bytes<3>();
+const void* sweep_fn(int ndim, bool perim, int variant) {
+  if (ndim == 2) {
+    switch (variant) {
+      case 1: return sweep_fn_v<2, 1>(perim);
+      case 2: return sweep_fn_v<2, 2>(perim);
+      default: return sweep_fn_v<2, 0>(perim);
+    }
+  }
+  switch (variant) {
+    case 1: return sweep_fn_v<3, 1>(perim);
+    case 2: return sweep_fn_v<3, 2>(perim);
+    default: return sweep_fn_v<3, 0>(perim);
+  }
 }
 
 }  // namespace
 
-cudaError_t sweep_prepare(int ndim, bool perim) {
-  return cudaFuncSetAttribute(sweep_fn(ndim, perim),
-                              cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)sweep_smem(ndim));
+SweepShape sweep_shape(int ndim, int variant) {
+  if (ndim == 2) {
+    switch (variant) {
+      case 1: return shape_of<2, 1>();
+      case 2: return shape_of<2, 2>();
+      default: return shape_of<2, 0>();
+    }
+  }
+  switch (variant) {
+    case 1: return shape_of<3, 1>();
+    case 2: return shape_of<3, 2>();
+    default: return shape_of<3, 0>();
+  }
 }
 
-int sweep_max_blocks_per_sm(int ndim, bool perim) {
+int sweep_max_blocks_per_sm(int ndim, bool perim, int variant) {
+  const SweepShape sh = sweep_shape(ndim, variant);
+  const void* fn = sweep_fn(ndim, perim, variant);
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)sh.smem) != cudaSuccess)
+    return 0;
   int n = 0;
-  if (sweep_prepare(ndim, perim) != cudaSuccess) return 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sweep_fn(ndim, perim),
-                                                    kSweepThreads,
-                                                    sweep_smem(ndim)) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, 32 * sh.warps, sh.smem) !=
+      cudaSuccess)
     return 0;
   return n;
 }
 
-int sweep_tile_targets(int ndim) {
-  return ndim == 2 ? Stage<2>::NT : Stage<3>::NT;
-}
-
-cudaError_t launch_sweep(int ndim, bool perim, const SweepArgs& a, int grid,
-                         cudaStream_t s) {
+cudaError_t launch_sweep(int ndim, bool perim, int variant, const SweepArgs& a,
+                         int grid, cudaStream_t s) {
+  const SweepShape sh = sweep_shape(ndim, variant);
   void* args[] = {const_cast<SweepArgs*>(&a)};
-  return cudaLaunchCooperativeKernel(sweep_fn(ndim, perim), dim3(grid),
-                                     dim3(kSweepThreads), args, sweep_smem(ndim), s);
+  return cudaLaunchCooperativeKernel(sweep_fn(ndim, perim, variant), dim3(grid),
+                                     dim3(32 * sh.warps), args, sh.smem, s);
 }
 
 cudaError_t launch_barrier_probe(uint32_t* ctl, unsigned long long timeout_ns,

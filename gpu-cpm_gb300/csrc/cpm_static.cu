@@ -154,10 +154,10 @@ extern "C" int cpm_sweep_static(int dimensionality, int nx, int ny, int nz,
   const long long rows = (long long)number_of_cells + 1;
   cudaStream_t s = (cudaStream_t)stream;
 
-  // Launch geometry, as the engine computes it for a single replica.
-  const int tcx = ndim == 2 ? TileGeom<2>::CX : TileGeom<3>::CX;
-  const int tcy = ndim == 2 ? TileGeom<2>::CY : TileGeom<3>::CY;
-  const int tcz = ndim == 2 ? TileGeom<2>::CZ : TileGeom<3>::CZ;
+  // Launch geometry, as the engine computes it for a single replica with
+  // tile variant 0.
+  const SweepShape sh = sweep_shape(ndim, 0);
+  const int tcx = sh.cx, tcy = sh.cy, tcz = sh.cz;
   int prefix[27 * 2] = {0};
   SweepArgs a;
   std::memset(&a, 0, sizeof a);
@@ -183,13 +183,12 @@ extern "C" int cpm_sweep_static(int dimensionality, int nx, int ny, int nz,
       if (params->lambda_perimeter[k] != 0.0f) return true;
     return false;
   }();
-  const int per_sm = sweep_max_blocks_per_sm(ndim, perim_on);
+  const int per_sm = sweep_max_blocks_per_sm(ndim, perim_on, 0);
   if (per_sm < 1) return fail(CPM_ERR_CUDA, "cpm_sweep_static: cannot place the sweep kernel");
-  const long long blocks_needed = (max_tiles + kSweepWarps - 1) / kSweepWarps;
+  const long long blocks_needed = (max_tiles + sh.warps - 1) / sh.warps;
   const int grid = (int)std::max(1LL, std::min<long long>((long long)per_sm * sms, blocks_needed));
-  const long long warps = (long long)grid * kSweepWarps;
-  const long long list_cap =
-      2LL * sweep_tile_targets(ndim) * kSweepWarps * ((max_tiles + warps - 1) / warps);
+  const long long warps = (long long)grid * sh.warps;
+  const long long list_cap = 2LL * tcx * tcy * tcz * sh.warps * ((max_tiles + warps - 1) / warps);
   if (list_cap * 2 * grid > kListEntries)
     return fail(CPM_ERR_INVALID,
                 "cpm_sweep_static: lattice shape needs more dirty-list space than the "
@@ -283,7 +282,7 @@ extern "C" int cpm_sweep_static(int dimensionality, int nx, int ny, int nz,
     a.nrep = 1;
     a.mcs = mcs;
     a.stream0 = stream_id;
-    STATIC_CUDA(launch_sweep(ndim, perim_on, a, grid, s));
+    STATIC_CUDA(launch_sweep(ndim, perim_on, 0, a, grid, s));
   }
 
   unpack_tables<<<pack_grid, 256, 0, s>>>(ap0, area, perimeter, rows);

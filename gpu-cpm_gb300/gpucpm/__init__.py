@@ -119,6 +119,10 @@ def library():
         "cpm_get_counters_r": [H, ctypes.c_int, ctypes.POINTER(_Counters)],
         "cpm_reset_counters": [H],
         "cpm_info": [H, ip, ip, ip, ctypes.POINTER(ctypes.c_uint64)],
+        "cpm_run_graph": [H, ctypes.c_int],
+        "cpm_autotune": [H, ctypes.c_int, ip, ctypes.POINTER(ctypes.c_float)],
+        "cpm_set_variant": [H, ctypes.c_int],
+        "cpm_sweep_config": [H, ip, ip, ip, ip, ip, ip],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -242,6 +246,27 @@ class _Engine:
     def run_mcs(self, mcs):
         """Enqueue `mcs` Monte Carlo steps (asynchronous)."""
         self._call("cpm_run", int(mcs))
+
+    def run_graph(self, mcs):
+        """Enqueue `mcs` MCS as one replay of a captured CUDA graph."""
+        self._call("cpm_run_graph", int(mcs))
+
+    def autotune(self, probe_mcs=2):
+        """Pick the fastest tile variant on the current state (state kept).
+        Returns (variant, ms per MCS)."""
+        v, ms = ctypes.c_int(), ctypes.c_float()
+        self._call("cpm_autotune", int(probe_mcs), ctypes.byref(v), ctypes.byref(ms))
+        return v.value, ms.value
+
+    def set_variant(self, variant):
+        self._call("cpm_set_variant", int(variant))
+
+    def sweep_config(self):
+        """dict(variant, tile, warps_per_block, grid) of the launch runs use."""
+        vals = [ctypes.c_int() for _ in range(6)]
+        self._call("cpm_sweep_config", *[ctypes.byref(v) for v in vals])
+        v, tx, ty, tz, w, g = (x.value for x in vals)
+        return {"variant": v, "tile": (tx, ty, tz), "warps_per_block": w, "grid": g}
 
 
 class Cpm(_Engine):

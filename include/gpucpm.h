@@ -146,6 +146,31 @@ int cpm_pull(cpm_handle* h);
  * reference's run() have no meaning here (the engine sizes its own grid). */
 int cpm_run(cpm_handle* h, int mcs);
 
+/* Same as cpm_run as one CUDA-graph launch: the first call with a given
+ * `mcs` (or after cpm_autotune / cpm_set_variant / cpm_set_stream) captures
+ * the run (barrier reset + the persistent sweep) into a graph; every call
+ * replays it.  The captured sweep reads its start time from device memory
+ * and advances it, so replays continue the Monte Carlo time like cpm_run.
+ * Needs a non-default stream (the handle's own stream qualifies).  No
+ * counterpart in the reference.  1 <= mcs <= 65536. */
+int cpm_run_graph(cpm_handle* h, int mcs);
+
+/* Project autotuner: times `probe_mcs` MCS of every compiled tile variant
+ * (warp tile shape and warps per block) on a saved copy of the current state,
+ * restores the state, and makes the fastest variant the one later runs use.
+ * The sweep's result does not depend on the variant.  *chosen (may be NULL)
+ * receives the variant, *ms_per_mcs (may be NULL) its time per MCS.  No
+ * counterpart in the reference, whose geometry is passed per run() call
+ * (src/python_wrapper.cpp:182-227). */
+int cpm_autotune(cpm_handle* h, int probe_mcs, int* chosen, float* ms_per_mcs);
+
+/* Select a tile variant explicitly (0, 1 or 2) / describe the current one:
+ * warp tile extent in targets, warps per block and grid size. */
+int cpm_set_variant(cpm_handle* h, int variant);
+int cpm_sweep_config(const cpm_handle* h, int* variant, int* tile_x,
+                     int* tile_y, int* tile_z, int* warps_per_block,
+                     int* grid);
+
 /* Replaces Cpm::synchronize (src/cpm.cu:653-655).  Waits for the handle's
  * stream and reports device-side errors (CPM_ERR_TIMEOUT, CPM_ERR_CUDA). */
 int cpm_synchronize(cpm_handle* h);
