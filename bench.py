@@ -56,8 +56,9 @@ def parse_args():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--workload", default="tissue_2d",
                    choices=["tissue_2d", "tissue_2d_8192", "tissue_3d", "sorting_2d",
-                            "ensemble"])
-    p.add_argument("--replicas", type=int, default=256, help="replicas of --workload ensemble")
+                            "ensemble", "gradient"])
+    p.add_argument("--replicas", type=int, default=None,
+                   help="replicas of --workload ensemble (256) / gradient (512)")
     p.add_argument("--mcs", type=int, default=None, help="MCS per step")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -449,7 +450,7 @@ def run_ensemble(args, world, rank, local):
 
     torch.cuda.set_device(local)
     gpucpm.set_device(local)
-    nrep = args.replicas
+    nrep = args.replicas or 256
     ws = W.ensemble_2d(nrep=nrep, seed=3)
     mcs = args.mcs or 500
     sizes = [w.lattice.shape[::-1] for w in ws]
@@ -543,6 +544,113 @@ def run_ensemble(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def run_gradient(args, world, rank, local):
+    """Differentiated ensemble: R replicas (default 512) of the 256x256
+    two-type sorting lattice (2600 cells of target area 25 on the 51x51 grid
+    of 5-strided slots), observable O = heterotypic fraction at MCS 500,
+    theta = (J_ll, J_dd, J_ld, J_lm, J_dm, lambda_area, T).
+
+    Times a forward pass alone (restart + 500 MCS + observation) against the
+    differentiated step (the same forward with score accumulation, then the
+    backward kernel through torch.autograd), and compares the likelihood-ratio
+    gradient of mean_r O with CRN central differences at +-1% of each
+    parameter.  Both estimates come with their standard errors over
+    replicas.  Each rank runs its own ensemble (stream ids offset by rank).
+    """
+    import numpy as np
+    import torch
+
+    import gpucpm
+    from gpucpm import grad as G
+    from gpucpm import workloads as W
+
+    torch.cuda.set_device(local)
+    gpucpm.set_device(local)
+    nrep = args.replicas or 512
+    mcs = args.mcs or 500
+    w = W.sorting_grid(n=256, ncells=2600, seed=0)
+    ens = G.Ensemble([w] * nrep, seed=0, stream_id=rank * nrep)
+    theta0 = ens.theta0()
+    names = ["J_ll", "J_dd", "J_ld", "J_lm", "J_dm", "lambda_area", "T"]
+
+    def fwd():
+        return ens.forward(theta0, mcs, [mcs], scores=False)[0]
+
+    def lr_step():
+        th = theta0.clone().requires_grad_(True)
+        O = G.LikelihoodRatio.apply(th, ens, mcs, [mcs])
+        O.mean().backward()
+        torch.cuda.synchronize()
+        return th.grad
+
+    for _ in range(args.warmup):
+        fwd()
+        lr_step()
+    torch.cuda.synchronize()
+    launches0 = ens.batch.kernel_launches()
+    dist_barrier(world)
+    sampler = ClockSampler(gpu_index_for(torch, local))
+    sampler.start()
+    t_fwd, t_lr = [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        fwd()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        g = lr_step()
+        t2 = time.perf_counter()
+        t_fwd.append(t1 - t0)
+        t_lr.append(t2 - t1)
+    clocks = sampler.stop()
+    dist_barrier(world)
+    launches = ens.batch.kernel_launches() - launches0
+    fwd_s = dist_max(world, statistics.median(t_fwd))
+    lr_s = dist_max(world, statistics.median(t_lr))
+
+    # standard error of the LR estimate from its per-replica terms
+    O, sc, _ = ens.forward(theta0, mcs, [mcs], scores=True)
+    o = O[:, 0].double().cpu().numpy()
+    cum = sc[:, :, :ens.nparam].double().sum(dim=1).cpu().numpy()
+    b = (o.sum() - o) / (nrep - 1)
+    terms = (o - b)[:, None] * cum
+    lr_np = terms.mean(axis=0)
+    lr_se = terms.std(axis=0, ddof=1) / np.sqrt(nrep)
+    fd, fd_per = G.crn_finite_difference(ens, theta0, mcs, rel_step=0.01, per_replica=True)
+    fd = fd.numpy()
+    fd_se = fd_per.numpy().std(axis=0, ddof=1) / np.sqrt(nrep)
+    lr = g.double().cpu().numpy()
+
+    if rank != 0:
+        return
+    sites = nrep * w.nsites
+    rel = np.abs(lr - fd) / np.maximum(np.abs(fd), 1e-30)
+    z = (lr - fd) / np.sqrt(lr_se ** 2 + fd_se ** 2)
+    per_param = {n: {"theta": float(theta0[k]), "lr": float(lr[k]), "lr_se": float(lr_se[k]),
+                     "fd": float(fd[k]), "fd_se": float(fd_se[k]), "rel_diff": float(rel[k]),
+                     "z": float(z[k])}
+                 for k, n in enumerate(names)}
+    line = {"metric": METRIC, "value": sites * mcs * world / lr_s, "unit": UNIT,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": lr_s * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u32+f32", "data": "synthetic (seeded sorting grid)",
+            "config": {"workload": f"gradient: {nrep} replicas of sorting_grid 256x256, "
+                                   "2600 cells of target area 25, O = heterotypic fraction "
+                                   f"at MCS {mcs}", "sites": sites, "mcs_per_step": mcs,
+                       "l2": "inputs larger than L2 (no flush)", "seed": 0},
+            "gradient": {"forward_ms": fwd_s * 1e3, "forward_scores_backward_ms": lr_s * 1e3,
+                         "cost_ratio": lr_s / fwd_s,
+                         "lr_matches_autograd": bool(np.allclose(lr_np, lr, rtol=1e-3,
+                                                                 atol=1e-3 * np.abs(lr).max())),
+                         "fd_step": "central, +-1% of each parameter, common random numbers",
+                         "params": per_param,
+                         "max_rel_diff": float(rel.max()),
+                         "within_5pct": [n for k, n in enumerate(names) if rel[k] <= 0.05]},
+            "timing": "wall clock of whole forward / differentiated steps (median), "
+                      "each including restart (H2D of the initial lattices) and observation",
+            "gpu_launches": int(launches), "clocks": clocks, "e2e": None}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     world, rank, local = dist_setup()
@@ -550,6 +658,8 @@ def main():
         run_reference(args, world, rank)
     elif args.workload == "ensemble":
         run_ensemble(args, world, rank, local)
+    elif args.workload == "gradient":
+        run_gradient(args, world, rank, local)
     else:
         run_ours(args, world, rank, local)
     if world > 1:

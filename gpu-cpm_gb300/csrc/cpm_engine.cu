@@ -774,6 +774,91 @@ int cpm_autotune(cpm_handle* h, int probe_mcs, int* chosen, float* ms_per_mcs) {
   return CPM_OK;
 }
 
+static_assert(sizeof(cpm_score_spec) == sizeof(ScoreSpec), "score spec layout");
+static_assert(CPM_SCORE_MAX == kScoreMax, "score width");
+
+int cpm_run_scores(cpm_handle* h, int mcs, float* d_scores, uint64_t score_base,
+                   int score_len, const cpm_score_spec* spec) {
+  CPM_BIND(h);
+  if (h->ndim != 2) return h->fail(CPM_ERR_UNSUPPORTED, "scores are computed for 2D engines");
+  if (mcs < 0 || !d_scores || !spec || score_len < 0)
+    return h->fail(CPM_ERR_INVALID, "cpm_run_scores: bad arguments");
+  if (!h->pushed) return h->fail(CPM_ERR_STATE, "run before a successful push_to_gpu()");
+  ScoreSpec sp;
+  std::memcpy(&sp, spec, sizeof sp);
+  if (sp.n_pairs < 0 || sp.n_pairs > kScorePairsMax ||
+      sp.n_pairs + (sp.lambda_area ? 1 : 0) + (sp.lambda_perim ? 1 : 0) +
+              (sp.temperature ? 1 : 0) > kScoreMax)
+    return h->fail(CPM_ERR_INVALID, "cpm_run_scores: too many score parameters");
+  for (int k = 0; k < sp.n_pairs; ++k)
+    if (sp.pair_a[k] < 0 || sp.pair_a[k] >= kScoreTypes || sp.pair_b[k] < 0 ||
+        sp.pair_b[k] >= kScoreTypes)
+      return h->fail(CPM_ERR_INVALID, "cpm_run_scores: score types must be < %d", kScoreTypes);
+  if (mcs == 0) return CPM_OK;
+  if (int rc = upload_params(h)) return rc;
+  SweepArgs a = sweep_args(h, h->variant);
+  a.scores = d_scores;
+  a.score_base = score_base;
+  a.score_len = score_len;
+  a.score_spec = sp;
+  int left = mcs;
+  while (left > 0) {
+    const int chunk = std::min(left, kMaxMcsPerLaunch);
+    a.tick0 = h->tick;
+    a.mcs = chunk;
+    CPM_CUDA(h, cudaMemsetAsync(h->d_ctl, 0, sizeof(uint32_t) * kCtlErr, h->stream));
+    CPM_CUDA(h, launch_sweep(h->ndim, any_perimeter(h), h->variant, a,
+                             h->cfg[h->variant].grid, h->stream, true));
+    h->launches += 1;
+    h->tick += (uint64_t)chunk;
+    left -= chunk;
+  }
+  h->d_tick_stale = true;
+  count_attempts(h, mcs);
+  return CPM_OK;
+}
+
+int cpm_observe_heterotypic(cpm_handle* h, float* out_host) {
+  CPM_BIND(h);
+  if (h->ndim != 2) return h->fail(CPM_ERR_UNSUPPORTED, "2D engines only");
+  if (!out_host) return h->fail(CPM_ERR_INVALID, "out_host is NULL");
+  unsigned long long* counts = nullptr;
+  CPM_CUDA(h, cudaMallocAsync((void**)&counts, sizeof(unsigned long long) * 2 * h->nrep,
+                              h->stream));
+  cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(unsigned long long) * 2 * h->nrep, h->stream);
+  if (e == cudaSuccess)
+    e = launch_observe_heterotypic(h->d_lat, h->d_reps, h->nrep, h->total_sites, counts,
+                                   h->stream);
+  h->launches += 1;
+  std::vector<unsigned long long> c(2 * h->nrep);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(c.data(), counts, sizeof(unsigned long long) * 2 * h->nrep,
+                        cudaMemcpyDeviceToHost, h->stream);
+  cudaFreeAsync(counts, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return h->cuda_fail(e, "cpm_observe_heterotypic");
+  for (int r = 0; r < h->nrep; ++r)
+    out_host[r] = c[2 * r] ? (float)((double)c[2 * r + 1] / (double)c[2 * r]) : 0.0f;
+  return CPM_OK;
+}
+
+int cpm_lr_backward(const float* scores, const float* dl_do, const float* obs,
+                    const int* checkpoints, int nrep, int len, int nparam, int ncheck,
+                    float* grad, void* stream) {
+  if (!scores || !dl_do || !obs || !checkpoints || !grad || nrep < 1 || len < 0 ||
+      nparam < 1 || nparam > kScoreMax || ncheck < 1 || ncheck > kMaxCheckpoints) {
+    g_create_error = "cpm_lr_backward: bad arguments";
+    return CPM_ERR_INVALID;
+  }
+  cudaError_t e = launch_lr_backward(scores, dl_do, obs, checkpoints, nrep, len, nparam,
+                                     ncheck, grad, (cudaStream_t)stream);
+  if (e != cudaSuccess) {
+    g_create_error = std::string("cpm_lr_backward: ") + cudaGetErrorString(e);
+    return CPM_ERR_CUDA;
+  }
+  return CPM_OK;
+}
+
 int cpm_set_variant(cpm_handle* h, int variant) {
   if (!h) return CPM_ERR_INVALID;
   if (variant < 0 || variant >= kTileVariants)

@@ -125,6 +125,26 @@ __host__ __device__ inline int unpack_perim(unsigned long long w) {
   return (int)(uint32_t)(w >> 32);
 }
 
+// Likelihood-ratio scores: up to kScoreMax parameters per replica and MCS,
+// in the order (J pairs..., lambda_area, lambda_perim, T).  J pair k is the
+// symmetric adhesion of types (pair_a[k], pair_b[k]); only types <
+// kScoreTypes enter the derivative.  lambda_area (lambda_perim) is one value
+// shared by every cell type's area (perimeter) lambda, each type keeping its
+// own target.
+constexpr int kScoreMax = 8;
+constexpr int kScorePairsMax = 6;
+constexpr int kScoreRegs = kScorePairsMax + 3;  // pairs, lambda_area, lambda_perim, T
+constexpr int kScoreTypes = 4;
+constexpr int kMaxCheckpoints = 64;  // observation times of one backward
+struct ScoreSpec {
+  int n_pairs;
+  int pair_a[kScorePairsMax];
+  int pair_b[kScorePairsMax];
+  int lambda_area;   // 1: include d/d lambda_area
+  int lambda_perim;  // 1: include d/d lambda_perim
+  int temperature;   // 1: include d/dT
+};
+
 // Arguments of the persistent sweep kernel.
 struct SweepArgs {
   uint32_t* lat;
@@ -145,6 +165,13 @@ struct SweepArgs {
   // mcs when the launch ends.
   unsigned long long* tick_ptr;
   unsigned long long tick0;
+  // Score output (score launches only): scores[(r * score_len + tick -
+  // score_base) * kScoreMax + k] receives replica r's summed score of
+  // parameter k over the attempts of MCS `tick`.
+  float* scores;
+  unsigned long long score_base;
+  int score_len;
+  ScoreSpec score_spec;
   unsigned long long seed;
   int nrep;
   int mcs;
@@ -158,8 +185,16 @@ void set_thread_error(const char* message);
 
 // Launchers (cpm_kernels.cu).  Each returns the cudaError_t of its launch.
 cudaError_t launch_sweep(int ndim, bool perim, int variant, const SweepArgs& a,
-                         int grid, cudaStream_t s);
-int sweep_max_blocks_per_sm(int ndim, bool perim, int variant);
+                         int grid, cudaStream_t s, bool scores = false);
+int sweep_max_blocks_per_sm(int ndim, bool perim, int variant, bool scores = false);
+// checkpoints: host array of ncheck (<= kMaxCheckpoints) MCS counts.
+cudaError_t launch_lr_backward(const float* scores, const float* dl_do,
+                               const float* obs, const int* checkpoints, int nrep,
+                               int len, int nparam, int ncheck, float* grad,
+                               cudaStream_t s);
+cudaError_t launch_observe_heterotypic(const uint32_t* lat, const DevReplica* reps,
+                                       int nrep, long long total_sites,
+                                       unsigned long long* counts, cudaStream_t s);
 cudaError_t launch_barrier_probe(uint32_t* ctl, unsigned long long timeout_ns,
                                  cudaStream_t s);
 cudaError_t launch_init(int ndim, const uint32_t* lat, const DevReplica* reps,

@@ -41,6 +41,7 @@
 // Memory.  Mutable data (lattice, tables, deltas, dirty lists) is read with
 // ld.global.cg so that no SM serves a stale L1 line after a barrier; the
 // per-replica parameters are read-only for the kernel's lifetime.
+#include <algorithm>
 #include <cstdint>
 
 #include "cpm_device.cuh"
@@ -208,7 +209,32 @@ __device__ __forceinline__ void replay(const uint32_t* list, unsigned n,
   }
 }
 
-template <int NDIM, bool PERIM, int V>
+// Warp-reduces a lane's score partial sums and adds them, by lane 0, to the
+// (replica, MCS) row of the score buffer: J pairs at their index, then
+// lambda_area, lambda_perim and T in that order when enabled.  Clears the
+// partial sums.
+__device__ __forceinline__ void flush_scores(const SweepArgs& a, float* sc, int rep,
+                                             unsigned long long tick) {
+#pragma unroll
+  for (int k = 0; k < kScoreRegs; ++k)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sc[k] += __shfl_xor_sync(kFull, sc[k], o);
+  const long long row = (long long)tick - (long long)a.score_base;
+  if ((threadIdx.x & 31) == 0 && rep >= 0 && row >= 0 && row < a.score_len) {
+    float* dst = a.scores + ((long long)rep * a.score_len + row) * kScoreMax;
+    int k = 0;
+#pragma unroll
+    for (int p = 0; p < kScorePairsMax; ++p)
+      if (p < a.score_spec.n_pairs) atomicAdd(dst + k++, sc[p]);
+    if (a.score_spec.lambda_area) atomicAdd(dst + k++, sc[kScorePairsMax]);
+    if (a.score_spec.lambda_perim) atomicAdd(dst + k++, sc[kScorePairsMax + 1]);
+    if (a.score_spec.temperature) atomicAdd(dst + k++, sc[kScorePairsMax + 2]);
+  }
+#pragma unroll
+  for (int k = 0; k < kScoreRegs; ++k) sc[k] = 0.0f;
+}
+
+template <int NDIM, bool PERIM, int V, bool SCORE>
 __global__ void __launch_bounds__(kSweepThreadsMax, 1)
     sweep_kernel(const SweepArgs a) {
   using G = TileGeom<NDIM, V>;
@@ -234,6 +260,12 @@ __global__ void __launch_bounds__(kSweepThreadsMax, 1)
   unsigned episode = 0;
   int cnt_rep = -1;
   unsigned long long n_eval = 0, n_acc = 0;  // warp-uniform
+  // (score launches) per-lane score sums of replica sc_rep at MCS sc_tick
+  float sc[kScoreRegs];
+#pragma unroll
+  for (int k = 0; k < kScoreRegs; ++k) sc[k] = 0.0f;
+  int sc_rep = -1;
+  unsigned long long sc_tick = 0;
   if (tid < 2) s_cnt[tid] = 0;
   // Every block reads *tick_ptr before its first barrier arrival, and block
   // 0 advances it only after the last barrier, so all blocks see one value.
@@ -277,6 +309,11 @@ __global__ void __launch_bounds__(kSweepThreadsMax, 1)
           }
           n_eval = n_acc = 0;
           cnt_rep = r;
+        }
+        if (SCORE && (r != sc_rep || tick != sc_tick)) {  // warp-uniform
+          flush_scores(a, sc, sc_rep, sc_tick);
+          sc_rep = r;
+          sc_tick = tick;
         }
         const DevParams* P = a.params + r;
         const int nx = __ldg(&a.reps[r].nx), ny = __ldg(&a.reps[r].ny),
@@ -393,6 +430,9 @@ __global__ void __launch_bounds__(kSweepThreadsMax, 1)
               const unsigned long long apt = t ? __ldcg(pt.rap + rt) : 0ull;
               float e_old = 0.0f, e_new = 0.0f;
               int cnt_s = 0, cnt_t = 0;
+              // (score launches) neighbours by type < kScoreTypes, one byte
+              // per type: of the new configuration (n != s), of the old (n != t)
+              unsigned by_new = 0, by_old = 0;
 #pragma unroll
               for (int k = 0; k < NB; ++k) {
                 const uint32_t v = ws.tile[c + S::nb_offset(k)];
@@ -401,6 +441,10 @@ __global__ void __launch_bounds__(kSweepThreadsMax, 1)
                 if (v != s) e_new = __fadd_rn(e_new, __ldg(&P->J[ts * kMaxTypes + tn]));
                 cnt_s += v == s;
                 cnt_t += v == t;
+                if (SCORE && tn < kScoreTypes) {
+                  if (v != s) by_new += 1u << (8 * tn);
+                  if (v != t) by_old += 1u << (8 * tn);
+                }
               }
               float dH = __fsub_rn(e_new, e_old);
               const int dps = NB - 2 * cnt_s;
@@ -429,6 +473,7 @@ __global__ void __launch_bounds__(kSweepThreadsMax, 1)
               }
               const float T = __ldg(&P->temperature);
               bool ok;
+              float ex = 1.0f;  // exp(-dH/T) when 0 <= dH and T > 0
               if (dH < 0.0f) {
                 ok = true;
               } else if (!(T > 0.0f)) {
@@ -436,7 +481,47 @@ __global__ void __launch_bounds__(kSweepThreadsMax, 1)
               } else {
                 const float u =
                     __fmul_rn(__uint2float_rn((entry.y >> 8) | 1u), 0x1p-24f);
-                ok = u < exp_neg(__fdiv_rn(-dH, T));
+                ex = exp_neg(__fdiv_rn(-dH, T));
+                ok = u < ex;
+              }
+              if (SCORE && dH > 0.0f && T > 0.0f) {
+                // d log P(decision) / d theta with P(accept) = exp(-dH/T):
+                // accept: -g, reject: e/(1-e) g, g = d(dH/T)/d theta.
+                const float x = dH / T;
+                const float om = x < 1e-2f
+                                     ? x * (1.0f - 0.5f * x * (1.0f - (x / 3.0f) *
+                                                                          (1.0f - 0.25f * x)))
+                                     : 1.0f - ex;  // 1 - exp(-x)
+                const float cT = (ok ? -1.0f : ex / om) / T;
+#pragma unroll
+                for (int p = 0; p < kScorePairsMax; ++p) {
+                  if (p < a.score_spec.n_pairs) {
+                    const int pa = a.score_spec.pair_a[p], pb = a.score_spec.pair_b[p];
+                    int d = 0;
+                    if (ts == pa) d += (by_new >> (8 * pb)) & 0xFF;
+                    if (pa != pb && ts == pb) d += (by_new >> (8 * pa)) & 0xFF;
+                    if (tt == pa) d -= (by_old >> (8 * pb)) & 0xFF;
+                    if (pa != pb && tt == pb) d -= (by_old >> (8 * pa)) & 0xFF;
+                    sc[p] += cT * (float)d;
+                  }
+                }
+                if (a.score_spec.lambda_area) {
+                  const int da =
+                      (s ? 1 + 2 * (unpack_area(aps) - __ldg(&P->tgt_area[ts])) : 0) +
+                      (t ? 1 - 2 * (unpack_area(apt) - __ldg(&P->tgt_area[tt])) : 0);
+                  sc[kScorePairsMax] += cT * (float)da;
+                }
+                if (a.score_spec.lambda_perim) {
+                  const long long dp =
+                      (s ? (long long)dps * (2LL * (unpack_perim(aps) -
+                                                    __ldg(&P->tgt_perim[ts])) + dps)
+                         : 0LL) +
+                      (t ? (long long)dpt * (2LL * (unpack_perim(apt) -
+                                                    __ldg(&P->tgt_perim[tt])) + dpt)
+                         : 0LL);
+                  sc[kScorePairsMax + 1] += cT * __ll2float_rn(dp);
+                }
+                if (a.score_spec.temperature) sc[kScorePairsMax + 2] -= cT * x;
               }
               if (ok) {
                 accepted = true;
@@ -492,6 +577,7 @@ __global__ void __launch_bounds__(kSweepThreadsMax, 1)
     if (n_eval) atomicAdd(&a.counters[2 * cnt_rep], n_eval);
     if (n_acc) atomicAdd(&a.counters[2 * cnt_rep + 1], n_acc);
   }
+  if (SCORE) flush_scores(a, sc, sc_rep, sc_tick);
   if (a.tick_ptr && blockIdx.x == 0 && tid == 0 && a.mcs > 0)
     *a.tick_ptr = s_tick0 + (unsigned long long)a.mcs;
 }
@@ -582,27 +668,146 @@ __global__ void barrier_probe(uint32_t* ctl, unsigned long long timeout_ns) {
 }
 
 template <int NDIM, int V>
-const void* sweep_fn_v(bool perim) {
-  return perim ? (const void*)sweep_kernel<NDIM, true, V>
-               : (const void*)sweep_kernel<NDIM, false, V>;
+const void* sweep_fn_v(bool perim, bool scores) {
+  if constexpr (NDIM == 2) {
+    if (scores)
+      return perim ? (const void*)sweep_kernel<NDIM, true, V, true>
+                   : (const void*)sweep_kernel<NDIM, false, V, true>;
+  }
+  return perim ? (const void*)sweep_kernel<NDIM, true, V, false>
+               : (const void*)sweep_kernel<NDIM, false, V, false>;
 }
 
-const void* sweep_fn(int ndim, bool perim, int variant) {
+// Score launches exist for 2D lattices (the differentiable ensembles).
+const void* sweep_fn(int ndim, bool perim, int variant, bool scores) {
   if (ndim == 2) {
     switch (variant) {
-      case 1: return sweep_fn_v<2, 1>(perim);
-      case 2: return sweep_fn_v<2, 2>(perim);
-      default: return sweep_fn_v<2, 0>(perim);
+      case 1: return sweep_fn_v<2, 1>(perim, scores);
+      case 2: return sweep_fn_v<2, 2>(perim, scores);
+      default: return sweep_fn_v<2, 0>(perim, scores);
     }
   }
   switch (variant) {
-    case 1: return sweep_fn_v<3, 1>(perim);
-    case 2: return sweep_fn_v<3, 2>(perim);
-    default: return sweep_fn_v<3, 0>(perim);
+    case 1: return sweep_fn_v<3, 1>(perim, false);
+    case 2: return sweep_fn_v<3, 2>(perim, false);
+    default: return sweep_fn_v<3, 0>(perim, false);
+  }
+}
+
+// ---- likelihood-ratio backward ---------------------------------------------
+struct Checkpoints {
+  int n;
+  int t[kMaxCheckpoints];
+};
+
+// grad[k] = sum_r sum_c dL/dO[r][c] (O[r][c] - b[r][c])
+//                     * sum_{t < checkpoints[c]} scores[r][t][k]
+// with the leave-one-out baseline b[r][c] = mean of O[.][c] over the other
+// replicas (0 for a single replica), so that each replica's term is an
+// unbiased estimate of dE[O]/dtheta scaled by dL/dO[r][c].
+// One block per parameter k; threads stride over replicas, each walking its
+// replica's scores once in time order while passing the checkpoints.
+__global__ void lr_backward_kernel(const float* __restrict__ scores,
+                                   const float* __restrict__ dl_do,
+                                   const float* __restrict__ obs, const Checkpoints cp,
+                                   int nrep, int len, float* grad) {
+  const int ncheck = cp.n;
+  const int k = blockIdx.x;
+  __shared__ float s_mean[kMaxCheckpoints];  // sum over replicas
+  __shared__ float s_red[32];
+  for (int c = threadIdx.x; c < ncheck; c += blockDim.x) {
+    float m = 0.0f;
+    for (int r = 0; r < nrep; ++r) m += obs[(long long)r * ncheck + c];
+    s_mean[c] = m;
+  }
+  __syncthreads();
+  float acc = 0.0f;
+  for (int r = threadIdx.x; r < nrep; r += blockDim.x) {
+    float cum = 0.0f;
+    int t = 0;
+    for (int c = 0; c < ncheck; ++c) {
+      const int upto = min(cp.t[c], len);
+      for (; t < upto; ++t) cum += scores[((long long)r * len + t) * kScoreMax + k];
+      const long long rc = (long long)r * ncheck + c;
+      const float o = obs[rc];
+      const float dev = nrep > 1 ? o - (s_mean[c] - o) / (float)(nrep - 1) : o;
+      acc += dl_do[rc] * dev * cum;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
+  if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    float v = threadIdx.x < (int)(blockDim.x >> 5) ? s_red[threadIdx.x] : 0.0f;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+    if (threadIdx.x == 0) grad[k] = v;
+  }
+}
+
+// ---- sorting order parameter -------------------------------------------------
+// Per replica: number of Moore neighbour pairs (each pair once) of two
+// different non-medium cells, and how many of them join cells of different
+// types.  counts[2 r] = all such pairs, counts[2 r + 1] = heterotypic ones.
+__global__ void observe_heterotypic_kernel(const uint32_t* __restrict__ lat,
+                                           const DevReplica* __restrict__ reps, int nrep,
+                                           long long total,
+                                           unsigned long long* counts) {
+  for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total;
+       g += (long long)gridDim.x * blockDim.x) {
+    const int r = find_site_replica(reps, nrep, g);
+    const DevReplica R = reps[r];
+    const long long local = g - R.lat_off;
+    const int x = (int)(local % R.nx), y = (int)((local / R.nx) % R.ny);
+    const uint32_t v = lat[g];
+    unsigned pairs = 0, hetero = 0;
+    if (v & 0xFFFFFFu) {
+      // forward half of the Moore neighbourhood: (0,1), (1,-1), (1,0), (1,1)
+      const int dys[4] = {0, 1, 1, 1}, dxs[4] = {1, -1, 0, 1};
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        int xx = x + dxs[k], yy = y + dys[k];
+        xx = xx < 0 ? xx + R.nx : (xx >= R.nx ? xx - R.nx : xx);
+        yy = yy >= R.ny ? yy - R.ny : yy;
+        const uint32_t w = lat[R.lat_off + (long long)yy * R.nx + xx];
+        if ((w & 0xFFFFFFu) && w != v) {
+          ++pairs;
+          hetero += (w >> 24) != (v >> 24);
+        }
+      }
+    }
+    if (pairs) {
+      atomicAdd(&counts[2 * r], (unsigned long long)pairs);
+      if (hetero) atomicAdd(&counts[2 * r + 1], (unsigned long long)hetero);
+    }
   }
 }
 
 }  // namespace
+
+cudaError_t launch_lr_backward(const float* scores, const float* dl_do,
+                               const float* obs, const int* checkpoints, int nrep,
+                               int len, int nparam, int ncheck, float* grad,
+                               cudaStream_t s) {
+  if (ncheck < 1 || ncheck > kMaxCheckpoints || nparam < 1 || nparam > kScoreMax)
+    return cudaErrorInvalidValue;
+  Checkpoints cp;
+  cp.n = ncheck;
+  for (int c = 0; c < ncheck; ++c) cp.t[c] = checkpoints[c];
+  lr_backward_kernel<<<nparam, 256, 0, s>>>(scores, dl_do, obs, cp, nrep, len, grad);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_observe_heterotypic(const uint32_t* lat, const DevReplica* reps,
+                                       int nrep, long long total_sites,
+                                       unsigned long long* counts, cudaStream_t s) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long want = (total_sites + 255) / 256;
+  const int grid = (int)std::max(1LL, std::min<long long>(want, (long long)sms * 8));
+  observe_heterotypic_kernel<<<grid, 256, 0, s>>>(lat, reps, nrep, total_sites, counts);
+  return cudaGetLastError();
+}
 
 SweepShape sweep_shape(int ndim, int variant) {
   if (ndim == 2) {
@@ -619,9 +824,9 @@ SweepShape sweep_shape(int ndim, int variant) {
   }
 }
 
-int sweep_max_blocks_per_sm(int ndim, bool perim, int variant) {
+int sweep_max_blocks_per_sm(int ndim, bool perim, int variant, bool scores) {
   const SweepShape sh = sweep_shape(ndim, variant);
-  const void* fn = sweep_fn(ndim, perim, variant);
+  const void* fn = sweep_fn(ndim, perim, variant, scores);
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)sh.smem) != cudaSuccess)
     return 0;
@@ -633,11 +838,16 @@ int sweep_max_blocks_per_sm(int ndim, bool perim, int variant) {
 }
 
 cudaError_t launch_sweep(int ndim, bool perim, int variant, const SweepArgs& a,
-                         int grid, cudaStream_t s) {
+                         int grid, cudaStream_t s, bool scores) {
   const SweepShape sh = sweep_shape(ndim, variant);
+  const void* fn = sweep_fn(ndim, perim, variant, scores);
+  if (scores) {  // the score kernels get their shared-memory attribute on first use
+    const cudaError_t e = cudaFuncSetAttribute(
+        fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem);
+    if (e != cudaSuccess) return e;
+  }
   void* args[] = {const_cast<SweepArgs*>(&a)};
-  return cudaLaunchCooperativeKernel(sweep_fn(ndim, perim, variant), dim3(grid),
-                                     dim3(32 * sh.warps), args, sh.smem, s);
+  return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(32 * sh.warps), args, sh.smem, s);
 }
 
 cudaError_t launch_barrier_probe(uint32_t* ctl, unsigned long long timeout_ns,

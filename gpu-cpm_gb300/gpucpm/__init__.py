@@ -55,6 +55,31 @@ class _Counters(ctypes.Structure):
                 ("accepted", ctypes.c_uint64)]
 
 
+SCORE_MAX = 8
+
+
+class ScoreSpec(ctypes.Structure):
+    """cpm_score_spec: J type pairs, then lambda_area, lambda_perim, T (flags)."""
+    _fields_ = [("n_pairs", ctypes.c_int), ("pair_a", ctypes.c_int * 6),
+                ("pair_b", ctypes.c_int * 6), ("lambda_area", ctypes.c_int),
+                ("lambda_perim", ctypes.c_int), ("temperature", ctypes.c_int)]
+
+    @classmethod
+    def make(cls, pairs, lambda_area=True, temperature=True, lambda_perim=False):
+        s = cls()
+        s.n_pairs = len(pairs)
+        for k, (a, b) in enumerate(pairs):
+            s.pair_a[k], s.pair_b[k] = int(a), int(b)
+        s.lambda_area = 1 if lambda_area else 0
+        s.lambda_perim = 1 if lambda_perim else 0
+        s.temperature = 1 if temperature else 0
+        return s
+
+    @property
+    def nparam(self):
+        return self.n_pairs + self.lambda_area + self.lambda_perim + self.temperature
+
+
 class StaticParams(ctypes.Structure):
     """cpm_static_params of include/gpucpm.h (parameters of sweep_static)."""
     _fields_ = [("J", ctypes.c_float * (MAX_TYPES * MAX_TYPES)),
@@ -123,6 +148,9 @@ def library():
         "cpm_autotune": [H, ctypes.c_int, ip, ctypes.POINTER(ctypes.c_float)],
         "cpm_set_variant": [H, ctypes.c_int],
         "cpm_sweep_config": [H, ip, ip, ip, ip, ip, ip],
+        "cpm_run_scores": [H, ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int,
+                           ctypes.POINTER(ScoreSpec)],
+        "cpm_observe_heterotypic": [H, ctypes.c_void_p],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -132,6 +160,9 @@ def library():
         ctypes.c_int, ctypes.POINTER(StaticParams), ctypes.c_uint64, ctypes.c_uint32,
         ctypes.c_uint64, ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]
     L.cpm_sweep_static.restype = ctypes.c_int
+    L.cpm_lr_backward.argtypes = [ctypes.c_void_p] * 3 + [ctypes.POINTER(ctypes.c_int)] + [
+        ctypes.c_int] * 4 + [ctypes.c_void_p, ctypes.c_void_p]
+    L.cpm_lr_backward.restype = ctypes.c_int
     L.cpm_set_device.argtypes = [ctypes.c_int]
     L.cpm_set_device.restype = ctypes.c_int
     L.cpm_debug_barrier_timeout.argtypes = [ctypes.c_uint64, ip]
@@ -260,6 +291,19 @@ class _Engine:
 
     def set_variant(self, variant):
         self._call("cpm_set_variant", int(variant))
+
+    def run_scores(self, mcs, scores_ptr, score_base, score_len, spec):
+        """cpm_run plus likelihood-ratio scores into a device float buffer
+        [n_replicas][score_len][SCORE_MAX] (2D engines)."""
+        self._call("cpm_run_scores", int(mcs), ctypes.c_void_p(int(scores_ptr)),
+                   ctypes.c_uint64(int(score_base)), int(score_len), ctypes.byref(spec))
+
+    def observe_heterotypic(self):
+        """Per replica: fraction of Moore pairs of two different cells whose
+        types differ (the sorting order parameter).  Synchronous."""
+        out = np.empty(self.n_replicas, np.float32)
+        self._call("cpm_observe_heterotypic", out.ctypes.data)
+        return out
 
     def sweep_config(self):
         """dict(variant, tile, warps_per_block, grid) of the launch runs use."""
@@ -456,6 +500,20 @@ def sweep_static(dimensionality, shape, number_of_cells, lattice_ptr, area_ptr,
         int(seed), int(stream_id), int(tick), int(mcs),
         ctypes.c_void_p(int(stream) if stream else None), c), None)
     return int(c[0]), int(c[1])
+
+
+def lr_backward(scores_ptr, dl_do_ptr, obs_ptr, checkpoints, nrep, length, nparam,
+                grad_ptr, stream=None):
+    """Backward kernel of the likelihood-ratio estimator (device pointers):
+    grad[k] = sum_r sum_c dL/dO[r,c] (O[r,c] - b[r,c])
+                        * sum_{t < checkpoints[c]} scores[r,t,k],
+    b[r,c] = mean of O[.,c] over the other replicas (0 for one replica)."""
+    cp = (ctypes.c_int * len(checkpoints))(*[int(c) for c in checkpoints])
+    _check(library().cpm_lr_backward(
+        ctypes.c_void_p(int(scores_ptr)), ctypes.c_void_p(int(dl_do_ptr)),
+        ctypes.c_void_p(int(obs_ptr)), cp, int(nrep), int(length), int(nparam),
+        len(checkpoints), ctypes.c_void_p(int(grad_ptr)),
+        ctypes.c_void_p(int(stream) if stream else None)), None)
 
 
 def set_device(device):

@@ -220,6 +220,52 @@ int cpm_reset_counters(cpm_handle* h);
 int cpm_info(const cpm_handle* h, int* n_replicas, int* dimensionality,
              int* sweep_grid, uint64_t* kernel_launches);
 
+/* ---- likelihood-ratio gradients (no counterpart in the reference) ------- */
+
+/* Parameters the scores differentiate, in this order: J of symmetric type
+ * pairs (pair_a[k], pair_b[k]) for k < n_pairs (types < 4); then, each if
+ * enabled, one lambda_area shared by all cell types, one lambda_perim shared
+ * by all cell types (every type keeps its own area / perimeter target), and
+ * the temperature.  At most CPM_SCORE_MAX parameters. */
+#define CPM_SCORE_MAX 8
+typedef struct {
+    int n_pairs;
+    int pair_a[6];
+    int pair_b[6];
+    int lambda_area;
+    int lambda_perim;
+    int temperature;
+} cpm_score_spec;
+
+/* cpm_run that also accumulates, per replica and MCS, the likelihood-ratio
+ * score sum_attempts d log P(decision | theta) / d theta of every attempt
+ * with dH > 0 (P(accept) = exp(-dH/T)); attempts with dH <= 0 are accepted
+ * with probability 1 and score 0.  The lattice evolves exactly as under
+ * cpm_run.  d_scores (device, float) is [n_replicas][score_len][CPM_SCORE_MAX];
+ * the MCS with tick t adds into row t - score_base (rows outside
+ * [0, score_len) are skipped).  2D engines only.  Asynchronous. */
+int cpm_run_scores(cpm_handle* h, int mcs, float* d_scores, uint64_t score_base,
+                   int score_len, const cpm_score_spec* spec);
+
+/* Sorting order parameter of every replica: the fraction of Moore neighbour
+ * pairs of two different non-medium cells that join cells of different
+ * types.  out_host receives n_replicas floats.  2D engines only.
+ * Synchronous. */
+int cpm_observe_heterotypic(cpm_handle* h, float* out_host);
+
+/* Backward of the likelihood-ratio estimator, on the GPU:
+ *   grad[k] = sum_r sum_c dl_do[r][c] (obs[r][c] - b[r][c])
+ *                     * sum_{t < checkpoints[c]} scores[r][t][k]
+ * with the leave-one-out baseline b[r][c] = mean of obs[.][c] over the
+ * other replicas (0 when R = 1).  For a loss L = mean_r f(obs[r]) this is
+ * an unbiased estimate of dE[f]/dtheta.  scores, dl_do, obs and
+ * grad are device pointers ([R][len][CPM_SCORE_MAX], [R][ncheck], [R][ncheck],
+ * [nparam]); checkpoints is a host array of ncheck (<= 64) MCS counts.
+ * Enqueued on `stream` (NULL: default stream). */
+int cpm_lr_backward(const float* scores, const float* dl_do, const float* obs,
+                    const int* checkpoints, int nrep, int len, int nparam,
+                    int ncheck, float* grad, void* stream);
+
 /* ---- sweep without allocation ------------------------------------------ */
 
 /* Size limits of cpm_sweep_static (its working memory is a fixed array). */

@@ -30,6 +30,25 @@ class Params(ctypes.Structure):
     ]
 
 
+class ScoreSpec(ctypes.Structure):
+    """Layout of cpm_score_spec: J type pairs, lambda_area, lambda_perim and
+    T flags."""
+    _fields_ = [("n_pairs", ctypes.c_int), ("pair_a", ctypes.c_int * 6),
+                ("pair_b", ctypes.c_int * 6), ("lambda_area", ctypes.c_int),
+                ("lambda_perim", ctypes.c_int), ("temperature", ctypes.c_int)]
+
+    @classmethod
+    def make(cls, pairs, lambda_area=True, temperature=True, lambda_perim=False):
+        s = cls()
+        s.n_pairs = len(pairs)
+        for k, (a, b) in enumerate(pairs):
+            s.pair_a[k], s.pair_b[k] = int(a), int(b)
+        s.lambda_area = 1 if lambda_area else 0
+        s.lambda_perim = 1 if lambda_perim else 0
+        s.temperature = 1 if temperature else 0
+        return s
+
+
 _lib = None
 
 
@@ -49,6 +68,8 @@ def lib():
                               ctypes.c_void_p, ctypes.c_void_p,
                               ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int,
                               ctypes.c_int, ctypes.c_void_p]
+        l.orc_run_scores.argtypes = l.orc_run.argtypes + [ctypes.c_void_p,
+                                                          ctypes.c_void_p]
         _lib = l
     return _lib
 
@@ -126,6 +147,19 @@ class OracleSim:
                       int(nthreads), self.counters.ctypes.data)
         self.tick += int(mcs)
         return self
+
+    def run_scores(self, mcs: int, spec, nthreads: int = 0):
+        """run() that also returns the FP64 likelihood-ratio scores, one row
+        of 8 (parameters in the spec's order) per MCS.  `spec` is a
+        ctypes structure with cpm_score_spec's layout."""
+        scores = np.zeros((int(mcs), 8), np.float64)
+        lib().orc_run_scores(ctypes.byref(self.params), self.lattice.ctypes.data,
+                             self.area.ctypes.data, self.perim.ctypes.data,
+                             self.csum.ctypes.data, self.tick, int(mcs),
+                             int(nthreads), self.counters.ctypes.data,
+                             ctypes.byref(spec), scores.ctypes.data)
+        self.tick += int(mcs)
+        return scores
 
     def recount(self):
         """Tables recomputed from scratch from the current lattice."""

@@ -151,12 +151,56 @@ struct Tables {
   int64_t* csum;
 };
 
+// Parameters the likelihood-ratio scores differentiate (layout of
+// cpm_score_spec): J of symmetric type pairs, then a lambda_area and a
+// lambda_perim shared by all cell types, then T.  Score slots: pairs at
+// 0..5, lambda_area at 6, lambda_perim at 7, T at 8.
+constexpr int kScoreSlots = 9;
+struct ScoreSpec {
+  int n_pairs;
+  int pair_a[6];
+  int pair_b[6];
+  int lambda_area;
+  int lambda_perim;
+  int temperature;
+};
+
+// d log P(decision)/d theta of one evaluated attempt with dH > 0, in FP64
+// from the attempt's (FP32) decision: P(accept) = exp(-x), x = dH / T;
+// accept contributes -dx/dtheta, reject exp(-x)/(1-exp(-x)) dx/dtheta.
+// dx/dJ_ab = (changes of the a-b contact count) / T, dx/dlambda_area and
+// dx/dlambda_perim = (the integer area / perimeter terms) / T, dx/dT = -x / T.
+void add_score(const ScoreSpec& sp, const uint32_t* nb, int N, uint32_t s, uint32_t t,
+               int64_t da, int64_t dp, double dH, double T, bool accepted,
+               double* sc) {
+  const double x = dH / T;
+  const double coef = accepted ? -1.0 : std::exp(-x) / -std::expm1(-x);
+  const double cT = coef / T;
+  const int ts = (int)(s >> 24), tt = (int)(t >> 24);
+  for (int k = 0; k < sp.n_pairs; ++k) {
+    const int a = sp.pair_a[k], b = sp.pair_b[k];
+    int d = 0;
+    for (int m = 0; m < N; ++m) {
+      const int tn = (int)(nb[m] >> 24);
+      const bool pair_new = (ts == a && tn == b) || (a != b && ts == b && tn == a);
+      const bool pair_old = (tt == a && tn == b) || (a != b && tt == b && tn == a);
+      if (nb[m] != s && pair_new) ++d;
+      if (nb[m] != t && pair_old) --d;
+    }
+    sc[k] += cT * d;
+  }
+  if (sp.lambda_area) sc[6] += cT * (double)da;
+  if (sp.lambda_perim) sc[7] += cT * (double)dp;
+  if (sp.temperature) sc[8] += -cT * x;
+}
+
 // One copy attempt at target (x, y, z).  Returns 0 for a no-op, 1 for an
 // evaluated and rejected attempt, 2 for an accepted one (lattice written,
-// *acc filled).
+// *acc filled).  With `sp`, adds the attempt's score to sc[8].
 inline int attempt(const Params& p, uint32_t* lat, const Tables& tb, int x,
                    int y, int z, uint64_t phase, bool perim_on,
-                   Accepted* acc) {
+                   Accepted* acc, const ScoreSpec* sp = nullptr,
+                   double* sc = nullptr) {
   const int nx = p.nx, ny = p.ny, nz = p.nz;
   const int N = p.ndim == 2 ? 8 : 26;
   uint32_t nb[26];
@@ -226,6 +270,14 @@ inline int attempt(const Params& p, uint32_t* lat, const Tables& tb, int x,
   } else {
     const float u = (float)((r[1] >> 8) | 1u) * 0x1p-24f;
     ok = u < exp_neg(-dH / p.temperature);
+  }
+  if (sp && dH > 0.0f && p.temperature > 0.0f) {
+    const int64_t da = (s ? 1 + 2 * ((int64_t)tb.area[is] - p.tgt_area[ts]) : 0) +
+                       (t ? 1 - 2 * ((int64_t)tb.area[it] - p.tgt_area[tt]) : 0);
+    const int64_t dp =
+        (s ? (int64_t)dps * (2 * ((int64_t)tb.perim[is] - p.tgt_perim[ts]) + dps) : 0) +
+        (t ? (int64_t)dpt * (2 * ((int64_t)tb.perim[it] - p.tgt_perim[tt]) + dpt) : 0);
+    add_score(*sp, nb, N, s, t, da, dp, dH, p.temperature, ok, sc);
   }
   if (!ok) return 1;
 
@@ -327,12 +379,13 @@ int orc_init_tables(const orc_params* pp, const uint32_t* lat, int32_t* area,
   return 0;
 }
 
-// Run `mcs` Monte Carlo steps from tick `tick0` in place.  counters[0..2]
-// receive attempts, evaluated and accepted counts (added to).  `nthreads`
-// <= 0 uses every OpenMP thread; the result does not depend on it.
-int orc_run(const orc_params* pp, uint32_t* lat, int32_t* area, int32_t* perim,
-            int64_t* csum, uint64_t tick0, int mcs, int nthreads,
-            uint64_t* counters) {
+}  // extern "C"
+
+namespace {
+
+int run_impl(const orc_params* pp, uint32_t* lat, int32_t* area, int32_t* perim,
+             int64_t* csum, uint64_t tick0, int mcs, int nthreads,
+             uint64_t* counters, const ScoreSpec* sp, double* scores) {
   const Params& p = *pp;
   const int nx = p.nx, ny = p.ny, nz = p.ndim == 3 ? p.nz : 1;
   const int nslots = p.ndim == 2 ? 9 : 27;
@@ -340,6 +393,7 @@ int orc_run(const orc_params* pp, uint32_t* lat, int32_t* area, int32_t* perim,
   Tables tb{area, perim, csum};
   if (nthreads <= 0) nthreads = omp_get_max_threads();
   std::vector<std::vector<Accepted>> logs(nthreads);
+  std::vector<double> tsc((size_t)nthreads * kScoreSlots, 0.0);
   uint64_t n_att = 0, n_eval = 0, n_acc = 0;
   for (int m = 0; m < mcs; ++m) {
     const uint64_t tick = tick0 + (uint64_t)m;
@@ -355,7 +409,9 @@ int orc_run(const orc_params* pp, uint32_t* lat, int32_t* area, int32_t* perim,
           uint64_t e = 0, a = 0;
 #pragma omp parallel num_threads(nthreads) reduction(+ : e, a)
           {
-            std::vector<Accepted>& log = logs[omp_get_thread_num()];
+            const int th = omp_get_thread_num();
+            std::vector<Accepted>& log = logs[th];
+            double* sc = sp ? &tsc[(size_t)th * kScoreSlots] : nullptr;
             log.clear();
 #pragma omp for schedule(static)
             for (int64_t row = 0; row < nrows; ++row) {
@@ -365,7 +421,7 @@ int orc_run(const orc_params* pp, uint32_t* lat, int32_t* area, int32_t* perim,
                 const int x = class_coord(nx, cx, i);
                 Accepted acc;
                 const int res = attempt(p, lat, tb, x, y, z, phase, perim_on,
-                                        &acc);
+                                        &acc, sp, sc);
                 if (res >= 1) ++e;
                 if (res == 2) {
                   ++a;
@@ -377,6 +433,18 @@ int orc_run(const orc_params* pp, uint32_t* lat, int32_t* area, int32_t* perim,
           n_att += (uint64_t)ncx * ncy * ncz;
           n_eval += e;
           n_acc += a;
+          if (sp) {  // scores of this MCS, in the slot order of the spec
+            double* row = scores + (size_t)m * 8;
+            for (int th = 0; th < nthreads; ++th) {
+              double* sc = &tsc[(size_t)th * kScoreSlots];
+              int k = 0;
+              for (int q = 0; q < sp->n_pairs; ++q) row[k++] += sc[q];
+              if (sp->lambda_area) row[k++] += sc[6];
+              if (sp->lambda_perim) row[k++] += sc[7];
+              if (sp->temperature) row[k++] += sc[8];
+              for (int q = 0; q < kScoreSlots; ++q) sc[q] = 0.0;
+            }
+          }
           // Apply the phase's deltas; integer sums, so order is irrelevant.
           for (auto& log : logs)
             for (const Accepted& c : log) {
@@ -404,6 +472,31 @@ int orc_run(const orc_params* pp, uint32_t* lat, int32_t* area, int32_t* perim,
     counters[2] += n_acc;
   }
   return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Run `mcs` Monte Carlo steps from tick `tick0` in place.  counters[0..2]
+// receive attempts, evaluated and accepted counts (added to).  `nthreads`
+// <= 0 uses every OpenMP thread; the result does not depend on it.
+int orc_run(const orc_params* pp, uint32_t* lat, int32_t* area, int32_t* perim,
+            int64_t* csum, uint64_t tick0, int mcs, int nthreads,
+            uint64_t* counters) {
+  return run_impl(pp, lat, area, perim, csum, tick0, mcs, nthreads, counters, nullptr,
+                  nullptr);
+}
+
+// orc_run that also sums, per MCS, the likelihood-ratio score of every
+// evaluated attempt with dH > 0 (FP64, from the attempts' own decisions):
+// scores[m * 8 + k] for parameter k of the spec's order, m < mcs (added to).
+int orc_run_scores(const orc_params* pp, uint32_t* lat, int32_t* area,
+                   int32_t* perim, int64_t* csum, uint64_t tick0, int mcs,
+                   int nthreads, uint64_t* counters, const void* spec,
+                   double* scores) {
+  return run_impl(pp, lat, area, perim, csum, tick0, mcs, nthreads, counters,
+                  static_cast<const ScoreSpec*>(spec), scores);
 }
 
 }  // extern "C"

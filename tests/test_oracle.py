@@ -239,3 +239,88 @@ def _total_energy(s):
     tp = np.asarray(s.params.tgt_perim)
     e += (lp[ty[ids]] * (s.perim[ids] - tp[ty[ids]]) ** 2).sum()
     return e
+
+
+PAIRS = ((1, 1), (2, 2), (1, 2), (1, 0), (2, 0))
+
+
+def _log_p(dH, T, accepted):
+    x = dH / T
+    return -x if accepted else math.log(-math.expm1(-x))
+
+
+def test_oracle_scores_are_derivatives_of_the_decision_log_likelihood():
+    """Replay one MCS with the reference's dH formula (as above); for every
+    evaluated attempt with dH > 0 differentiate log P(its decision) by
+    central differences in each parameter, with the lattice and tables of
+    that moment held fixed, and compare the sum with the oracle's FP64
+    scores for that MCS."""
+    w = W.random_small((16, 16), 10, seed=11, temperature=6.0)
+    J = np.rint(w.J).astype(float)
+    lam_a = [0.0, 1.0, 1.0]
+    tgt_a = [0, 20, 20]
+    lam_p = [0.0, 0.5, 0.5]
+    tgt_p = [0, 18, 18]
+    T = 6.0
+    sim = oracle.OracleSim(w.lattice, w.ncells, J.astype(np.float32), lam_a, tgt_a,
+                           lam_p, tgt_p, temperature=T, seed=7)
+    spec = oracle.ScoreSpec.make(PAIRS, lambda_perim=True)
+    lat = w.lattice.copy()
+    area, perim = sim.area.copy(), sim.perim.copy()
+    n = 16
+    want = np.zeros(8)
+    evaluated_pos = 0
+
+    def dH_of(theta, ax, ay, sx, sy):
+        Jt = J.copy()
+        for k, (a, b) in enumerate(PAIRS):
+            Jt[a, b] = Jt[b, a] = theta[k]
+        la = [0.0, theta[5], theta[5]]
+        lp = [0.0, theta[6], theta[6]]
+        return _reference_dh(lat, ax, ay, sx, sy, area, perim, Jt, la, tgt_a, lp, tgt_p)
+
+    theta = np.array([J[a, b] for a, b in PAIRS] + [1.0, 0.5, T])
+    for cy in (0, 1):
+        for cx in (0, 1):
+            slot = cy * 3 + cx
+            changes = []
+            for y in range(cy, n, 2):
+                for x in range(cx, n, 2):
+                    t = int(lat[y, x])
+                    nbs = [(x + i, y + j) for j in (-1, 0, 1) for i in (-1, 0, 1)
+                           if (i, j) != (0, 0)]
+                    vals = [int(lat[b % n, a % n]) for a, b in nbs]
+                    if all(v == t for v in vals):
+                        continue
+                    r = oracle.philox4x32_10([y * n + x, slot, 0, 0], [7, 0])
+                    k = (r[0] * 8) >> 32
+                    if vals[k] == t:
+                        continue
+                    sx, sy = nbs[k][0] % n, nbs[k][1] % n
+                    dH = dH_of(theta, x, y, sx, sy)
+                    u = ((r[1] >> 8) | 1) * 2.0 ** -24
+                    acc = dH < 0 or u < math.exp(-dH / T)
+                    if dH > 0:
+                        evaluated_pos += 1
+                        for q in range(8):
+                            h = 1e-4 * max(1.0, abs(theta[q]))
+                            tp, tm = theta.copy(), theta.copy()
+                            tp[q] += h
+                            tm[q] -= h
+                            lp = _log_p(dH_of(tp, x, y, sx, sy), tp[7], acc)
+                            lm = _log_p(dH_of(tm, x, y, sx, sy), tm[7], acc)
+                            want[q] += (lp - lm) / (2 * h)
+                    if acc:
+                        changes.append((x, y, vals[k], t, vals))
+            for x, y, s, t, vals in changes:
+                lat[y, x] = s
+                if s:
+                    area[s & 0xFFFFFF] += 1
+                    perim[s & 0xFFFFFF] += 8 - 2 * sum(v == s for v in vals)
+                if t:
+                    area[t & 0xFFFFFF] -= 1
+                    perim[t & 0xFFFFFF] += 2 * sum(v == t for v in vals) - 8
+    got = sim.run_scores(1, spec)[0, :8]
+    assert evaluated_pos > 20
+    np.testing.assert_allclose(got, want, rtol=1e-5, atol=1e-6)
+    np.testing.assert_array_equal(sim.lattice, lat)
