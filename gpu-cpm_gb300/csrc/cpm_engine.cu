@@ -54,7 +54,6 @@ struct cpm_handle {
   long long* d_cs[2] = {nullptr, nullptr};
   unsigned long long* d_dap[2] = {nullptr, nullptr};
   long long* d_dcs[2] = {nullptr, nullptr};
-  uint32_t* d_dflag[2] = {nullptr, nullptr};
   uint32_t* d_dlist = nullptr;
   uint32_t* d_ctl = nullptr;
   unsigned long long* d_counters = nullptr;
@@ -63,6 +62,7 @@ struct cpm_handle {
   DevReplica* d_reps = nullptr;
   DevParams* d_params = nullptr;
   int* d_task_prefix = nullptr;
+  int* d_rep_order = nullptr;  // replicas by decreasing site count
 
   cudaStream_t stream = nullptr;      // stream work is enqueued on
   cudaStream_t own_stream = nullptr;  // created with the handle
@@ -70,12 +70,15 @@ struct cpm_handle {
   // (0 until cpm_autotune picks another).
   struct Config {
     SweepShape shape;
-    int grid = 1;
+    int grid = 1;                  // grid dispatch
     long long list_cap = 0;
+    int grid_local = 1;            // replica dispatch
+    long long list_cap_local = 0;
     std::vector<int> task_prefix;  // [27][nrep + 1] warp tiles per slot
     std::vector<int> active_slots;
   } cfg[kTileVariants];
   int variant = 0;
+  int dispatch = CPM_DISPATCH_GRID;  // CPM_DISPATCH_*
   std::vector<unsigned long long> attempts;  // per replica, host-counted
 
   // Graph-captured run (cpm_run_graph): the captured launch reads and
@@ -83,7 +86,7 @@ struct cpm_handle {
   unsigned long long* d_tick = nullptr;
   bool d_tick_stale = true;
   cudaGraphExec_t graph_exec = nullptr;
-  int graph_mcs = 0, graph_variant = -1;
+  int graph_mcs = 0, graph_variant = -1, graph_dispatch = -1;
   cudaStream_t graph_stream = nullptr;
 
   uint64_t seed = 0;
@@ -139,7 +142,6 @@ void free_all(cpm_handle* h) {
     cudaFree(h->d_cs[b]);
     cudaFree(h->d_dap[b]);
     cudaFree(h->d_dcs[b]);
-    cudaFree(h->d_dflag[b]);
   }
   cudaFree(h->d_dlist);
   cudaFree(h->d_ctl);
@@ -149,6 +151,7 @@ void free_all(cpm_handle* h) {
   cudaFree(h->d_reps);
   cudaFree(h->d_params);
   cudaFree(h->d_task_prefix);
+  cudaFree(h->d_rep_order);
   cudaFree(h->d_tick);
   if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
@@ -240,7 +243,6 @@ int build_engine(int n, int ndim, const int* nx, const int* ny, const int* nz,
     al((void**)&h->d_cs[b], sizeof(long long) * rows * ndim);
     al((void**)&h->d_dap[b], sizeof(unsigned long long) * rows);
     al((void**)&h->d_dcs[b], sizeof(long long) * rows * ndim);
-    al((void**)&h->d_dflag[b], sizeof(uint32_t) * rows);
   }
   al((void**)&h->d_ctl, sizeof(uint32_t) * kCtlWords);
   al((void**)&h->d_counters, sizeof(unsigned long long) * 2 * n);
@@ -249,6 +251,7 @@ int build_engine(int n, int ndim, const int* nx, const int* ny, const int* nz,
   al((void**)&h->d_reps, sizeof(DevReplica) * n);
   al((void**)&h->d_params, sizeof(DevParams) * n);
   al((void**)&h->d_task_prefix, sizeof(int) * kTileVariants * 27 * (n + 1));
+  al((void**)&h->d_rep_order, sizeof(int) * n);
   al((void**)&h->d_tick, sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMallocHost((void**)&h->h_lat, sizeof(uint32_t) * (sites ? sites : 1));
   if (e != cudaSuccess) {
@@ -264,6 +267,17 @@ int build_engine(int n, int ndim, const int* nx, const int* ny, const int* nz,
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
   long long dlist_entries = 1;
+  long long max_rows = 1, max_sites = 1;
+  for (const DevReplica& R : h->reps) {
+    max_rows = std::max(max_rows, (long long)R.ncells + 1);
+    max_sites = std::max(max_sites, (long long)R.nx * R.ny * R.nz);
+  }
+  std::vector<int> order(n);
+  for (int r = 0; r < n; ++r) order[r] = r;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    const DevReplica &X = h->reps[x], &Y = h->reps[y];
+    return (long long)X.nx * X.ny * X.nz > (long long)Y.nx * Y.ny * Y.nz;
+  });
   for (int v = 0; v < kTileVariants; ++v) {
     cpm_handle::Config& c = h->cfg[v];
     c.shape = sweep_shape(ndim, v);
@@ -310,6 +324,16 @@ int build_engine(int n, int ndim, const int* nx, const int* ny, const int* nz,
     const long long nt = (long long)c.shape.cx * c.shape.cy * c.shape.cz;
     c.list_cap = 2LL * nt * c.shape.warps * ((max_tasks + warps - 1) / warps);
     dlist_entries = std::max(dlist_entries, c.list_cap * 2 * c.grid);
+    // Replica dispatch: one block per replica at a time; its dirty list takes
+    // up to two rows per attempt of the replica's largest slot.
+    long long max_rep_tiles = 1;
+    for (int slot = 0; slot < 27; ++slot)
+      for (int r = 0; r < n; ++r)
+        max_rep_tiles = std::max<long long>(
+            max_rep_tiles, c.task_prefix[slot * (n + 1) + r + 1] - c.task_prefix[slot * (n + 1) + r]);
+    c.grid_local = std::min(per_sm * sms, n);
+    c.list_cap_local = n > 1 ? 2LL * nt * max_rep_tiles : 0;  // batches only
+    dlist_entries = std::max(dlist_entries, c.list_cap_local * 2 * c.grid_local);
   }
   e = cudaMalloc((void**)&h->d_dlist, sizeof(uint32_t) * dlist_entries);
   if (e != cudaSuccess) {
@@ -319,8 +343,18 @@ int build_engine(int n, int ndim, const int* nx, const int* ny, const int* nz,
     return e == cudaErrorMemoryAllocation ? CPM_ERR_ALLOC : CPM_ERR_CUDA;
   }
 
+  // Replica dispatch by default when there are replicas for every block and
+  // no replica is much larger than a block's fair share of the sites (the
+  // autotuner can change the choice).
+  h->dispatch = (n >= h->cfg[0].grid_local && n >= sms &&
+                 max_sites * (long long)h->cfg[0].grid_local <= 2 * sites)
+                    ? CPM_DISPATCH_REPLICA
+                    : CPM_DISPATCH_GRID;
   e = cudaMemcpyAsync(h->d_reps, h->reps.data(), sizeof(DevReplica) * n,
                       cudaMemcpyHostToDevice, h->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(h->d_rep_order, order.data(), sizeof(int) * n,
+                        cudaMemcpyHostToDevice, h->stream);
   for (int v = 0; v < kTileVariants && e == cudaSuccess; ++v)
     e = cudaMemcpyAsync(h->d_task_prefix + (size_t)v * 27 * (n + 1),
                         h->cfg[v].task_prefix.data(), sizeof(int) * 27 * (n + 1),
@@ -423,9 +457,9 @@ bool any_perimeter(const cpm_handle* h) {
   return false;
 }
 
-// Kernel arguments of a sweep with tile variant v (tick0 / mcs filled in by
-// the caller).
-SweepArgs sweep_args(const cpm_handle* h, int v) {
+// Kernel arguments of a sweep with tile variant v and dispatch d (tick0 /
+// mcs filled in by the caller).
+SweepArgs sweep_args(const cpm_handle* h, int v, int d) {
   SweepArgs a;
   std::memset(&a, 0, sizeof a);
   a.lat = h->d_lat;
@@ -434,11 +468,12 @@ SweepArgs sweep_args(const cpm_handle* h, int v) {
     a.cs[b] = h->d_cs[b];
     a.dap[b] = h->d_dap[b];
     a.dcs[b] = h->d_dcs[b];
-    a.dflag[b] = h->d_dflag[b];
   }
   const cpm_handle::Config& c = h->cfg[v];
   a.dlist = h->d_dlist;
-  a.list_cap = c.list_cap;
+  a.block_local = d == CPM_DISPATCH_REPLICA ? 1 : 0;
+  a.list_cap = a.block_local ? c.list_cap_local : c.list_cap;
+  a.rep_order = h->d_rep_order;
   a.ctl = h->d_ctl;
   a.counters = h->d_counters;
   a.reps = h->d_reps;
@@ -450,6 +485,10 @@ SweepArgs sweep_args(const cpm_handle* h, int v) {
   a.nslot_active = (int)c.active_slots.size();
   for (int i = 0; i < a.nslot_active; ++i) a.slots[i] = c.active_slots[i];
   return a;
+}
+
+int grid_of(const cpm_handle* h, int v, int d) {
+  return d == CPM_DISPATCH_REPLICA ? h->cfg[v].grid_local : h->cfg[v].grid;
 }
 
 void count_attempts(cpm_handle* h, int mcs) {
@@ -470,6 +509,7 @@ std::string describe_errors(uint32_t w) {
   if (w & kErrMediumType) add("a site holds id 0 with a non-zero type");
   if (w & kErrTypeConflict) add("one cell id appears with two different types");
   if (w & kErrTimeout) add("a grid barrier of the sweep timed out");
+  if (w & kErrListFull) add("a dirty list of the sweep was too small (internal error)");
   return s;
 }
 
@@ -589,7 +629,6 @@ int cpm_push(cpm_handle* h) {
     CPM_CUDA(h, cudaMemsetAsync(h->d_cs[b], 0, sizeof(long long) * h->rows * h->ndim, h->stream));
     CPM_CUDA(h, cudaMemsetAsync(h->d_dap[b], 0, sizeof(unsigned long long) * h->rows, h->stream));
     CPM_CUDA(h, cudaMemsetAsync(h->d_dcs[b], 0, sizeof(long long) * h->rows * h->ndim, h->stream));
-    CPM_CUDA(h, cudaMemsetAsync(h->d_dflag[b], 0, sizeof(uint32_t) * h->rows, h->stream));
   }
   CPM_CUDA(h, cudaMemsetAsync(h->d_first, 0xFF, sizeof(unsigned long long) * h->rows, h->stream));
   CPM_CUDA(h, cudaMemsetAsync(h->d_ctype, 0xFF, sizeof(int) * h->rows, h->stream));
@@ -629,7 +668,7 @@ int cpm_run(cpm_handle* h, int mcs) {
   if (mcs == 0) return CPM_OK;
   if (int rc = upload_params(h)) return rc;
   const bool any_perim = any_perimeter(h);
-  SweepArgs a = sweep_args(h, h->variant);
+  SweepArgs a = sweep_args(h, h->variant, h->dispatch);
   int left = mcs;
   while (left > 0) {
     const int chunk = std::min(left, kMaxMcsPerLaunch);
@@ -638,8 +677,8 @@ int cpm_run(cpm_handle* h, int mcs) {
     // Barrier counter and release flag start at zero in every launch; the
     // sticky error word is left alone until cpm_synchronize reads it.
     CPM_CUDA(h, cudaMemsetAsync(h->d_ctl, 0, sizeof(uint32_t) * kCtlErr, h->stream));
-    CPM_CUDA(h, launch_sweep(h->ndim, any_perim, h->variant, a, h->cfg[h->variant].grid,
-                             h->stream));
+    CPM_CUDA(h, launch_sweep(h->ndim, any_perim, h->variant, a,
+                             grid_of(h, h->variant, h->dispatch), h->stream));
     h->launches += 1;
     h->tick += (uint64_t)chunk;
     left -= chunk;
@@ -658,14 +697,14 @@ int cpm_run_graph(cpm_handle* h, int mcs) {
     return h->fail(CPM_ERR_STATE, "graph runs need a non-default stream");
   if (int rc = upload_params(h)) return rc;
   if (!h->graph_exec || h->graph_mcs != mcs || h->graph_variant != h->variant ||
-      h->graph_stream != h->stream) {
+      h->graph_dispatch != h->dispatch || h->graph_stream != h->stream) {
     if (h->graph_exec) {
       cudaGraphExecDestroy(h->graph_exec);
       h->graph_exec = nullptr;
     }
     // Capture: reset the barrier words, then the persistent sweep reading
     // its start time from (and advancing) the device tick.
-    SweepArgs a = sweep_args(h, h->variant);
+    SweepArgs a = sweep_args(h, h->variant, h->dispatch);
     a.tick_ptr = h->d_tick;
     a.mcs = mcs;
     cudaGraph_t g = nullptr;
@@ -673,7 +712,7 @@ int cpm_run_graph(cpm_handle* h, int mcs) {
     cudaError_t e1 = cudaMemsetAsync(h->d_ctl, 0, sizeof(uint32_t) * kCtlErr, h->stream);
     cudaError_t e2 = e1 == cudaSuccess
                          ? launch_sweep(h->ndim, any_perimeter(h), h->variant, a,
-                                        h->cfg[h->variant].grid, h->stream)
+                                        grid_of(h, h->variant, h->dispatch), h->stream)
                          : e1;
     cudaError_t e3 = cudaStreamEndCapture(h->stream, &g);
     if (e2 != cudaSuccess) return h->cuda_fail(e2, "capture of the sweep launch");
@@ -683,6 +722,7 @@ int cpm_run_graph(cpm_handle* h, int mcs) {
     if (e4 != cudaSuccess) return h->cuda_fail(e4, "cudaGraphInstantiate");
     h->graph_mcs = mcs;
     h->graph_variant = h->variant;
+    h->graph_dispatch = h->dispatch;
     h->graph_stream = h->stream;
   }
   if (h->d_tick_stale) {
@@ -736,18 +776,21 @@ int cpm_autotune(cpm_handle* h, int probe_mcs, int* chosen, float* ms_per_mcs) {
   if (e == cudaSuccess) e = cudaEventCreate(&ev[1]);
   if (e == cudaSuccess) e = copy(true);
   const uint64_t tick = h->tick;
-  const int keep = h->variant;
   float best = -1.0f;
-  int best_v = keep;
+  int best_v = h->variant, best_d = h->dispatch;
   const bool any_perim = any_perimeter(h);
-  for (int v = 0; v < kTileVariants && e == cudaSuccess; ++v) {
-    SweepArgs a = sweep_args(h, v);
+  // Every (tile variant, dispatch) pair; replica dispatch only for batches.
+  const int ndispatch = h->nrep > 1 ? 2 : 1;
+  for (int i = 0; i < kTileVariants * ndispatch && e == cudaSuccess; ++i) {
+    const int v = i % kTileVariants, d = i / kTileVariants;
+    SweepArgs a = sweep_args(h, v, d);
     a.tick0 = tick;
     a.mcs = probe_mcs;
     e = copy(false);
     if (e == cudaSuccess) e = cudaMemsetAsync(h->d_ctl, 0, sizeof(uint32_t) * kCtlErr, h->stream);
     if (e == cudaSuccess) e = cudaEventRecord(ev[0], h->stream);
-    if (e == cudaSuccess) e = launch_sweep(h->ndim, any_perim, v, a, h->cfg[v].grid, h->stream);
+    if (e == cudaSuccess)
+      e = launch_sweep(h->ndim, any_perim, v, a, grid_of(h, v, d), h->stream);
     if (e == cudaSuccess) e = cudaEventRecord(ev[1], h->stream);
     if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
     float ms = 0.0f;
@@ -756,6 +799,7 @@ int cpm_autotune(cpm_handle* h, int probe_mcs, int* chosen, float* ms_per_mcs) {
     if (e == cudaSuccess && (best < 0.0f || ms < best)) {
       best = ms;
       best_v = v;
+      best_d = d;
     }
   }
   if (e == cudaSuccess) e = copy(false);
@@ -768,6 +812,7 @@ int cpm_autotune(cpm_handle* h, int probe_mcs, int* chosen, float* ms_per_mcs) {
   if (int rc = read_error_word(h, &w)) return rc;
   if (w) return h->fail(CPM_ERR_TIMEOUT, "autotune: %s", describe_errors(w).c_str());
   h->variant = best_v;
+  h->dispatch = best_d;
   h->tick = tick;
   if (chosen) *chosen = best_v;
   if (ms_per_mcs) *ms_per_mcs = best / (float)probe_mcs;
@@ -796,7 +841,7 @@ int cpm_run_scores(cpm_handle* h, int mcs, float* d_scores, uint64_t score_base,
       return h->fail(CPM_ERR_INVALID, "cpm_run_scores: score types must be < %d", kScoreTypes);
   if (mcs == 0) return CPM_OK;
   if (int rc = upload_params(h)) return rc;
-  SweepArgs a = sweep_args(h, h->variant);
+  SweepArgs a = sweep_args(h, h->variant, h->dispatch);
   a.scores = d_scores;
   a.score_base = score_base;
   a.score_len = score_len;
@@ -808,7 +853,7 @@ int cpm_run_scores(cpm_handle* h, int mcs, float* d_scores, uint64_t score_base,
     a.mcs = chunk;
     CPM_CUDA(h, cudaMemsetAsync(h->d_ctl, 0, sizeof(uint32_t) * kCtlErr, h->stream));
     CPM_CUDA(h, launch_sweep(h->ndim, any_perimeter(h), h->variant, a,
-                             h->cfg[h->variant].grid, h->stream, true));
+                             grid_of(h, h->variant, h->dispatch), h->stream, true));
     h->launches += 1;
     h->tick += (uint64_t)chunk;
     left -= chunk;
@@ -844,14 +889,16 @@ int cpm_observe_heterotypic(cpm_handle* h, float* out_host) {
 
 int cpm_lr_backward(const float* scores, const float* dl_do, const float* obs,
                     const int* checkpoints, int nrep, int len, int nparam, int ncheck,
-                    float* grad, void* stream) {
+                    const float* obs_total, int nrep_total, float* grad, void* stream) {
   if (!scores || !dl_do || !obs || !checkpoints || !grad || nrep < 1 || len < 0 ||
-      nparam < 1 || nparam > kScoreMax || ncheck < 1 || ncheck > kMaxCheckpoints) {
+      nparam < 1 || nparam > kScoreMax || ncheck < 1 || ncheck > kMaxCheckpoints ||
+      (obs_total && nrep_total < nrep)) {
     g_create_error = "cpm_lr_backward: bad arguments";
     return CPM_ERR_INVALID;
   }
   cudaError_t e = launch_lr_backward(scores, dl_do, obs, checkpoints, nrep, len, nparam,
-                                     ncheck, grad, (cudaStream_t)stream);
+                                     ncheck, obs_total, nrep_total, grad,
+                                     (cudaStream_t)stream);
   if (e != cudaSuccess) {
     g_create_error = std::string("cpm_lr_backward: ") + cudaGetErrorString(e);
     return CPM_ERR_CUDA;
@@ -864,6 +911,16 @@ int cpm_set_variant(cpm_handle* h, int variant) {
   if (variant < 0 || variant >= kTileVariants)
     return h->fail(CPM_ERR_INVALID, "tile variant %d out of range [0, %d)", variant, kTileVariants);
   h->variant = variant;
+  return CPM_OK;
+}
+
+int cpm_set_dispatch(cpm_handle* h, int dispatch) {
+  if (!h) return CPM_ERR_INVALID;
+  if (dispatch != CPM_DISPATCH_GRID && dispatch != CPM_DISPATCH_REPLICA)
+    return h->fail(CPM_ERR_INVALID, "dispatch %d is neither grid (0) nor replica (1)", dispatch);
+  if (dispatch == CPM_DISPATCH_REPLICA && h->nrep < 2)
+    return h->fail(CPM_ERR_UNSUPPORTED, "replica dispatch needs a batch of two or more replicas");
+  h->dispatch = dispatch;
   return CPM_OK;
 }
 
@@ -1001,13 +1058,13 @@ int cpm_info(const cpm_handle* h, int* n_replicas, int* dimensionality,
   if (!h) return CPM_ERR_INVALID;
   if (n_replicas) *n_replicas = h->nrep;
   if (dimensionality) *dimensionality = h->ndim;
-  if (sweep_grid) *sweep_grid = h->cfg[h->variant].grid;
+  if (sweep_grid) *sweep_grid = grid_of(h, h->variant, h->dispatch);
   if (kernel_launches) *kernel_launches = h->launches;
   return CPM_OK;
 }
 
 int cpm_sweep_config(const cpm_handle* h, int* variant, int* tile_x, int* tile_y,
-                     int* tile_z, int* warps_per_block, int* grid) {
+                     int* tile_z, int* warps_per_block, int* grid, int* dispatch) {
   if (!h) return CPM_ERR_INVALID;
   const cpm_handle::Config& c = h->cfg[h->variant];
   if (variant) *variant = h->variant;
@@ -1015,7 +1072,8 @@ int cpm_sweep_config(const cpm_handle* h, int* variant, int* tile_x, int* tile_y
   if (tile_y) *tile_y = c.shape.cy;
   if (tile_z) *tile_z = c.shape.cz;
   if (warps_per_block) *warps_per_block = c.shape.warps;
-  if (grid) *grid = c.grid;
+  if (grid) *grid = grid_of(h, h->variant, h->dispatch);
+  if (dispatch) *dispatch = h->dispatch;
   return CPM_OK;
 }
 

@@ -12,14 +12,16 @@
 //                                        two copies
 //   dap[2], dcs[2]                       deltas of one phase (two phases in
 //                                        flight alternate)
-//   dflag[2]: uint32 [rows]              row is on a dirty list of a phase
-//   dlist  : uint32 [grid * 2 * list_cap] two dirty lists per sweep block
+//   dlist  : uint32 [grid * 2 * list_cap] two dirty lists per sweep block:
+//                                        rows changed in a phase (a row may
+//                                        appear more than once)
 //   ctl    : uint32 [64]                 barrier counter / release flag,
 //                                        sticky error bits
 // Table double buffering: phase k reads copy k % 2 and adds its deltas both
 // into the other copy and into dap/dcs[k % 2]; phase k + 1 replays those
-// deltas into copy k % 2, which missed them.  So every phase reads tables as
-// they stood when it began, with one grid barrier per phase.  The tables are
+// deltas into copy k % 2, which missed them (each delta is taken with an
+// exchange, so a row listed twice is replayed once).  So every phase reads
+// tables as they stood when it began, with one grid barrier per phase.  The tables are
 // small next to the lattice (4096^2 at 100 sites per cell: 67 MB of lattice,
 // 4 MB per table copy) and stay L2-resident through a run.
 #pragma once
@@ -83,6 +85,7 @@ SweepShape sweep_shape(int ndim, int variant);
 // ones)
 constexpr int kCtlBarrier = 0;
 constexpr int kCtlFlag = 32;
+constexpr int kCtlQueue = 40;  // next replica to claim (replica dispatch)
 constexpr int kCtlErr = 48;  // words [0, kCtlErr) are zeroed before a launch
 constexpr int kCtlWords = 64;
 
@@ -92,6 +95,7 @@ constexpr int kErrBadId = 2;        // site id above the replica's ncells
 constexpr int kErrBadType = 4;      // type >= kMaxTypes
 constexpr int kErrMediumType = 8;   // id 0 with a non-zero type
 constexpr int kErrTypeConflict = 16;  // one id with two types
+constexpr int kErrListFull = 32;      // a dirty list would overflow (not written)
 
 // Per-replica parameters, kept in global memory (read through the
 // read-only cache; a replica's few hundred used bytes stay L1-resident).
@@ -152,7 +156,6 @@ struct SweepArgs {
   long long* cs[2];
   unsigned long long* dap[2];
   long long* dcs[2];
-  uint32_t* dflag[2];
   uint32_t* dlist;
   uint32_t* ctl;
   unsigned long long* counters;  // [nrep][2]: evaluated, accepted
@@ -160,6 +163,11 @@ struct SweepArgs {
   const DevParams* params;
   const int* task_prefix;  // [27][nrep + 1] warp tiles per slot, prefix
   long long list_cap;      // entries of one dirty list of one block
+  // Dispatch: 0 = the tiles of every slot over all replicas go to all warps
+  // of the grid, one grid barrier per phase; 1 = each block claims whole
+  // replicas in rep_order and runs all their phases with block barriers.
+  int block_local;
+  const int* rep_order;  // [nrep] replicas by decreasing site count
   // Monte Carlo time of the first MCS: tick0, or *tick_ptr when tick_ptr is
   // set (graph replays); in the latter case block 0 advances *tick_ptr by
   // mcs when the launch ends.
@@ -190,8 +198,8 @@ int sweep_max_blocks_per_sm(int ndim, bool perim, int variant, bool scores = fal
 // checkpoints: host array of ncheck (<= kMaxCheckpoints) MCS counts.
 cudaError_t launch_lr_backward(const float* scores, const float* dl_do,
                                const float* obs, const int* checkpoints, int nrep,
-                               int len, int nparam, int ncheck, float* grad,
-                               cudaStream_t s);
+                               int len, int nparam, int ncheck, const float* obs_total,
+                               int nrep_total, float* grad, cudaStream_t s);
 cudaError_t launch_observe_heterotypic(const uint32_t* lat, const DevReplica* reps,
                                        int nrep, long long total_sites,
                                        unsigned long long* counts, cudaStream_t s);

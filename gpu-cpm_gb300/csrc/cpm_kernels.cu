@@ -157,15 +157,14 @@ struct PhaseTables {
   long long* wcs;
   unsigned long long* dap;        // this phase's deltas (replayed next phase)
   long long* dcs;
-  uint32_t* dflag;
   uint32_t* list;                 // this block's dirty list for the phase
   unsigned* cnt;                  // its length (shared memory)
 };
 
 // One accepted copy's change of one table row: added to the other table
-// copy and to the phase delta table.  The first block to touch the row in
-// the phase (dflag 0 -> 1) puts it on its own dirty list; that block
-// replays the row's delta into the read copy during the next phase.
+// copy and to the phase delta table.  Reductions only (no value comes
+// back), so the accepting warp does not wait on L2.  The row goes on the
+// block's dirty list separately (warp-aggregated, duplicates allowed).
 template <int NDIM>
 __device__ __forceinline__ void add_delta(const PhaseTables<NDIM>& pt,
                                           long long row, int darea, int dperim,
@@ -179,33 +178,27 @@ __device__ __forceinline__ void add_delta(const PhaseTables<NDIM>& pt,
     atomicAdd(reinterpret_cast<unsigned long long*>(pt.wcs + row * NDIM + k), v);
     atomicAdd(reinterpret_cast<unsigned long long*>(pt.dcs + row * NDIM + k), v);
   }
-  if (atomicExch(pt.dflag + row, 1u) == 0u) {
-    const unsigned pos = atomicAdd(pt.cnt, 1u);
-    pt.list[pos] = (uint32_t)row;
-  }
 }
 
-// Replays the deltas of the rows on a block's dirty list into `ap`/`cs`
-// and clears them (delta, flag), strided over the block's threads.
+// Replays the deltas of the rows on a block's dirty list into `ap`/`cs`,
+// strided over the block's threads.  A row can be on several lists (or
+// twice on one); taking its delta with an exchange hands it to exactly one
+// of them and leaves the delta table zeroed for the phase after next.
 template <int NDIM>
 __device__ __forceinline__ void replay(const uint32_t* list, unsigned n,
                                        unsigned long long* dap, long long* dcs,
-                                       uint32_t* dflag, unsigned long long* ap,
-                                       long long* cs) {
+                                       unsigned long long* ap, long long* cs) {
   for (unsigned j = threadIdx.x; j < n; j += blockDim.x) {
     const uint32_t row = __ldcg(list + j);
-    const unsigned long long d = __ldcg(dap + row);
+    const unsigned long long d = atomicExch(dap + row, 0ull);
     if (d) atomicAdd(ap + row, d);
-    dap[row] = 0ull;
 #pragma unroll
     for (int k = 0; k < NDIM; ++k) {
       const long long idx = (long long)row * NDIM + k;
-      const long long dc = __ldcg(dcs + idx);
-      if (dc) atomicAdd(reinterpret_cast<unsigned long long*>(cs + idx),
-                        (unsigned long long)dc);
-      dcs[idx] = 0;
+      const unsigned long long dc =
+          atomicExch(reinterpret_cast<unsigned long long*>(dcs + idx), 0ull);
+      if (dc) atomicAdd(reinterpret_cast<unsigned long long*>(cs + idx), dc);
     }
-    dflag[row] = 0u;
   }
 }
 
@@ -246,6 +239,7 @@ __global__ void __launch_bounds__(kSweepThreadsMax, 1)
   __shared__ int s_ok;
   __shared__ unsigned s_cnt[2];
   __shared__ unsigned long long s_tick0;
+  __shared__ int s_claim;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int wpb = blockDim.x >> 5;  // warps (tiles in flight) per block
@@ -268,311 +262,390 @@ __global__ void __launch_bounds__(kSweepThreadsMax, 1)
   unsigned long long sc_tick = 0;
   if (tid < 2) s_cnt[tid] = 0;
   // Every block reads *tick_ptr before its first barrier arrival, and block
-  // 0 advances it only after the last barrier, so all blocks see one value.
+  // 0 advances it only after its last barrier, so all blocks see one value.
   if (tid == 0) s_tick0 = a.tick_ptr ? __ldcg(a.tick_ptr) : a.tick0;
   __syncthreads();
 
-  int step = 0;
-  for (int m = 0; m < a.mcs; ++m) {
-    const unsigned long long tick = s_tick0 + (unsigned long long)m;
-    for (int si = 0; si < a.nslot_active; ++si, ++step) {
-      const int cur = step & 1, prv = cur ^ 1;
-      PhaseTables<NDIM> pt;
-      pt.rap = cur ? a.ap[1] : a.ap[0];
-      pt.rcs = cur ? a.cs[1] : a.cs[0];
-      pt.wap = cur ? a.ap[0] : a.ap[1];
-      pt.wcs = cur ? a.cs[0] : a.cs[1];
-      pt.dap = cur ? a.dap[1] : a.dap[0];
-      pt.dcs = cur ? a.dcs[1] : a.dcs[0];
-      pt.dflag = cur ? a.dflag[1] : a.dflag[0];
-      pt.list = blist(cur);
-      pt.cnt = &s_cnt[cur];
+  // Tables of the phase with double-buffer index `cur`.
+  auto tables = [&](int cur) {
+    PhaseTables<NDIM> pt;
+    pt.rap = cur ? a.ap[1] : a.ap[0];
+    pt.rcs = cur ? a.cs[1] : a.cs[0];
+    pt.wap = cur ? a.ap[0] : a.ap[1];
+    pt.wcs = cur ? a.cs[0] : a.cs[1];
+    pt.dap = cur ? a.dap[1] : a.dap[0];
+    pt.dcs = cur ? a.dcs[1] : a.dcs[0];
+    pt.list = blist(cur);
+    pt.cnt = &s_cnt[cur];
+    return pt;
+  };
+  // Replay of the deltas of the phase with index `prv` into the copy it
+  // read (rows on this block's list only).
+  auto replay_phase = [&](int prv) {
+    const unsigned n = min(s_cnt[prv], (unsigned)a.list_cap);  // see kErrListFull
+    replay<NDIM>(blist(prv), n, prv ? a.dap[1] : a.dap[0],
+                 prv ? a.dcs[1] : a.dcs[0], prv ? a.ap[1] : a.ap[0],
+                 prv ? a.cs[1] : a.cs[0]);
+  };
 
-      // Replay the previous phase's deltas into the copy that phase read.
-      if (step > 0)
-        replay<NDIM>(blist(prv), s_cnt[prv], cur ? a.dap[0] : a.dap[1],
-                     cur ? a.dcs[0] : a.dcs[1], cur ? a.dflag[0] : a.dflag[1],
-                     pt.wap, pt.wcs);
+  // One warp tile of replica r (its `local`-th tile of the slot): stage the
+  // tile, then boundary test, source pick and dH / test / commit.
+  auto run_tile = [&](const PhaseTables<NDIM>& pt, const int r, const int local,
+                      const int cx, const int cy, const int cz,
+                      const unsigned long long tick, const unsigned long long phase) {
+    if (r != cnt_rep) {
+      if (lane == 0 && cnt_rep >= 0) {
+        if (n_eval) atomicAdd(&a.counters[2 * cnt_rep], n_eval);
+        if (n_acc) atomicAdd(&a.counters[2 * cnt_rep + 1], n_acc);
+      }
+      n_eval = n_acc = 0;
+      cnt_rep = r;
+    }
+    if (SCORE && (r != sc_rep || tick != sc_tick)) {  // warp-uniform
+      flush_scores(a, sc, sc_rep, sc_tick);
+      sc_rep = r;
+      sc_tick = tick;
+    }
+    const DevParams* P = a.params + r;
+    const int nx = __ldg(&a.reps[r].nx), ny = __ldg(&a.reps[r].ny),
+              nz = __ldg(&a.reps[r].nz), ncells = __ldg(&a.reps[r].ncells);
+    const long long lat_off = __ldg(&a.reps[r].lat_off);
+    const long long cell_off = __ldg(&a.reps[r].cell_off);
+    const int ncx = class_count(nx, cx), ncy = class_count(ny, cy),
+              ncz = class_count(nz, cz);
+    const int tnx = (ncx + G::CX - 1) / G::CX;
+    const int tny = (ncy + G::CY - 1) / G::CY;
+    const int tx = local % tnx, rest = local / tnx;
+    const int ty = rest % tny, tz = rest / tny;
+    const int i0 = tx * G::CX, j0 = ty * G::CY, l0 = tz * G::CZ;
+    const int cntx = min(G::CX, ncx - i0), cnty = min(G::CY, ncy - j0),
+              cntz = min(G::CZ, ncz - l0);
+    const int xorig = class_coord(nx, cx, i0) - 1;
+    const int yorig = class_coord(ny, cy, j0) - 1;
+    const int zorig = NDIM == 3 ? class_coord(nz, cz, l0) - 1 : 0;
+    const int ux = 2 * cntx + 1, uy = 2 * cnty + 1,
+              uz = NDIM == 3 ? 2 * cntz + 1 : 1;
+    uint32_t* L = a.lat + lat_off;
 
-      const int slot = a.slots[si];
-      const int cx = slot % 3, cy = (slot / 3) % 3, cz = slot / 9;
-      const unsigned long long phase = tick * NSLOTS + (unsigned long long)slot;
-      const int* pre = a.task_prefix + slot * (a.nrep + 1);
-      const int ntiles = __ldg(pre + a.nrep);
-
-      for (int task = gwarp; task < ntiles; task += nwarps) {
-        const int r = find_task_replica(pre, a.nrep, task);
-        if (r != cnt_rep) {
-          if (lane == 0 && cnt_rep >= 0) {
-            if (n_eval) atomicAdd(&a.counters[2 * cnt_rep], n_eval);
-            if (n_acc) atomicAdd(&a.counters[2 * cnt_rep + 1], n_acc);
-          }
-          n_eval = n_acc = 0;
-          cnt_rep = r;
-        }
-        if (SCORE && (r != sc_rep || tick != sc_tick)) {  // warp-uniform
-          flush_scores(a, sc, sc_rep, sc_tick);
-          sc_rep = r;
-          sc_tick = tick;
-        }
-        const DevParams* P = a.params + r;
-        const int nx = __ldg(&a.reps[r].nx), ny = __ldg(&a.reps[r].ny),
-                  nz = __ldg(&a.reps[r].nz), ncells = __ldg(&a.reps[r].ncells);
-        const long long lat_off = __ldg(&a.reps[r].lat_off);
-        const long long cell_off = __ldg(&a.reps[r].cell_off);
-        const int ncx = class_count(nx, cx), ncy = class_count(ny, cy),
-                  ncz = class_count(nz, cz);
-        const int tnx = (ncx + G::CX - 1) / G::CX;
-        const int tny = (ncy + G::CY - 1) / G::CY;
-        const int local = task - __ldg(pre + r);
-        const int tx = local % tnx, rest = local / tnx;
-        const int ty = rest % tny, tz = rest / tny;
-        const int i0 = tx * G::CX, j0 = ty * G::CY, l0 = tz * G::CZ;
-        const int cntx = min(G::CX, ncx - i0), cnty = min(G::CY, ncy - j0),
-                  cntz = min(G::CZ, ncz - l0);
-        const int xorig = class_coord(nx, cx, i0) - 1;
-        const int yorig = class_coord(ny, cy, j0) - 1;
-        const int zorig = NDIM == 3 ? class_coord(nz, cz, l0) - 1 : 0;
-        const int ux = 2 * cntx + 1, uy = 2 * cnty + 1,
-                  uz = NDIM == 3 ? 2 * cntz + 1 : 1;
-        uint32_t* L = a.lat + lat_off;
-
-        // ---- stage the tile and its halo (periodic wrap applied here) ----
-        int gx[3];
+    // ---- stage the tile and its halo (periodic wrap applied here) ----
+    int gx[3];
+#pragma unroll
+    for (int u = 0; u < 3; ++u) {
+      int v = xorig + lane + 32 * u;
+      gx[u] = v < 0 ? v + nx : (v >= nx ? v - nx : v);
+    }
+    for (int zz = 0; zz < uz; ++zz) {
+      int gz = zorig + zz;
+      gz = gz < 0 ? gz + nz : (gz >= nz ? gz - nz : gz);
+#pragma unroll
+      for (int yy = 0; yy < uy; ++yy) {
+        int gy = yorig + yy;
+        gy = gy < 0 ? gy + ny : (gy >= ny ? gy - ny : gy);
+        const uint32_t* src = L + ((long long)gz * ny + gy) * nx;
+        uint32_t* dst = ws.tile + (zz * S::SY + yy) * S::SXP;
 #pragma unroll
         for (int u = 0; u < 3; ++u) {
-          int v = xorig + lane + 32 * u;
-          gx[u] = v < 0 ? v + nx : (v >= nx ? v - nx : v);
+          const int c = lane + 32 * u;
+          if (c < ux) dst[(c & 1) * S::HALF + (c >> 1)] = __ldcg(src + gx[u]);
         }
-        for (int zz = 0; zz < uz; ++zz) {
-          int gz = zorig + zz;
-          gz = gz < 0 ? gz + nz : (gz >= nz ? gz - nz : gz);
+      }
+    }
+    __syncwarp();
+
+    // ---- pass 1: boundary test ---------------------------------------
+    int na = 0;
 #pragma unroll
-          for (int yy = 0; yy < uy; ++yy) {
-            int gy = yorig + yy;
-            gy = gy < 0 ? gy + ny : (gy >= ny ? gy - ny : gy);
-            const uint32_t* src = L + ((long long)gz * ny + gy) * nx;
-            uint32_t* dst = ws.tile + (zz * S::SY + yy) * S::SXP;
+    for (int it = 0; it < NT / 32; ++it) {
+      const int q = it * 32 + lane;
+      const int qy = it % G::CY, qz = it / G::CY;
+      bool bnd = false;
+      if (lane < cntx && qy < cnty && qz < cntz) {
+        const int c = S::center(q);
+        const uint32_t t = ws.tile[c];
 #pragma unroll
-            for (int u = 0; u < 3; ++u) {
-              const int c = lane + 32 * u;
-              if (c < ux) dst[(c & 1) * S::HALF + (c >> 1)] = __ldcg(src + gx[u]);
+        for (int k = 0; k < NB; ++k) bnd |= ws.tile[c + S::nb_offset(k)] != t;
+      }
+      const unsigned ball = __ballot_sync(kFull, bnd);
+      if (bnd) ws.qa[na + __popc(ball & lanemask_lt())] = (uint16_t)q;
+      na += __popc(ball);
+    }
+    __syncwarp();
+
+    // ---- pass 2: random draw and source pick -------------------------
+    int nb = 0;
+    for (int base = 0; base < na; base += 32) {
+      const int j = base + lane;
+      bool keep = false;
+      uint2 entry = make_uint2(0u, 0u);
+      if (j < na) {
+        const int q = ws.qa[j];
+        const int qx = q % G::CX, qy = (q / G::CX) % G::CY,
+                  qz = q / (G::CX * G::CY);
+        const int x = class_coord(nx, cx, i0 + qx);
+        const int y = class_coord(ny, cy, j0 + qy);
+        const int z = NDIM == 3 ? class_coord(nz, cz, l0 + qz) : 0;
+        const long long site = ((long long)z * ny + y) * nx + x;
+        uint32_t c0 = (uint32_t)site, c1 = (uint32_t)phase,
+                 c2 = a.stream0 + (uint32_t)r, c3 = (uint32_t)(phase >> 32);
+        philox4x32_10(c0, c1, c2, c3, k0, k1);
+        const int kdir = (int)__umulhi(c0, (unsigned)NB);
+        const int c = S::center(q);
+        keep = ws.tile[c + S::nb_offset(kdir)] != ws.tile[c];
+        entry = make_uint2((uint32_t)q | ((uint32_t)kdir << 16), c1);
+      }
+      const unsigned ball = __ballot_sync(kFull, keep);
+      if (keep) ws.qb[nb + __popc(ball & lanemask_lt())] = entry;
+      nb += __popc(ball);
+    }
+    __syncwarp();
+
+    // ---- pass 3: dH, Metropolis test, commit -------------------------
+    for (int base = 0; base < nb; base += 32) {
+      const int j = base + lane;
+      bool accepted = false;
+      long long push_s = -1, push_t = -1;  // table rows this lane changed
+      if (j < nb) {
+        const uint2 entry = ws.qb[j];
+        const int q = (int)(entry.x & 0xFFFFu), kdir = (int)(entry.x >> 16);
+        const int c = S::center(q);
+        const uint32_t t = ws.tile[c];
+        const uint32_t s = ws.tile[c + S::nb_offset(kdir)];
+        const uint32_t is = s & 0xFFFFFFu, it = t & 0xFFFFFFu;
+        if (is > (uint32_t)ncells || it > (uint32_t)ncells) {
+          atomicOr(err, kErrBadId);
+        } else {
+          const int ts = (int)(s >> 24) & (kMaxTypes - 1);
+          const int tt = (int)(t >> 24) & (kMaxTypes - 1);
+          const long long rs = cell_off + is, rt = cell_off + it;
+          const unsigned long long aps = s ? __ldcg(pt.rap + rs) : 0ull;
+          const unsigned long long apt = t ? __ldcg(pt.rap + rt) : 0ull;
+          // centroid sums, needed only on acceptance, fetched with the row
+          // so that an accepted attempt waits on one L2 round trip
+          long long cs_s[NDIM], cs_t[NDIM];
+#pragma unroll
+          for (int k = 0; k < NDIM; ++k) {
+            cs_s[k] = s ? __ldcg(pt.rcs + rs * NDIM + k) : 0;
+            cs_t[k] = t ? __ldcg(pt.rcs + rt * NDIM + k) : 0;
+          }
+          float e_old = 0.0f, e_new = 0.0f;
+          int cnt_s = 0, cnt_t = 0;
+          // (score launches) neighbours by type < kScoreTypes, one byte
+          // per type: of the new configuration (n != s), of the old (n != t)
+          unsigned by_new = 0, by_old = 0;
+#pragma unroll
+          for (int k = 0; k < NB; ++k) {
+            const uint32_t v = ws.tile[c + S::nb_offset(k)];
+            const int tn = (int)(v >> 24) & (kMaxTypes - 1);
+            if (v != t) e_old = __fadd_rn(e_old, __ldg(&P->J[tt * kMaxTypes + tn]));
+            if (v != s) e_new = __fadd_rn(e_new, __ldg(&P->J[ts * kMaxTypes + tn]));
+            cnt_s += v == s;
+            cnt_t += v == t;
+            if (SCORE && tn < kScoreTypes) {
+              if (v != s) by_new += 1u << (8 * tn);
+              if (v != t) by_old += 1u << (8 * tn);
             }
           }
-        }
-        __syncwarp();
-
-        // ---- pass 1: boundary test ---------------------------------------
-        int na = 0;
-#pragma unroll
-        for (int it = 0; it < NT / 32; ++it) {
-          const int q = it * 32 + lane;
-          const int qy = it % G::CY, qz = it / G::CY;
-          bool bnd = false;
-          if (lane < cntx && qy < cnty && qz < cntz) {
-            const int c = S::center(q);
-            const uint32_t t = ws.tile[c];
-#pragma unroll
-            for (int k = 0; k < NB; ++k) bnd |= ws.tile[c + S::nb_offset(k)] != t;
+          float dH = __fsub_rn(e_new, e_old);
+          const int dps = NB - 2 * cnt_s;
+          const int dpt = 2 * cnt_t - NB;
+          if (PERIM && __ldg(&P->perim_on)) {
+            if (s) {
+              const long long qv = (long long)dps *
+                  (2LL * (unpack_perim(aps) - __ldg(&P->tgt_perim[ts])) + dps);
+              dH = __fmaf_rn(__ldg(&P->lam_perim[ts]), __ll2float_rn(qv), dH);
+            }
+            if (t) {
+              const long long qv = (long long)dpt *
+                  (2LL * (unpack_perim(apt) - __ldg(&P->tgt_perim[tt])) + dpt);
+              dH = __fmaf_rn(__ldg(&P->lam_perim[tt]), __ll2float_rn(qv), dH);
+            }
           }
-          const unsigned ball = __ballot_sync(kFull, bnd);
-          if (bnd) ws.qa[na + __popc(ball & lanemask_lt())] = (uint16_t)q;
-          na += __popc(ball);
-        }
-        __syncwarp();
-
-        // ---- pass 2: random draw and source pick -------------------------
-        int nb = 0;
-        for (int base = 0; base < na; base += 32) {
-          const int j = base + lane;
-          bool keep = false;
-          uint2 entry = make_uint2(0u, 0u);
-          if (j < na) {
-            const int q = ws.qa[j];
+          if (s) {
+            const long long qv =
+                1 + 2LL * (unpack_area(aps) - __ldg(&P->tgt_area[ts]));
+            dH = __fmaf_rn(__ldg(&P->lam_area[ts]), __ll2float_rn(qv), dH);
+          }
+          if (t) {
+            const long long qv =
+                1 - 2LL * (unpack_area(apt) - __ldg(&P->tgt_area[tt]));
+            dH = __fmaf_rn(__ldg(&P->lam_area[tt]), __ll2float_rn(qv), dH);
+          }
+          const float T = __ldg(&P->temperature);
+          bool ok;
+          float ex = 1.0f;  // exp(-dH/T) when 0 <= dH and T > 0
+          if (dH < 0.0f) {
+            ok = true;
+          } else if (!(T > 0.0f)) {
+            ok = false;
+          } else {
+            const float u =
+                __fmul_rn(__uint2float_rn((entry.y >> 8) | 1u), 0x1p-24f);
+            ex = exp_neg(__fdiv_rn(-dH, T));
+            ok = u < ex;
+          }
+          if (SCORE && dH >= 0.0f && T > 0.0f) {
+            // d log P(decision) / d theta with P(accept) = min(1, exp(-dH/T)):
+            // accept: -g, reject: e/(1-e) g, g = d(dH/T)/d theta.  At
+            // dH = 0 exactly (integer parameters make it common) P has a
+            // kink, slope -g on one side and 0 on the other; the score takes
+            // the mean of the two one-sided derivatives, -g/2.
+            const float x = dH / T;
+            const float om = x < 1e-2f
+                                 ? x * (1.0f - 0.5f * x * (1.0f - (x / 3.0f) *
+                                                                      (1.0f - 0.25f * x)))
+                                 : 1.0f - ex;  // 1 - exp(-x)
+            const float cT = (dH == 0.0f ? -0.5f : (ok ? -1.0f : ex / om)) / T;
+#pragma unroll
+            for (int p = 0; p < kScorePairsMax; ++p) {
+              if (p < a.score_spec.n_pairs) {
+                const int pa = a.score_spec.pair_a[p], pb = a.score_spec.pair_b[p];
+                int d = 0;
+                if (ts == pa) d += (by_new >> (8 * pb)) & 0xFF;
+                if (pa != pb && ts == pb) d += (by_new >> (8 * pa)) & 0xFF;
+                if (tt == pa) d -= (by_old >> (8 * pb)) & 0xFF;
+                if (pa != pb && tt == pb) d -= (by_old >> (8 * pa)) & 0xFF;
+                sc[p] += cT * (float)d;
+              }
+            }
+            if (a.score_spec.lambda_area) {
+              const int da =
+                  (s ? 1 + 2 * (unpack_area(aps) - __ldg(&P->tgt_area[ts])) : 0) +
+                  (t ? 1 - 2 * (unpack_area(apt) - __ldg(&P->tgt_area[tt])) : 0);
+              sc[kScorePairsMax] += cT * (float)da;
+            }
+            if (a.score_spec.lambda_perim) {
+              const long long dp =
+                  (s ? (long long)dps * (2LL * (unpack_perim(aps) -
+                                                __ldg(&P->tgt_perim[ts])) + dps)
+                     : 0LL) +
+                  (t ? (long long)dpt * (2LL * (unpack_perim(apt) -
+                                                __ldg(&P->tgt_perim[tt])) + dpt)
+                     : 0LL);
+              sc[kScorePairsMax + 1] += cT * __ll2float_rn(dp);
+            }
+            if (a.score_spec.temperature) sc[kScorePairsMax + 2] -= cT * x;
+          }
+          if (ok) {
+            accepted = true;
             const int qx = q % G::CX, qy = (q / G::CX) % G::CY,
                       qz = q / (G::CX * G::CY);
             const int x = class_coord(nx, cx, i0 + qx);
             const int y = class_coord(ny, cy, j0 + qy);
             const int z = NDIM == 3 ? class_coord(nz, cz, l0 + qz) : 0;
-            const long long site = ((long long)z * ny + y) * nx + x;
-            uint32_t c0 = (uint32_t)site, c1 = (uint32_t)phase,
-                     c2 = a.stream0 + (uint32_t)r, c3 = (uint32_t)(phase >> 32);
-            philox4x32_10(c0, c1, c2, c3, k0, k1);
-            const int kdir = (int)__umulhi(c0, (unsigned)NB);
-            const int c = S::center(q);
-            keep = ws.tile[c + S::nb_offset(kdir)] != ws.tile[c];
-            entry = make_uint2((uint32_t)q | ((uint32_t)kdir << 16), c1);
-          }
-          const unsigned ball = __ballot_sync(kFull, keep);
-          if (keep) ws.qb[nb + __popc(ball & lanemask_lt())] = entry;
-          nb += __popc(ball);
-        }
-        __syncwarp();
-
-        // ---- pass 3: dH, Metropolis test, commit -------------------------
-        for (int base = 0; base < nb; base += 32) {
-          const int j = base + lane;
-          bool accepted = false;
-          if (j < nb) {
-            const uint2 entry = ws.qb[j];
-            const int q = (int)(entry.x & 0xFFFFu), kdir = (int)(entry.x >> 16);
-            const int c = S::center(q);
-            const uint32_t t = ws.tile[c];
-            const uint32_t s = ws.tile[c + S::nb_offset(kdir)];
-            const uint32_t is = s & 0xFFFFFFu, it = t & 0xFFFFFFu;
-            if (is > (uint32_t)ncells || it > (uint32_t)ncells) {
-              atomicOr(err, kErrBadId);
-            } else {
-              const int ts = (int)(s >> 24) & (kMaxTypes - 1);
-              const int tt = (int)(t >> 24) & (kMaxTypes - 1);
-              const long long rs = cell_off + is, rt = cell_off + it;
-              const unsigned long long aps = s ? __ldcg(pt.rap + rs) : 0ull;
-              const unsigned long long apt = t ? __ldcg(pt.rap + rt) : 0ull;
-              float e_old = 0.0f, e_new = 0.0f;
-              int cnt_s = 0, cnt_t = 0;
-              // (score launches) neighbours by type < kScoreTypes, one byte
-              // per type: of the new configuration (n != s), of the old (n != t)
-              unsigned by_new = 0, by_old = 0;
+            L[((long long)z * ny + y) * nx + x] = s;
+            const int crd[3] = {x, y, z};
+            const int dim[3] = {nx, ny, nz};
+            long long img[NDIM];
+            if (s) {
 #pragma unroll
-              for (int k = 0; k < NB; ++k) {
-                const uint32_t v = ws.tile[c + S::nb_offset(k)];
-                const int tn = (int)(v >> 24) & (kMaxTypes - 1);
-                if (v != t) e_old = __fadd_rn(e_old, __ldg(&P->J[tt * kMaxTypes + tn]));
-                if (v != s) e_new = __fadd_rn(e_new, __ldg(&P->J[ts * kMaxTypes + tn]));
-                cnt_s += v == s;
-                cnt_t += v == t;
-                if (SCORE && tn < kScoreTypes) {
-                  if (v != s) by_new += 1u << (8 * tn);
-                  if (v != t) by_old += 1u << (8 * tn);
-                }
-              }
-              float dH = __fsub_rn(e_new, e_old);
-              const int dps = NB - 2 * cnt_s;
-              const int dpt = 2 * cnt_t - NB;
-              if (PERIM && __ldg(&P->perim_on)) {
-                if (s) {
-                  const long long qv = (long long)dps *
-                      (2LL * (unpack_perim(aps) - __ldg(&P->tgt_perim[ts])) + dps);
-                  dH = __fmaf_rn(__ldg(&P->lam_perim[ts]), __ll2float_rn(qv), dH);
-                }
-                if (t) {
-                  const long long qv = (long long)dpt *
-                      (2LL * (unpack_perim(apt) - __ldg(&P->tgt_perim[tt])) + dpt);
-                  dH = __fmaf_rn(__ldg(&P->lam_perim[tt]), __ll2float_rn(qv), dH);
-                }
-              }
-              if (s) {
-                const long long qv =
-                    1 + 2LL * (unpack_area(aps) - __ldg(&P->tgt_area[ts]));
-                dH = __fmaf_rn(__ldg(&P->lam_area[ts]), __ll2float_rn(qv), dH);
-              }
-              if (t) {
-                const long long qv =
-                    1 - 2LL * (unpack_area(apt) - __ldg(&P->tgt_area[tt]));
-                dH = __fmaf_rn(__ldg(&P->lam_area[tt]), __ll2float_rn(qv), dH);
-              }
-              const float T = __ldg(&P->temperature);
-              bool ok;
-              float ex = 1.0f;  // exp(-dH/T) when 0 <= dH and T > 0
-              if (dH < 0.0f) {
-                ok = true;
-              } else if (!(T > 0.0f)) {
-                ok = false;
-              } else {
-                const float u =
-                    __fmul_rn(__uint2float_rn((entry.y >> 8) | 1u), 0x1p-24f);
-                ex = exp_neg(__fdiv_rn(-dH, T));
-                ok = u < ex;
-              }
-              if (SCORE && dH > 0.0f && T > 0.0f) {
-                // d log P(decision) / d theta with P(accept) = exp(-dH/T):
-                // accept: -g, reject: e/(1-e) g, g = d(dH/T)/d theta.
-                const float x = dH / T;
-                const float om = x < 1e-2f
-                                     ? x * (1.0f - 0.5f * x * (1.0f - (x / 3.0f) *
-                                                                          (1.0f - 0.25f * x)))
-                                     : 1.0f - ex;  // 1 - exp(-x)
-                const float cT = (ok ? -1.0f : ex / om) / T;
+              for (int k = 0; k < NDIM; ++k)
+                img[k] = nearest_image(crd[k], dim[k], unpack_area(aps), cs_s[k]);
+              add_delta<NDIM>(pt, rs, 1, dps, img, 1);
+              push_s = rs;
+            }
+            if (t) {
 #pragma unroll
-                for (int p = 0; p < kScorePairsMax; ++p) {
-                  if (p < a.score_spec.n_pairs) {
-                    const int pa = a.score_spec.pair_a[p], pb = a.score_spec.pair_b[p];
-                    int d = 0;
-                    if (ts == pa) d += (by_new >> (8 * pb)) & 0xFF;
-                    if (pa != pb && ts == pb) d += (by_new >> (8 * pa)) & 0xFF;
-                    if (tt == pa) d -= (by_old >> (8 * pb)) & 0xFF;
-                    if (pa != pb && tt == pb) d -= (by_old >> (8 * pa)) & 0xFF;
-                    sc[p] += cT * (float)d;
-                  }
-                }
-                if (a.score_spec.lambda_area) {
-                  const int da =
-                      (s ? 1 + 2 * (unpack_area(aps) - __ldg(&P->tgt_area[ts])) : 0) +
-                      (t ? 1 - 2 * (unpack_area(apt) - __ldg(&P->tgt_area[tt])) : 0);
-                  sc[kScorePairsMax] += cT * (float)da;
-                }
-                if (a.score_spec.lambda_perim) {
-                  const long long dp =
-                      (s ? (long long)dps * (2LL * (unpack_perim(aps) -
-                                                    __ldg(&P->tgt_perim[ts])) + dps)
-                         : 0LL) +
-                      (t ? (long long)dpt * (2LL * (unpack_perim(apt) -
-                                                    __ldg(&P->tgt_perim[tt])) + dpt)
-                         : 0LL);
-                  sc[kScorePairsMax + 1] += cT * __ll2float_rn(dp);
-                }
-                if (a.score_spec.temperature) sc[kScorePairsMax + 2] -= cT * x;
-              }
-              if (ok) {
-                accepted = true;
-                const int qx = q % G::CX, qy = (q / G::CX) % G::CY,
-                          qz = q / (G::CX * G::CY);
-                const int x = class_coord(nx, cx, i0 + qx);
-                const int y = class_coord(ny, cy, j0 + qy);
-                const int z = NDIM == 3 ? class_coord(nz, cz, l0 + qz) : 0;
-                L[((long long)z * ny + y) * nx + x] = s;
-                const int crd[3] = {x, y, z};
-                const int dim[3] = {nx, ny, nz};
-                long long img[NDIM];
-                if (s) {
-#pragma unroll
-                  for (int k = 0; k < NDIM; ++k)
-                    img[k] = nearest_image(crd[k], dim[k], unpack_area(aps),
-                                           __ldcg(pt.rcs + rs * NDIM + k));
-                  add_delta<NDIM>(pt, rs, 1, dps, img, 1);
-                }
-                if (t) {
-#pragma unroll
-                  for (int k = 0; k < NDIM; ++k)
-                    img[k] = nearest_image(crd[k], dim[k], unpack_area(apt),
-                                           __ldcg(pt.rcs + rt * NDIM + k));
-                  add_delta<NDIM>(pt, rt, -1, dpt, img, -1);
-                }
-              }
+              for (int k = 0; k < NDIM; ++k)
+                img[k] = nearest_image(crd[k], dim[k], unpack_area(apt), cs_t[k]);
+              add_delta<NDIM>(pt, rt, -1, dpt, img, -1);
+              push_t = rt;
             }
           }
-          n_acc += __popc(__ballot_sync(kFull, accepted));
         }
-        n_eval += nb;
-        __syncwarp();  // the tile buffers are rewritten by the next tile
       }
+      n_acc += __popc(__ballot_sync(kFull, accepted));
+      // the changed rows onto the block's dirty list: one shared-memory
+      // atomic per warp and batch
+      const unsigned bs = __ballot_sync(kFull, push_s >= 0);
+      const unsigned bt = __ballot_sync(kFull, push_t >= 0);
+      if (bs | bt) {  // warp-uniform
+        const unsigned npush = (unsigned)(__popc(bs) + __popc(bt));
+        unsigned at = 0;
+        if (lane == 0) at = atomicAdd(pt.cnt, npush);
+        at = __shfl_sync(kFull, at, 0);
+        // The host sizes the lists for two rows per attempt; a list that
+        // would still overflow is reported, never written past its end.
+        if ((long long)at + npush > a.list_cap) {
+          if (lane == 0) atomicOr(err, kErrListFull);
+        } else {
+          if (push_s >= 0) pt.list[at + __popc(bs & lanemask_lt())] = (uint32_t)push_s;
+          if (push_t >= 0)
+            pt.list[at + __popc(bs) + __popc(bt & lanemask_lt())] = (uint32_t)push_t;
+        }
+      }
+    }
+    n_eval += nb;
+    __syncwarp();  // the tile buffers are rewritten by the next tile
+  };
 
-      // The replayed list is consumed; every attempt of the slot is done
-      // once all blocks pass the barrier.
+  if (!a.block_local) {
+    // Grid dispatch: the tiles of a slot, over all replicas, are dealt out
+    // to every warp of the grid; one grid barrier ends each phase.
+    int step = 0;
+    for (int m = 0; m < a.mcs; ++m) {
+      const unsigned long long tick = s_tick0 + (unsigned long long)m;
+      for (int si = 0; si < a.nslot_active; ++si, ++step) {
+        const int cur = step & 1, prv = cur ^ 1;
+        const PhaseTables<NDIM> pt = tables(cur);
+        if (step > 0) replay_phase(prv);
+        const int slot = a.slots[si];
+        const int cx = slot % 3, cy = (slot / 3) % 3, cz = slot / 9;
+        const unsigned long long phase = tick * NSLOTS + (unsigned long long)slot;
+        const int* pre = a.task_prefix + slot * (a.nrep + 1);
+        const int ntiles = __ldg(pre + a.nrep);
+        for (int task = gwarp; task < ntiles; task += nwarps) {
+          const int r = find_task_replica(pre, a.nrep, task);
+          run_tile(pt, r, task - __ldg(pre + r), cx, cy, cz, tick, phase);
+        }
+        // The replayed list is consumed; every attempt of the slot is done
+        // once all blocks pass the barrier.
+        __syncthreads();
+        if (tid == 0) s_cnt[prv] = 0;
+        if (!grid_barrier(a.ctl, ++episode, &s_ok)) return;
+      }
+    }
+    // Final replay: the last phase's deltas into the copy it read, so that
+    // both copies agree when the kernel ends.
+    if (step > 0) replay_phase((step - 1) & 1);
+  } else {
+    // Replica dispatch: a block claims whole replicas (largest first) and
+    // runs all their MCS with block barriers between phases; a replica's
+    // lattice and tables then stay in this SM's share of L2.  The one grid
+    // barrier makes every block read the starting tick before block 0 can
+    // advance it.
+    if (!grid_barrier(a.ctl, ++episode, &s_ok)) return;
+    for (;;) {
+      if (tid == 0) s_claim = (int)atomicAdd(&a.ctl[kCtlQueue], 1u);
       __syncthreads();
-      if (tid == 0) s_cnt[prv] = 0;
-      if (!grid_barrier(a.ctl, ++episode, &s_ok)) return;
+      const int qi = s_claim;
+      if (qi >= a.nrep) break;  // block-uniform
+      const int r = __ldg(a.rep_order + qi);
+      int step = 0;
+      for (int m = 0; m < a.mcs; ++m) {
+        const unsigned long long tick = s_tick0 + (unsigned long long)m;
+        for (int si = 0; si < a.nslot_active; ++si, ++step) {
+          const int cur = step & 1, prv = cur ^ 1;
+          const PhaseTables<NDIM> pt = tables(cur);
+          if (step > 0) replay_phase(prv);
+          const int slot = a.slots[si];
+          const int cx = slot % 3, cy = (slot / 3) % 3, cz = slot / 9;
+          const unsigned long long phase = tick * NSLOTS + (unsigned long long)slot;
+          const int* pre = a.task_prefix + slot * (a.nrep + 1);
+          const int ntiles = __ldg(pre + r + 1) - __ldg(pre + r);
+          for (int local = warp; local < ntiles; local += wpb)
+            run_tile(pt, r, local, cx, cy, cz, tick, phase);
+          __syncthreads();
+          if (tid == 0) s_cnt[prv] = 0;
+          __syncthreads();
+        }
+      }
+      if (step > 0) replay_phase((step - 1) & 1);
+      __syncthreads();
+      if (tid < 2) s_cnt[tid] = 0;
+      __syncthreads();
     }
   }
 
-  // Final replay: the last phase's deltas into the copy it read, so that
-  // both copies agree when the kernel ends.
-  if (step > 0) {
-    const int last = (step - 1) & 1;
-    replay<NDIM>(blist(last), s_cnt[last], last ? a.dap[1] : a.dap[0],
-                 last ? a.dcs[1] : a.dcs[0], last ? a.dflag[1] : a.dflag[0],
-                 last ? a.ap[1] : a.ap[0], last ? a.cs[1] : a.cs[0]);
-  }
   if (lane == 0 && cnt_rep >= 0) {
     if (n_eval) atomicAdd(&a.counters[2 * cnt_rep], n_eval);
     if (n_acc) atomicAdd(&a.counters[2 * cnt_rep + 1], n_acc);
@@ -698,13 +771,19 @@ const void* sweep_fn(int ndim, bool perim, int variant, bool scores) {
 struct Checkpoints {
   int n;
   int t[kMaxCheckpoints];
+  // Baseline over replicas beyond this launch's (replicas sharded over
+  // processes): sum of O[.][c] and replica count of all shards.
+  int use_total;
+  int nrep_total;
+  float total[kMaxCheckpoints];
 };
 
 // grad[k] = sum_r sum_c dL/dO[r][c] (O[r][c] - b[r][c])
 //                     * sum_{t < checkpoints[c]} scores[r][t][k]
 // with the leave-one-out baseline b[r][c] = mean of O[.][c] over the other
 // replicas (0 for a single replica), so that each replica's term is an
-// unbiased estimate of dE[O]/dtheta scaled by dL/dO[r][c].
+// unbiased estimate of dE[O]/dtheta scaled by dL/dO[r][c].  With use_total
+// the other replicas are those of every shard (total / nrep_total).
 // One block per parameter k; threads stride over replicas, each walking its
 // replica's scores once in time order while passing the checkpoints.
 __global__ void lr_backward_kernel(const float* __restrict__ scores,
@@ -717,9 +796,14 @@ __global__ void lr_backward_kernel(const float* __restrict__ scores,
   __shared__ float s_red[32];
   for (int c = threadIdx.x; c < ncheck; c += blockDim.x) {
     float m = 0.0f;
-    for (int r = 0; r < nrep; ++r) m += obs[(long long)r * ncheck + c];
+    if (cp.use_total) {
+      m = cp.total[c];
+    } else {
+      for (int r = 0; r < nrep; ++r) m += obs[(long long)r * ncheck + c];
+    }
     s_mean[c] = m;
   }
+  const int nall = cp.use_total ? cp.nrep_total : nrep;
   __syncthreads();
   float acc = 0.0f;
   for (int r = threadIdx.x; r < nrep; r += blockDim.x) {
@@ -730,7 +814,7 @@ __global__ void lr_backward_kernel(const float* __restrict__ scores,
       for (; t < upto; ++t) cum += scores[((long long)r * len + t) * kScoreMax + k];
       const long long rc = (long long)r * ncheck + c;
       const float o = obs[rc];
-      const float dev = nrep > 1 ? o - (s_mean[c] - o) / (float)(nrep - 1) : o;
+      const float dev = nall > 1 ? o - (s_mean[c] - o) / (float)(nall - 1) : o;
       acc += dl_do[rc] * dev * cum;
     }
   }
@@ -786,13 +870,18 @@ __global__ void observe_heterotypic_kernel(const uint32_t* __restrict__ lat,
 
 cudaError_t launch_lr_backward(const float* scores, const float* dl_do,
                                const float* obs, const int* checkpoints, int nrep,
-                               int len, int nparam, int ncheck, float* grad,
-                               cudaStream_t s) {
+                               int len, int nparam, int ncheck, const float* obs_total,
+                               int nrep_total, float* grad, cudaStream_t s) {
   if (ncheck < 1 || ncheck > kMaxCheckpoints || nparam < 1 || nparam > kScoreMax)
     return cudaErrorInvalidValue;
   Checkpoints cp;
   cp.n = ncheck;
-  for (int c = 0; c < ncheck; ++c) cp.t[c] = checkpoints[c];
+  cp.use_total = obs_total ? 1 : 0;
+  cp.nrep_total = nrep_total;
+  for (int c = 0; c < ncheck; ++c) {
+    cp.t[c] = checkpoints[c];
+    cp.total[c] = obs_total ? obs_total[c] : 0.0f;
+  }
   lr_backward_kernel<<<nparam, 256, 0, s>>>(scores, dl_do, obs, cp, nrep, len, grad);
   return cudaGetLastError();
 }

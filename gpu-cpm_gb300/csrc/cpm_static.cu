@@ -43,9 +43,7 @@ constexpr size_t kOffDap0 = kOffCs1 + align256(8 * 3 * kMaxRows);
 constexpr size_t kOffDap1 = kOffDap0 + align256(8 * kMaxRows);
 constexpr size_t kOffDcs0 = kOffDap1 + align256(8 * kMaxRows);
 constexpr size_t kOffDcs1 = kOffDcs0 + align256(8 * 3 * kMaxRows);
-constexpr size_t kOffFlag0 = kOffDcs1 + align256(8 * 3 * kMaxRows);
-constexpr size_t kOffFlag1 = kOffFlag0 + align256(4 * kMaxRows);
-constexpr size_t kOffFirst = kOffFlag1 + align256(4 * kMaxRows);
+constexpr size_t kOffFirst = kOffDcs1 + align256(8 * 3 * kMaxRows);
 constexpr size_t kOffCtype = kOffFirst + align256(8 * kMaxRows);
 constexpr size_t kOffList = kOffCtype + align256(4 * kMaxRows);
 constexpr size_t kOffCtl = kOffList + align256(4 * kListEntries);
@@ -208,7 +206,7 @@ extern "C" int cpm_sweep_static(int dimensionality, int nx, int ny, int nz,
 
   // Everything the sweep expects to start at zero (the array keeps the last
   // call's contents, and a failed call may have left deltas behind).
-  // (deltas and dirty flags of both phases: kOffDap0 .. kOffFirst)
+  // (deltas of both phases: kOffDap0 .. kOffFirst)
   STATIC_CUDA(cudaMemsetAsync(w + kOffDap0, 0, kOffFirst - kOffDap0, s));
   STATIC_CUDA(cudaMemsetAsync(ctl, 0, 4 * kCtlWords, s));
   STATIC_CUDA(cudaMemsetAsync(counters, 0, 16, s));
@@ -268,8 +266,6 @@ extern "C" int cpm_sweep_static(int dimensionality, int nx, int ny, int nz,
     a.dap[1] = reinterpret_cast<unsigned long long*>(w + kOffDap1);
     a.dcs[0] = reinterpret_cast<long long*>(w + kOffDcs0);
     a.dcs[1] = reinterpret_cast<long long*>(w + kOffDcs1);
-    a.dflag[0] = reinterpret_cast<uint32_t*>(w + kOffFlag0);
-    a.dflag[1] = reinterpret_cast<uint32_t*>(w + kOffFlag1);
     a.dlist = reinterpret_cast<uint32_t*>(w + kOffList);
     a.ctl = ctl;
     a.counters = counters;
@@ -300,6 +296,8 @@ extern "C" int cpm_sweep_static(int dimensionality, int nx, int ny, int nz,
   }
   if (word & kErrTimeout)
     return fail(CPM_ERR_TIMEOUT, "cpm_sweep_static: a grid barrier of the sweep timed out");
+  if (word & kErrListFull)
+    return fail(CPM_ERR_CUDA, "cpm_sweep_static: a dirty list was too small (internal error)");
   if (word)
     return fail(CPM_ERR_INVALID, "cpm_sweep_static: the sweep met an id above number_of_cells");
   return CPM_OK;

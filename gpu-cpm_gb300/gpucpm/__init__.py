@@ -40,6 +40,8 @@ CPM_ERR_STATE = 4
 CPM_ERR_TIMEOUT = 5
 CPM_ERR_UNSUPPORTED = 6
 MAX_TYPES = 32
+DISPATCH_GRID = 0
+DISPATCH_REPLICA = 1
 
 
 class CpmError(RuntimeError):
@@ -147,7 +149,8 @@ def library():
         "cpm_run_graph": [H, ctypes.c_int],
         "cpm_autotune": [H, ctypes.c_int, ip, ctypes.POINTER(ctypes.c_float)],
         "cpm_set_variant": [H, ctypes.c_int],
-        "cpm_sweep_config": [H, ip, ip, ip, ip, ip, ip],
+        "cpm_sweep_config": [H, ip, ip, ip, ip, ip, ip, ip],
+        "cpm_set_dispatch": [H, ctypes.c_int],
         "cpm_run_scores": [H, ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int,
                            ctypes.POINTER(ScoreSpec)],
         "cpm_observe_heterotypic": [H, ctypes.c_void_p],
@@ -161,7 +164,8 @@ def library():
         ctypes.c_uint64, ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]
     L.cpm_sweep_static.restype = ctypes.c_int
     L.cpm_lr_backward.argtypes = [ctypes.c_void_p] * 3 + [ctypes.POINTER(ctypes.c_int)] + [
-        ctypes.c_int] * 4 + [ctypes.c_void_p, ctypes.c_void_p]
+        ctypes.c_int] * 4 + [ctypes.POINTER(ctypes.c_float), ctypes.c_int, ctypes.c_void_p,
+                             ctypes.c_void_p]
     L.cpm_lr_backward.restype = ctypes.c_int
     L.cpm_set_device.argtypes = [ctypes.c_int]
     L.cpm_set_device.restype = ctypes.c_int
@@ -292,6 +296,11 @@ class _Engine:
     def set_variant(self, variant):
         self._call("cpm_set_variant", int(variant))
 
+    def set_dispatch(self, dispatch):
+        """DISPATCH_GRID (all warps on every slot of all replicas) or
+        DISPATCH_REPLICA (a block runs whole replicas); same results."""
+        self._call("cpm_set_dispatch", int(dispatch))
+
     def run_scores(self, mcs, scores_ptr, score_base, score_len, spec):
         """cpm_run plus likelihood-ratio scores into a device float buffer
         [n_replicas][score_len][SCORE_MAX] (2D engines)."""
@@ -306,11 +315,13 @@ class _Engine:
         return out
 
     def sweep_config(self):
-        """dict(variant, tile, warps_per_block, grid) of the launch runs use."""
-        vals = [ctypes.c_int() for _ in range(6)]
+        """dict(variant, tile, warps_per_block, grid, dispatch) of the launch
+        runs use."""
+        vals = [ctypes.c_int() for _ in range(7)]
         self._call("cpm_sweep_config", *[ctypes.byref(v) for v in vals])
-        v, tx, ty, tz, w, g = (x.value for x in vals)
-        return {"variant": v, "tile": (tx, ty, tz), "warps_per_block": w, "grid": g}
+        v, tx, ty, tz, w, g, d = (x.value for x in vals)
+        return {"variant": v, "tile": (tx, ty, tz), "warps_per_block": w, "grid": g,
+                "dispatch": "replica" if d == DISPATCH_REPLICA else "grid"}
 
 
 class Cpm(_Engine):
@@ -464,18 +475,33 @@ class Batch(_Engine):
         """Writable host view of one replica's lattice ([y, x] / [z, y, x])."""
         return self._host_view(replica, tuple(reversed(self.sizes[replica])))
 
+    # replica None: every replica of the batch
     def set_temperature(self, replica, temperature):
-        self._call("cpm_set_temperature_r", int(replica), float(temperature))
+        if replica is None:
+            self._call("cpm_set_temperature", float(temperature))
+        else:
+            self._call("cpm_set_temperature_r", int(replica), float(temperature))
 
     def set_area(self, replica, cell_type, target, lam):
-        self._call("cpm_set_area_r", int(replica), int(cell_type), int(target), float(lam))
+        if replica is None:
+            self._call("cpm_set_area", int(cell_type), int(target), float(lam))
+        else:
+            self._call("cpm_set_area_r", int(replica), int(cell_type), int(target), float(lam))
 
     def set_perimeter(self, replica, cell_type, target, lam):
-        self._call("cpm_set_perimeter_r", int(replica), int(cell_type), int(target), float(lam))
+        if replica is None:
+            self._call("cpm_set_perimeter", int(cell_type), int(target), float(lam))
+        else:
+            self._call("cpm_set_perimeter_r", int(replica), int(cell_type), int(target),
+                       float(lam))
 
     def set_adhesion(self, replica, cell_type, other, J, symmetric=True):
-        self._call("cpm_set_adhesion_r", int(replica), int(cell_type), int(other), float(J),
-                   1 if symmetric else 0)
+        if replica is None:
+            self._call("cpm_set_adhesion", int(cell_type), int(other), float(J),
+                       1 if symmetric else 0)
+        else:
+            self._call("cpm_set_adhesion_r", int(replica), int(cell_type), int(other),
+                       float(J), 1 if symmetric else 0)
 
 
 def sweep_static(dimensionality, shape, number_of_cells, lattice_ptr, area_ptr,
@@ -503,16 +529,21 @@ def sweep_static(dimensionality, shape, number_of_cells, lattice_ptr, area_ptr,
 
 
 def lr_backward(scores_ptr, dl_do_ptr, obs_ptr, checkpoints, nrep, length, nparam,
-                grad_ptr, stream=None):
+                grad_ptr, stream=None, obs_total=None, nrep_total=0):
     """Backward kernel of the likelihood-ratio estimator (device pointers):
     grad[k] = sum_r sum_c dL/dO[r,c] (O[r,c] - b[r,c])
                         * sum_{t < checkpoints[c]} scores[r,t,k],
-    b[r,c] = mean of O[.,c] over the other replicas (0 for one replica)."""
+    b[r,c] = mean of O[.,c] over the other replicas (0 for one replica).
+    obs_total (host floats, one per checkpoint) and nrep_total extend "the
+    other replicas" to every shard of a sharded ensemble."""
     cp = (ctypes.c_int * len(checkpoints))(*[int(c) for c in checkpoints])
+    tot = None
+    if obs_total is not None:
+        tot = (ctypes.c_float * len(checkpoints))(*[float(v) for v in obs_total])
     _check(library().cpm_lr_backward(
         ctypes.c_void_p(int(scores_ptr)), ctypes.c_void_p(int(dl_do_ptr)),
         ctypes.c_void_p(int(obs_ptr)), cp, int(nrep), int(length), int(nparam),
-        len(checkpoints), ctypes.c_void_p(int(grad_ptr)),
+        len(checkpoints), tot, int(nrep_total), ctypes.c_void_p(int(grad_ptr)),
         ctypes.c_void_p(int(stream) if stream else None)), None)
 
 

@@ -25,6 +25,14 @@ d E[f(O)] / d theta.
 Because the Philox stream is a pure function of (seed, replica, site,
 phase), two forward passes with the same seed use common random numbers,
 which is what `crn_finite_difference` relies on.
+
+Sharded ensembles: with `group` (a torch.distributed process group, one
+process per GPU, each holding its own replicas with distinct stream ids),
+backward all-reduces the per-checkpoint sums of O and the replica count
+before the backward kernel, so that the baseline runs over every shard's
+replicas, and all-reduces the gradient after it (averaged over shards, the
+convention of data-parallel training: each shard's loss is the mean over
+its own replicas).  These two small all-reduces are the only collectives.
 """
 import numpy as np
 import torch
@@ -35,10 +43,11 @@ import gpucpm
 class Ensemble:
     def __init__(self, workloads, pairs=((1, 1), (2, 2), (1, 2), (1, 0), (2, 0)),
                  lambda_area=True, temperature=True, seed=0, stream_id=0, device=0,
-                 lambda_perim=False):
+                 lambda_perim=False, group=None):
         if any(w.ndim != 2 for w in workloads):
             raise ValueError("likelihood-ratio ensembles are 2D")
         self.workloads = list(workloads)
+        self.group = group
         self.spec = gpucpm.ScoreSpec.make(pairs, lambda_area, temperature, lambda_perim)
         self.pairs = [tuple(p) for p in pairs]
         self.seed, self.stream_id = int(seed), int(stream_id)
@@ -48,9 +57,24 @@ class Ensemble:
         self.stream = torch.cuda.Stream(device=self.device)
         self.batch.set_stream(self.stream.cuda_stream)
         self.batch.set_seed(self.seed, self.stream_id)
-        for r, w in enumerate(self.workloads):
-            w.apply(self.batch, replica=r)
+        # replicas built from one Workload object share its parameters, which
+        # are then set once for all replicas (replica None)
+        self._shared = all(w is self.workloads[0] for w in self.workloads)
+        if self._shared:
+            w = self.workloads[0]
+            nt = w.J.shape[0]
+            for a in range(nt):
+                for b in range(nt):
+                    self.batch.set_adhesion(None, a, b, float(w.J[a, b]), symmetric=False)
+                self.batch.set_area(None, a, int(w.tgt_area[a]), float(w.lam_area[a]))
+                self.batch.set_perimeter(None, a, int(w.tgt_perim[a]), float(w.lam_perim[a]))
+            self.batch.set_temperature(None, w.temperature)
+        else:
+            for r, w in enumerate(self.workloads):
+                w.apply(self.batch, replica=r)
         self.cell_types = sorted({t for w in self.workloads for t in range(1, w.J.shape[0])})
+        self._views = [self.batch.lattice(r) for r in range(len(self.workloads))]
+        self._initial = {id(w): w.lattice.view(np.int32) for w in self.workloads}
 
     @property
     def nparam(self):
@@ -71,27 +95,27 @@ class Ensemble:
     def _apply_theta(self, theta):
         th = [float(v) for v in theta]
         k = 0
-        for a, b in self.pairs:
-            for r in range(len(self.workloads)):
-                self.batch.set_adhesion(r, a, b, th[k], symmetric=True)
+        for a, b in self.pairs:  # the same value on every replica
+            self.batch.set_adhesion(None, a, b, th[k], symmetric=True)
             k += 1
+        # lambdas keep each replica's own targets
+        reps = [(None, self.workloads[0])] if self._shared else list(enumerate(self.workloads))
         if self.spec.lambda_area:
-            for r, w in enumerate(self.workloads):
+            for r, w in reps:
                 for t in self.cell_types:
                     self.batch.set_area(r, t, int(w.tgt_area[t]), th[k])
             k += 1
         if self.spec.lambda_perim:
-            for r, w in enumerate(self.workloads):
+            for r, w in reps:
                 for t in self.cell_types:
                     self.batch.set_perimeter(r, t, int(w.tgt_perim[t]), th[k])
             k += 1
         if self.spec.temperature:
-            for r in range(len(self.workloads)):
-                self.batch.set_temperature(r, th[k])
+            self.batch.set_temperature(None, th[k])
 
     def _restart(self):
-        for r, w in enumerate(self.workloads):
-            self.batch.lattice(r)[...] = w.lattice.view(np.int32)
+        for v, w in zip(self._views, self.workloads):
+            v[...] = self._initial[id(w)]
         self.batch.push_to_gpu()
         self.batch.tick = 0
         self.batch.reset_counters()
@@ -144,10 +168,32 @@ class LikelihoodRatio(torch.autograd.Function):
         dl = grad_O.detach().to(device=O.device, dtype=torch.float32).contiguous()
         grad = torch.zeros(ens.nparam, dtype=torch.float32, device=O.device)
         stream = torch.cuda.current_stream(O.device)
+        tot, ntot = (None, 0) if ens.group is None else shard_totals(O, ens.group)
         gpucpm.lr_backward(sc.data_ptr(), dl.data_ptr(), O.contiguous().data_ptr(), ctx.cps,
                            O.shape[0], ctx.mcs, ens.nparam, grad.data_ptr(),
-                           stream.cuda_stream)
+                           stream.cuda_stream, obs_total=tot, nrep_total=ntot)
+        if ens.group is not None:
+            reduce_gradient(grad, ens.group)
         return grad.to(ctx.theta_device, ctx.theta_dtype), None, None, None
+
+
+def shard_totals(O, group=None):
+    """Sum of O[:, c] over the replicas of every shard (one float per
+    checkpoint) and the number of those replicas: one all-reduce."""
+    import torch.distributed as dist
+    buf = torch.cat([O.detach().double().sum(dim=0),
+                     torch.tensor([float(O.shape[0])], dtype=torch.float64, device=O.device)])
+    dist.all_reduce(buf, group=group)
+    vals = buf.cpu().tolist()
+    return vals[:-1], int(round(vals[-1]))
+
+
+def reduce_gradient(grad, group=None):
+    """Average of the shards' gradients, in place: one all-reduce."""
+    import torch.distributed as dist
+    dist.all_reduce(grad, group=group)
+    grad /= dist.get_world_size(group)
+    return grad
 
 
 def crn_finite_difference(ensemble, theta, mcs, rel_step=0.01, checkpoint=None,

@@ -147,7 +147,8 @@ int cpm_pull(cpm_handle* h);
 int cpm_run(cpm_handle* h, int mcs);
 
 /* Same as cpm_run as one CUDA-graph launch: the first call with a given
- * `mcs` (or after cpm_autotune / cpm_set_variant / cpm_set_stream) captures
+ * `mcs` (or after cpm_autotune / cpm_set_variant / cpm_set_dispatch /
+ * cpm_set_stream) captures
  * the run (barrier reset + the persistent sweep) into a graph; every call
  * replays it.  The captured sweep reads its start time from device memory
  * and advances it, so replays continue the Monte Carlo time like cpm_run.
@@ -155,21 +156,38 @@ int cpm_run(cpm_handle* h, int mcs);
  * counterpart in the reference.  1 <= mcs <= 65536. */
 int cpm_run_graph(cpm_handle* h, int mcs);
 
+/* Dispatch of a sweep launch over the replicas of a batch:
+ *   CPM_DISPATCH_GRID     the tiles of a slot, over all replicas, go to all
+ *                         warps of the grid; one grid barrier per phase
+ *                         (one large lattice, or a few);
+ *   CPM_DISPATCH_REPLICA  each block claims whole replicas, largest first,
+ *                         and runs all their phases with block barriers, so
+ *                         a replica's lattice and tables stay near one SM
+ *                         (many small replicas).
+ * Results do not depend on the dispatch.  A batch starts with REPLICA when
+ * it has a replica for every block and none is much larger than a block's
+ * share of the sites, else GRID. */
+#define CPM_DISPATCH_GRID 0
+#define CPM_DISPATCH_REPLICA 1
+
 /* Project autotuner: times `probe_mcs` MCS of every compiled tile variant
- * (warp tile shape and warps per block) on a saved copy of the current state,
- * restores the state, and makes the fastest variant the one later runs use.
- * The sweep's result does not depend on the variant.  *chosen (may be NULL)
- * receives the variant, *ms_per_mcs (may be NULL) its time per MCS.  No
- * counterpart in the reference, whose geometry is passed per run() call
+ * (warp tile shape and warps per block), under both dispatches for a batch,
+ * on a saved copy of the current state, restores the state, and makes the
+ * fastest pair the one later runs use.  The sweep's result does not depend
+ * on either choice.  *chosen (may be NULL) receives the variant,
+ * *ms_per_mcs (may be NULL) its time per MCS.  No counterpart in the
+ * reference, whose geometry is passed per run() call
  * (src/python_wrapper.cpp:182-227). */
 int cpm_autotune(cpm_handle* h, int probe_mcs, int* chosen, float* ms_per_mcs);
 
-/* Select a tile variant explicitly (0, 1 or 2) / describe the current one:
- * warp tile extent in targets, warps per block and grid size. */
+/* Select a tile variant (0, 1 or 2) or a dispatch explicitly / describe the
+ * current launch: warp tile extent in targets, warps per block, grid size
+ * and dispatch. */
 int cpm_set_variant(cpm_handle* h, int variant);
+int cpm_set_dispatch(cpm_handle* h, int dispatch);
 int cpm_sweep_config(const cpm_handle* h, int* variant, int* tile_x,
                      int* tile_y, int* tile_z, int* warps_per_block,
-                     int* grid);
+                     int* grid, int* dispatch);
 
 /* Replaces Cpm::synchronize (src/cpm.cu:653-655).  Waits for the handle's
  * stream and reports device-side errors (CPM_ERR_TIMEOUT, CPM_ERR_CUDA). */
@@ -258,13 +276,17 @@ int cpm_observe_heterotypic(cpm_handle* h, float* out_host);
  *                     * sum_{t < checkpoints[c]} scores[r][t][k]
  * with the leave-one-out baseline b[r][c] = mean of obs[.][c] over the
  * other replicas (0 when R = 1).  For a loss L = mean_r f(obs[r]) this is
- * an unbiased estimate of dE[f]/dtheta.  scores, dl_do, obs and
+ * an unbiased estimate of dE[f]/dtheta.  When the replicas are sharded over
+ * processes, obs_total (host, [ncheck]: sum of obs[.][c] over every shard)
+ * and nrep_total (replicas of every shard) make the baseline global; NULL
+ * and 0 use this launch's replicas only.  scores, dl_do, obs and
  * grad are device pointers ([R][len][CPM_SCORE_MAX], [R][ncheck], [R][ncheck],
  * [nparam]); checkpoints is a host array of ncheck (<= 64) MCS counts.
  * Enqueued on `stream` (NULL: default stream). */
 int cpm_lr_backward(const float* scores, const float* dl_do, const float* obs,
                     const int* checkpoints, int nrep, int len, int nparam,
-                    int ncheck, float* grad, void* stream);
+                    int ncheck, const float* obs_total, int nrep_total,
+                    float* grad, void* stream);
 
 /* ---- sweep without allocation ------------------------------------------ */
 

@@ -165,16 +165,18 @@ struct ScoreSpec {
   int temperature;
 };
 
-// d log P(decision)/d theta of one evaluated attempt with dH > 0, in FP64
-// from the attempt's (FP32) decision: P(accept) = exp(-x), x = dH / T;
-// accept contributes -dx/dtheta, reject exp(-x)/(1-exp(-x)) dx/dtheta.
+// d log P(decision)/d theta of one evaluated attempt with dH >= 0, in FP64
+// from the attempt's (FP32) decision: P(accept) = min(1, exp(-x)), x = dH / T;
+// accept contributes -dx/dtheta, reject exp(-x)/(1-exp(-x)) dx/dtheta.  At
+// dH = 0 exactly P has a kink (slope -dx/dtheta on one side, 0 on the
+// other) and the score is the mean of the two, -dx/dtheta / 2.
 // dx/dJ_ab = (changes of the a-b contact count) / T, dx/dlambda_area and
 // dx/dlambda_perim = (the integer area / perimeter terms) / T, dx/dT = -x / T.
 void add_score(const ScoreSpec& sp, const uint32_t* nb, int N, uint32_t s, uint32_t t,
                int64_t da, int64_t dp, double dH, double T, bool accepted,
                double* sc) {
   const double x = dH / T;
-  const double coef = accepted ? -1.0 : std::exp(-x) / -std::expm1(-x);
+  const double coef = dH == 0.0 ? -0.5 : accepted ? -1.0 : std::exp(-x) / -std::expm1(-x);
   const double cT = coef / T;
   const int ts = (int)(s >> 24), tt = (int)(t >> 24);
   for (int k = 0; k < sp.n_pairs; ++k) {
@@ -271,7 +273,7 @@ inline int attempt(const Params& p, uint32_t* lat, const Tables& tb, int x,
     const float u = (float)((r[1] >> 8) | 1u) * 0x1p-24f;
     ok = u < exp_neg(-dH / p.temperature);
   }
-  if (sp && dH > 0.0f && p.temperature > 0.0f) {
+  if (sp && dH >= 0.0f && p.temperature > 0.0f) {
     const int64_t da = (s ? 1 + 2 * ((int64_t)tb.area[is] - p.tgt_area[ts]) : 0) +
                        (t ? 1 - 2 * ((int64_t)tb.area[it] - p.tgt_area[tt]) : 0);
     const int64_t dp =

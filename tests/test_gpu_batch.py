@@ -109,3 +109,93 @@ def test_autotune_leaves_state_unchanged(engine_lib):
     lat = _state(e)[0]
     sim = oracle.OracleSim(w.lattice, w.ncells, **w.oracle_kwargs(), seed=5).run(7)
     np.testing.assert_array_equal(lat.view(np.uint32), sim.lattice)
+
+
+def _batch(ws, seed, stream0):
+    import gpucpm
+    b = gpucpm.Batch(ws[0].ndim, [w.lattice.shape[::-1] for w in ws], [w.ncells for w in ws])
+    for r, w in enumerate(ws):
+        b.lattice(r)[...] = w.lattice.view(np.int32)
+        w.apply(b, replica=r)
+    b.set_seed(seed, stream0)
+    b.push_to_gpu()
+    return b
+
+
+def _batch_state(b, n):
+    b.synchronize()
+    b.pull_from_gpu()
+    return [(b.lattice(r).copy(), *b.tables(r), b.counters(r)) for r in range(n)]
+
+
+@pytest.mark.parametrize("dims", [2, 3])
+@pytest.mark.parametrize("variant", [0, 2])
+def test_replica_dispatch_matches_oracle_and_grid(engine_lib, dims, variant):
+    """Blocks running whole replicas (largest first) give the same lattices,
+    tables and counters as the grid dispatch and as the oracle, for ragged
+    sizes including odd sides, plain and graph-captured runs."""
+    import gpucpm
+    shapes = ([(40, 44), (64, 64), (33, 70), (21, 19), (96, 50)] if dims == 2 else
+              [(12, 13, 14), (16, 16, 16), (9, 11, 10)])
+    ws = [W.random_small(s, 12 + 6 * i, seed=70 + i, temperature=6.0 + i)
+          for i, s in enumerate(shapes)]
+    mcs = 5 if dims == 2 else 3
+    out = {}
+    for d in (gpucpm.DISPATCH_GRID, gpucpm.DISPATCH_REPLICA):
+        b = _batch(ws, seed=17, stream0=30)
+        b.set_variant(variant)
+        b.set_dispatch(d)
+        cfg = b.sweep_config()
+        assert cfg["dispatch"] == ("replica" if d == gpucpm.DISPATCH_REPLICA else "grid")
+        b.run_mcs(mcs)
+        b.run_graph(mcs)
+        out[d] = _batch_state(b, len(ws))
+    for r, w in enumerate(ws):
+        sim = oracle.OracleSim(w.lattice, w.ncells, **w.oracle_kwargs(), seed=17,
+                               stream=30 + r).run(2 * mcs)
+        for d in out:
+            lat, a, p, c, cnt = out[d][r]
+            np.testing.assert_array_equal(lat.view(np.uint32), sim.lattice)
+            np.testing.assert_array_equal(a, sim.area)
+            np.testing.assert_array_equal(p, sim.perim)
+            np.testing.assert_array_equal(c, sim.csum)
+            assert cnt["accepted"] == int(sim.counters[2])
+
+
+def test_replica_dispatch_scores_and_autotune(engine_lib):
+    """Score launches under replica dispatch equal those under grid dispatch
+    (FP32 sums, summation order differs); the autotuner over variants and
+    dispatches leaves the batch state unchanged."""
+    import torch
+
+    import gpucpm
+    ws = [W.sorting_2d(n=40 + 8 * i, ncells=20 + 5 * i, seed=60 + i) for i in range(4)]
+    spec = gpucpm.ScoreSpec.make(((1, 1), (2, 2), (1, 2)), lambda_perim=True)
+    res = {}
+    for d in (gpucpm.DISPATCH_GRID, gpucpm.DISPATCH_REPLICA):
+        b = _batch(ws, seed=4, stream0=0)
+        b.set_dispatch(d)
+        sc = torch.zeros((len(ws), 6, gpucpm.SCORE_MAX), device="cuda")
+        torch.cuda.synchronize()
+        b.run_scores(6, sc.data_ptr(), 0, 6, spec)
+        res[d] = (_batch_state(b, len(ws)), sc.cpu().numpy())
+    (sg, scg), (sr, scr) = res[gpucpm.DISPATCH_GRID], res[gpucpm.DISPATCH_REPLICA]
+    for r in range(len(ws)):
+        np.testing.assert_array_equal(sg[r][0], sr[r][0])
+    scale = np.abs(scg).max(axis=(0, 1)) + 1e-6
+    assert (np.abs(scg - scr) / scale).max() < 1e-4
+    b = _batch(ws, seed=4, stream0=0)
+    b.run_mcs(2)
+    before = _batch_state(b, len(ws))
+    variant, ms = b.autotune(probe_mcs=1)
+    assert variant in (0, 1, 2) and ms > 0
+    after = _batch_state(b, len(ws))
+    for x, y in zip(before, after):
+        for u, v in zip(x[:4], y[:4]):
+            np.testing.assert_array_equal(u, v)
+    b.run_mcs(3)
+    fin = _batch_state(b, len(ws))
+    for r, w in enumerate(ws):
+        sim = oracle.OracleSim(w.lattice, w.ncells, **w.oracle_kwargs(), seed=4,
+                               stream=r).run(5)
+        np.testing.assert_array_equal(fin[r][0].view(np.uint32), sim.lattice)

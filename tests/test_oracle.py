@@ -245,31 +245,43 @@ PAIRS = ((1, 1), (2, 2), (1, 2), (1, 0), (2, 0))
 
 
 def _log_p(dH, T, accepted):
-    x = dH / T
+    """log of P(decision), P(accept) = min(1, exp(-dH/T))."""
+    x = max(dH, 0.0) / T
     return -x if accepted else math.log(-math.expm1(-x))
 
 
-def test_oracle_scores_are_derivatives_of_the_decision_log_likelihood():
+@pytest.mark.parametrize("case", ["voronoi_perimeter", "sorting_integer"])
+def test_oracle_scores_are_derivatives_of_the_decision_log_likelihood(case):
     """Replay one MCS with the reference's dH formula (as above); for every
-    evaluated attempt with dH > 0 differentiate log P(its decision) by
+    evaluated attempt with dH >= 0 differentiate log P(its decision) by
     central differences in each parameter, with the lattice and tables of
     that moment held fixed, and compare the sum with the oracle's FP64
-    scores for that MCS."""
-    w = W.random_small((16, 16), 10, seed=11, temperature=6.0)
-    J = np.rint(w.J).astype(float)
-    lam_a = [0.0, 1.0, 1.0]
-    tgt_a = [0, 20, 20]
-    lam_p = [0.0, 0.5, 0.5]
-    tgt_p = [0, 18, 18]
-    T = 6.0
+    scores for that MCS.  At dH = 0 (frequent with integer parameters) the
+    central difference is the mean of the two one-sided slopes, the value
+    the scores use there."""
+    if case == "voronoi_perimeter":
+        w = W.random_small((16, 16), 10, seed=11, temperature=6.0)
+        J = np.rint(w.J).astype(float)
+        lam_a, tgt_a = [0.0, 1.0, 1.0], [0, 20, 20]
+        lam_p, tgt_p = [0.0, 0.5, 0.5], [0, 18, 18]
+        T = 6.0
+    else:  # integer J and area terms, no perimeter term: many dH = 0 exactly
+        w = W.sorting_grid(n=30, ncells=35, seed=2)
+        J = w.J.astype(float)
+        lam_a, tgt_a = [0.0, 1.0, 1.0], [0, 25, 25]
+        lam_p, tgt_p = [0.0, 0.0, 0.0], [0, 0, 0]
+        T = 10.0
     sim = oracle.OracleSim(w.lattice, w.ncells, J.astype(np.float32), lam_a, tgt_a,
                            lam_p, tgt_p, temperature=T, seed=7)
+    # the sorting case replays MCS 6, once the squares have roughened
+    tick0 = 5 if case == "sorting_integer" else 0
+    sim.run(tick0)
     spec = oracle.ScoreSpec.make(PAIRS, lambda_perim=True)
-    lat = w.lattice.copy()
+    lat = sim.lattice.copy()
     area, perim = sim.area.copy(), sim.perim.copy()
-    n = 16
+    n = lat.shape[0]
     want = np.zeros(8)
-    evaluated_pos = 0
+    evaluated_pos = zero_dh = 0
 
     def dH_of(theta, ax, ay, sx, sy):
         Jt = J.copy()
@@ -279,7 +291,7 @@ def test_oracle_scores_are_derivatives_of_the_decision_log_likelihood():
         lp = [0.0, theta[6], theta[6]]
         return _reference_dh(lat, ax, ay, sx, sy, area, perim, Jt, la, tgt_a, lp, tgt_p)
 
-    theta = np.array([J[a, b] for a, b in PAIRS] + [1.0, 0.5, T])
+    theta = np.array([J[a, b] for a, b in PAIRS] + [1.0, lam_p[1], T])
     for cy in (0, 1):
         for cx in (0, 1):
             slot = cy * 3 + cx
@@ -292,7 +304,7 @@ def test_oracle_scores_are_derivatives_of_the_decision_log_likelihood():
                     vals = [int(lat[b % n, a % n]) for a, b in nbs]
                     if all(v == t for v in vals):
                         continue
-                    r = oracle.philox4x32_10([y * n + x, slot, 0, 0], [7, 0])
+                    r = oracle.philox4x32_10([y * n + x, tick0 * 9 + slot, 0, 0], [7, 0])
                     k = (r[0] * 8) >> 32
                     if vals[k] == t:
                         continue
@@ -300,10 +312,17 @@ def test_oracle_scores_are_derivatives_of_the_decision_log_likelihood():
                     dH = dH_of(theta, x, y, sx, sy)
                     u = ((r[1] >> 8) | 1) * 2.0 ** -24
                     acc = dH < 0 or u < math.exp(-dH / T)
-                    if dH > 0:
+                    if dH == 0:
+                        zero_dh += 1
+                    if dH >= 0:
                         evaluated_pos += 1
                         for q in range(8):
                             h = 1e-4 * max(1.0, abs(theta[q]))
+                            if case == "sorting_integer" and q == 6:
+                                # lambda_perim = 0; perimeter terms of ~700 and
+                                # a large cancellation between accepted and
+                                # rejected attempts call for a small step
+                                h = 1e-6
                             tp, tm = theta.copy(), theta.copy()
                             tp[q] += h
                             tm[q] -= h
@@ -322,5 +341,7 @@ def test_oracle_scores_are_derivatives_of_the_decision_log_likelihood():
                     perim[t & 0xFFFFFF] += 2 * sum(v == t for v in vals) - 8
     got = sim.run_scores(1, spec)[0, :8]
     assert evaluated_pos > 20
+    if case == "sorting_integer":
+        assert zero_dh > 0
     np.testing.assert_allclose(got, want, rtol=1e-5, atol=1e-6)
     np.testing.assert_array_equal(sim.lattice, lat)
