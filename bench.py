@@ -344,6 +344,8 @@ def run_ours(args, world, rank, local):
     stream = torch.cuda.Stream()
     sim.set_stream(stream.cuda_stream)
     sim.push_to_gpu()
+    # the engine's own autotuner picks the tile variant (state is restored)
+    variant, tuned_ms = sim.autotune(probe_mcs=2)
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
 
     for _ in range(args.warmup):
@@ -416,7 +418,9 @@ def run_ours(args, world, rank, local):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "u32+f32", "data": "synthetic (seeded Voronoi tissue)",
-            "config": describe(w, mcs), "roofline": roofline, "e2e": e2e,
+            "config": dict(describe(w, mcs), tile=sim.sweep_config()["tile"]),
+            "roofline": roofline, "e2e": e2e,
+            "autotune": {"variant": variant, "probe_ms_per_mcs": tuned_ms},
             "gpu_launches": int(launches), "clocks": clocks,
             "mcs_per_s": value / w.nsites / world,
             "wall_s": wall, "step_ms": step_ms}

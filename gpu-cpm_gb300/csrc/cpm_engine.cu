@@ -43,8 +43,15 @@ struct cpm_handle {
   int nrep = 0;
   int device = 0;
   std::vector<DevReplica> reps;
-  std::vector<DevParams> params;
+  // Parameter records shared by replicas (reps[r].pset), copied on the first
+  // write that addresses one replica only; records no replica uses are
+  // dropped at upload.  A batch whose replicas share their parameters
+  // uploads one record.
+  std::vector<DevParams> psets;
+  std::vector<int> pset_refs;  // replicas using each record
   bool params_dirty = true;
+  bool reps_dirty = false;  // some reps[r].pset changed since the last upload
+  int params_cap = 0;       // records d_params holds
   long long total_sites = 0;
   long long rows = 0;
 
@@ -227,8 +234,10 @@ int build_engine(int n, int ndim, const int* nx, const int* ny, const int* nz,
   }
   h->total_sites = sites;
   h->rows = rows;
-  h->params.resize(n);
-  for (auto& p : h->params) default_params(p, T);
+  h->psets.resize(1);
+  default_params(h->psets[0], T);
+  h->pset_refs.assign(1, n);
+  for (auto& R : h->reps) R.pset = 0;
   h->attempts.assign(n, 0);
 
   cudaError_t e = cudaGetDevice(&h->device);
@@ -249,7 +258,8 @@ int build_engine(int n, int ndim, const int* nx, const int* ny, const int* nz,
   al((void**)&h->d_first, sizeof(unsigned long long) * rows);
   al((void**)&h->d_ctype, sizeof(int) * rows);
   al((void**)&h->d_reps, sizeof(DevReplica) * n);
-  al((void**)&h->d_params, sizeof(DevParams) * n);
+  al((void**)&h->d_params, sizeof(DevParams));
+  h->params_cap = 1;
   al((void**)&h->d_task_prefix, sizeof(int) * kTileVariants * 27 * (n + 1));
   al((void**)&h->d_rep_order, sizeof(int) * n);
   al((void**)&h->d_tick, sizeof(unsigned long long));
@@ -390,10 +400,20 @@ template <class F>
 int for_replicas(cpm_handle* h, int r, F&& f) {
   if (!h) return CPM_ERR_INVALID;
   if (r == -1) {
-    for (auto& p : h->params) f(p);
+    for (size_t i = 0; i < h->psets.size(); ++i)
+      if (h->pset_refs[i] > 0) f(h->psets[i]);
   } else {
     if (int rc = check_replica(h, r)) return rc;
-    f(h->params[r]);
+    int p = h->reps[r].pset;
+    if (h->pset_refs[p] > 1) {  // shared: give replica r its own copy
+      h->psets.push_back(h->psets[p]);
+      h->pset_refs.push_back(1);
+      --h->pset_refs[p];
+      p = (int)h->psets.size() - 1;
+      h->reps[r].pset = p;
+      h->reps_dirty = true;
+    }
+    f(h->psets[p]);
   }
   h->params_dirty = true;
   return CPM_OK;
@@ -424,6 +444,25 @@ int set_perimeter(cpm_handle* h, int r, int type, int target, float lambda) {
   });
 }
 
+int set_fixed(cpm_handle* h, int r, int type, int fixed) {
+  if (!h) return CPM_ERR_INVALID;
+  if (int rc = check_type(h, type)) return rc;
+  return for_replicas(h, r, [&](DevParams& p) {
+    if (fixed)
+      p.fixed_mask |= 1u << type;
+    else
+      p.fixed_mask &= ~(1u << type);
+  });
+}
+
+int set_stickiness(cpm_handle* h, int r, int type, int other, float S) {
+  if (!h) return CPM_ERR_INVALID;
+  if (int rc = check_type(h, type)) return rc;
+  if (int rc = check_type(h, other)) return rc;
+  if (!std::isfinite(S)) return h->fail(CPM_ERR_INVALID, "stickiness must be finite");
+  return for_replicas(h, r, [&](DevParams& p) { p.stick[type * kMaxTypes + other] = S; });
+}
+
 int set_adhesion(cpm_handle* h, int r, int type, int other, float J, int sym) {
   if (!h) return CPM_ERR_INVALID;
   if (int rc = check_type(h, type)) return rc;
@@ -442,18 +481,58 @@ int read_error_word(cpm_handle* h, uint32_t* word) {
 }
 
 int upload_params(cpm_handle* h) {
-  if (!h->params_dirty) return CPM_OK;
-  for (auto& p : h->params) p.perim_on = perim_on(p) ? 1 : 0;
-  CPM_CUDA(h, cudaMemcpyAsync(h->d_params, h->params.data(), sizeof(DevParams) * h->nrep,
+  if (!h->params_dirty && !h->reps_dirty) return CPM_OK;
+  // Drop records no replica uses and renumber the rest.
+  const int n0 = (int)h->psets.size();
+  std::vector<int> remap(n0, -1);
+  int m = 0;
+  for (int i = 0; i < n0; ++i) {
+    if (h->pset_refs[i] <= 0) continue;
+    remap[i] = m;
+    if (m != i) {
+      h->psets[m] = h->psets[i];
+      h->pset_refs[m] = h->pset_refs[i];
+    }
+    ++m;
+  }
+  if (m != n0) {
+    h->psets.resize(m);
+    h->pset_refs.resize(m);
+    for (auto& R : h->reps) R.pset = remap[R.pset];
+    h->reps_dirty = true;
+  }
+  for (auto& p : h->psets) {
+    p.perim_on = perim_on(p) ? 1 : 0;
+    p.stick_on = 0;
+    for (int k = 0; k < kMaxTypes * kMaxTypes; ++k)
+      if (p.stick[k] != 0.0f) p.stick_on = 1;
+  }
+  if (m > h->params_cap) {
+    CPM_CUDA(h, cudaStreamSynchronize(h->stream));
+    cudaFree(h->d_params);
+    h->d_params = nullptr;
+    h->params_cap = 0;
+    CPM_CUDA(h, cudaMalloc((void**)&h->d_params, sizeof(DevParams) * m));
+    h->params_cap = m;
+    if (h->graph_exec) {  // it holds the old address
+      cudaGraphExecDestroy(h->graph_exec);
+      h->graph_exec = nullptr;
+    }
+  }
+  CPM_CUDA(h, cudaMemcpyAsync(h->d_params, h->psets.data(), sizeof(DevParams) * m,
                               cudaMemcpyHostToDevice, h->stream));
-  CPM_CUDA(h, cudaStreamSynchronize(h->stream));  // the host copy may change next
+  if (h->reps_dirty)
+    CPM_CUDA(h, cudaMemcpyAsync(h->d_reps, h->reps.data(), sizeof(DevReplica) * h->nrep,
+                                cudaMemcpyHostToDevice, h->stream));
+  CPM_CUDA(h, cudaStreamSynchronize(h->stream));  // the host copies may change next
   h->params_dirty = false;
+  h->reps_dirty = false;
   return CPM_OK;
 }
 
 bool any_perimeter(const cpm_handle* h) {
-  for (auto& p : h->params)
-    if (p.perim_on) return true;
+  for (size_t i = 0; i < h->psets.size(); ++i)
+    if (h->pset_refs[i] > 0 && perim_on(h->psets[i])) return true;
   return false;
 }
 
@@ -579,6 +658,16 @@ int cpm_set_perimeter(cpm_handle* h, int type, int target, float lambda) {
 }
 int cpm_set_perimeter_r(cpm_handle* h, int r, int type, int target, float lambda) {
   return set_perimeter(h, r < 0 ? -2 : r, type, target, lambda);
+}
+int cpm_set_fixed(cpm_handle* h, int type, int fixed) { return set_fixed(h, -1, type, fixed); }
+int cpm_set_fixed_r(cpm_handle* h, int r, int type, int fixed) {
+  return set_fixed(h, r < 0 ? -2 : r, type, fixed);
+}
+int cpm_set_stickiness(cpm_handle* h, int type, int other, float S) {
+  return set_stickiness(h, -1, type, other, S);
+}
+int cpm_set_stickiness_r(cpm_handle* h, int r, int type, int other, float S) {
+  return set_stickiness(h, r < 0 ? -2 : r, type, other, S);
 }
 int cpm_set_adhesion(cpm_handle* h, int type, int other, float J, int symmetric) {
   return set_adhesion(h, -1, type, other, J, symmetric);

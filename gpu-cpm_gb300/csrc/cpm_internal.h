@@ -48,11 +48,11 @@ template <int NDIM, int V>
 struct TileGeom;
 template <>
 struct TileGeom<2, 0> {
-  static constexpr int CX = 32, CY = 8, CZ = 1;
+  static constexpr int CX = 32, CY = 6, CZ = 1;
 };
 template <>
 struct TileGeom<2, 1> {
-  static constexpr int CX = 32, CY = 4, CZ = 1;
+  static constexpr int CX = 32, CY = 8, CZ = 1;
 };
 template <>
 struct TileGeom<2, 2> {
@@ -100,20 +100,26 @@ constexpr int kErrListFull = 32;      // a dirty list would overflow (not writte
 // Per-replica parameters, kept in global memory (read through the
 // read-only cache; a replica's few hundred used bytes stay L1-resident).
 struct DevParams {
-  float J[kMaxTypes * kMaxTypes];  // J[own type][neighbour type]
+  float J[kMaxTypes * kMaxTypes];      // J[own type][neighbour type]
+  // stickiness S[own type][neighbour type]: added to the adhesion of the
+  // configuration before the copy only (src/kernels2d.cu:399-400)
+  float stick[kMaxTypes * kMaxTypes];
   float lam_area[kMaxTypes];
   int tgt_area[kMaxTypes];
   float lam_perim[kMaxTypes];
   int tgt_perim[kMaxTypes];
   float temperature;
-  int perim_on;  // any lam_perim != 0
-  int pad[2];
+  int perim_on;         // any lam_perim != 0
+  unsigned fixed_mask;  // bit t: cells of type t never move (src/kernels2d.cu:280-290)
+  int stick_on;         // any stickiness != 0
 };
 
 struct DevReplica {
   int nx, ny, nz, ncells;
   long long lat_off;   // first site of the replica in lat[]
   long long cell_off;  // table row of the replica's id 0
+  int pset;            // its parameter record in params[] (shared by replicas)
+  int pad;
 };
 
 // (area, perimeter) packed in one 64-bit word: area in the low 32 bits (it

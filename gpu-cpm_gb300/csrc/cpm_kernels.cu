@@ -306,7 +306,9 @@ __global__ void __launch_bounds__(kSweepThreadsMax, 1)
       sc_rep = r;
       sc_tick = tick;
     }
-    const DevParams* P = a.params + r;
+    const DevParams* P = a.params + __ldg(&a.reps[r].pset);
+    const unsigned fixed_mask = __ldg(&P->fixed_mask);
+    const bool stick_on = __ldg(&P->stick_on) != 0;
     const int nx = __ldg(&a.reps[r].nx), ny = __ldg(&a.reps[r].ny),
               nz = __ldg(&a.reps[r].nz), ncells = __ldg(&a.reps[r].ncells);
     const long long lat_off = __ldg(&a.reps[r].lat_off);
@@ -390,8 +392,20 @@ __global__ void __launch_bounds__(kSweepThreadsMax, 1)
         philox4x32_10(c0, c1, c2, c3, k0, k1);
         const int kdir = (int)__umulhi(c0, (unsigned)NB);
         const int c = S::center(q);
-        keep = ws.tile[c + S::nb_offset(kdir)] != ws.tile[c];
-        entry = make_uint2((uint32_t)q | ((uint32_t)kdir << 16), c1);
+        const uint32_t tv = ws.tile[c], sv = ws.tile[c + S::nb_offset(kdir)];
+        keep = sv != tv;
+        uint32_t medium = 0;  // 1: the source is replaced by the medium
+        if (fixed_mask && keep) {
+          // a target of a fixed type never changes; a source of a fixed type
+          // proposes the medium instead (src/kernels2d.cu:280-290)
+          if ((fixed_mask >> ((tv >> 24) & (kMaxTypes - 1))) & 1u) {
+            keep = false;
+          } else if ((fixed_mask >> ((sv >> 24) & (kMaxTypes - 1))) & 1u) {
+            medium = 1;
+            keep = tv != 0u;
+          }
+        }
+        entry = make_uint2((uint32_t)q | ((uint32_t)kdir << 16) | (medium << 24), c1);
       }
       const unsigned ball = __ballot_sync(kFull, keep);
       if (keep) ws.qb[nb + __popc(ball & lanemask_lt())] = entry;
@@ -406,10 +420,10 @@ __global__ void __launch_bounds__(kSweepThreadsMax, 1)
       long long push_s = -1, push_t = -1;  // table rows this lane changed
       if (j < nb) {
         const uint2 entry = ws.qb[j];
-        const int q = (int)(entry.x & 0xFFFFu), kdir = (int)(entry.x >> 16);
+        const int q = (int)(entry.x & 0xFFFFu), kdir = (int)((entry.x >> 16) & 0xFFu);
         const int c = S::center(q);
         const uint32_t t = ws.tile[c];
-        const uint32_t s = ws.tile[c + S::nb_offset(kdir)];
+        const uint32_t s = (entry.x >> 24) ? 0u : ws.tile[c + S::nb_offset(kdir)];
         const uint32_t is = s & 0xFFFFFFu, it = t & 0xFFFFFFu;
         if (is > (uint32_t)ncells || it > (uint32_t)ncells) {
           atomicOr(err, kErrBadId);
@@ -419,13 +433,15 @@ __global__ void __launch_bounds__(kSweepThreadsMax, 1)
           const long long rs = cell_off + is, rt = cell_off + it;
           const unsigned long long aps = s ? __ldcg(pt.rap + rs) : 0ull;
           const unsigned long long apt = t ? __ldcg(pt.rap + rt) : 0ull;
-          // centroid sums, needed only on acceptance, fetched with the row
-          // so that an accepted attempt waits on one L2 round trip
+          // centroid sums, needed only on acceptance: in 2D fetched with the
+          // row so that an accepted attempt waits on one L2 round trip; in
+          // 3D (three words a side, fewer acceptances) on acceptance
+          constexpr bool kEarlyCs = NDIM == 2;
           long long cs_s[NDIM], cs_t[NDIM];
 #pragma unroll
           for (int k = 0; k < NDIM; ++k) {
-            cs_s[k] = s ? __ldcg(pt.rcs + rs * NDIM + k) : 0;
-            cs_t[k] = t ? __ldcg(pt.rcs + rt * NDIM + k) : 0;
+            cs_s[k] = kEarlyCs && s ? __ldcg(pt.rcs + rs * NDIM + k) : 0;
+            cs_t[k] = kEarlyCs && t ? __ldcg(pt.rcs + rt * NDIM + k) : 0;
           }
           float e_old = 0.0f, e_new = 0.0f;
           int cnt_s = 0, cnt_t = 0;
@@ -444,6 +460,18 @@ __global__ void __launch_bounds__(kSweepThreadsMax, 1)
               if (v != s) by_new += 1u << (8 * tn);
               if (v != t) by_old += 1u << (8 * tn);
             }
+          }
+          if (stick_on) {  // uniform over the tile (one replica)
+            // stickiness of the old configuration, summed in neighbour order
+            // and added to its adhesion as one term
+            float e_st = 0.0f;
+#pragma unroll
+            for (int k = 0; k < NB; ++k) {
+              const uint32_t v = ws.tile[c + S::nb_offset(k)];
+              const int tn = (int)(v >> 24) & (kMaxTypes - 1);
+              if (v != t) e_st = __fadd_rn(e_st, __ldg(&P->stick[tt * kMaxTypes + tn]));
+            }
+            e_old = __fadd_rn(e_old, e_st);
           }
           float dH = __fsub_rn(e_new, e_old);
           const int dps = NB - 2 * cnt_s;
@@ -539,14 +567,16 @@ __global__ void __launch_bounds__(kSweepThreadsMax, 1)
             if (s) {
 #pragma unroll
               for (int k = 0; k < NDIM; ++k)
-                img[k] = nearest_image(crd[k], dim[k], unpack_area(aps), cs_s[k]);
+                img[k] = nearest_image(crd[k], dim[k], unpack_area(aps),
+                                       kEarlyCs ? cs_s[k] : __ldcg(pt.rcs + rs * NDIM + k));
               add_delta<NDIM>(pt, rs, 1, dps, img, 1);
               push_s = rs;
             }
             if (t) {
 #pragma unroll
               for (int k = 0; k < NDIM; ++k)
-                img[k] = nearest_image(crd[k], dim[k], unpack_area(apt), cs_t[k]);
+                img[k] = nearest_image(crd[k], dim[k], unpack_area(apt),
+                                       kEarlyCs ? cs_t[k] : __ldcg(pt.rcs + rt * NDIM + k));
               add_delta<NDIM>(pt, rt, -1, dpt, img, -1);
               push_t = rt;
             }

@@ -218,6 +218,8 @@ extern "C" int cpm_sweep_static(int dimensionality, int nx, int ny, int nz,
   R.ncells = number_of_cells;
   R.lat_off = 0;
   R.cell_off = 0;
+  R.pset = 0;
+  R.pad = 0;
   DevParams P;
   std::memset(&P, 0, sizeof P);
   std::memcpy(P.J, params->J, sizeof P.J);
@@ -227,6 +229,11 @@ extern "C" int cpm_sweep_static(int dimensionality, int nx, int ny, int nz,
   std::memcpy(P.tgt_perim, params->target_perimeter, sizeof P.tgt_perim);
   P.temperature = params->temperature;
   P.perim_on = perim_on ? 1 : 0;
+  std::memcpy(P.stick, params->stickiness, sizeof P.stick);
+  for (int k = 0; k < kMaxTypes * kMaxTypes; ++k)
+    if (P.stick[k] != 0.0f) P.stick_on = 1;
+  for (int k = 0; k < kMaxTypes; ++k)
+    if (params->fixed[k]) P.fixed_mask |= 1u << k;
   STATIC_CUDA(cudaMemcpyAsync(rep, &R, sizeof R, cudaMemcpyHostToDevice, s));
   STATIC_CUDA(cudaMemcpyAsync(dparams, &P, sizeof P, cudaMemcpyHostToDevice, s));
   STATIC_CUDA(cudaMemcpyAsync(dprefix, prefix, sizeof prefix, cudaMemcpyHostToDevice, s));

@@ -18,10 +18,14 @@ Differences from the reference, all deliberate:
   * runs are reproducible: the random stream is keyed by a seed (default 0,
     see set_seed) instead of std::random_device (src/cpm.cu:347-350);
   * get_state's array keeps its Cpm alive (the reference's view dangles
-    once the object is freed).
-The act, chemotaxis, persistence, fixed and stickiness terms are not part of
-this engine: setting them raises CpmError, and get_act_state / get_field
-return zero arrays of the reference's shapes.
+    once the object is freed);
+  * stickiness accepts floats; fixed and stickiness apply whatever the
+    run() toggles (the reference applies fixed types only when
+    partial_dispatch is off or some type is fixed, src/cpm.cu:308-320,
+    which for a non-zero fixed flag is the same).
+The act, chemotaxis and persistence terms are not part of this engine:
+setting them raises CpmError, and get_act_state / get_field return zero
+arrays of the reference's shapes.
 """
 import ctypes
 import os
@@ -89,7 +93,9 @@ class StaticParams(ctypes.Structure):
                 ("target_area", ctypes.c_int * MAX_TYPES),
                 ("lambda_perimeter", ctypes.c_float * MAX_TYPES),
                 ("target_perimeter", ctypes.c_int * MAX_TYPES),
-                ("temperature", ctypes.c_float)]
+                ("temperature", ctypes.c_float),
+                ("stickiness", ctypes.c_float * (MAX_TYPES * MAX_TYPES)),
+                ("fixed", ctypes.c_int * MAX_TYPES)]
 
 
 _lib = None
@@ -125,6 +131,10 @@ def library():
         "cpm_set_adhesion": [H, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_int],
         "cpm_set_adhesion_r": [H, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                ctypes.c_float, ctypes.c_int],
+        "cpm_set_fixed": [H, ctypes.c_int, ctypes.c_int],
+        "cpm_set_fixed_r": [H, ctypes.c_int, ctypes.c_int, ctypes.c_int],
+        "cpm_set_stickiness": [H, ctypes.c_int, ctypes.c_int, ctypes.c_float],
+        "cpm_set_stickiness_r": [H, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float],
         "cpm_add_cell": [H, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int],
         "cpm_host_lattice": [H, ctypes.POINTER(ctypes.c_void_p),
                              ctypes.POINTER(ctypes.c_int64)],
@@ -360,12 +370,11 @@ class Cpm(_Engine):
         """Set per-type Hamiltonian parameters (src/python_wrapper.cpp:55-129).
 
         A group is applied only when all of its fields differ from -1, as in
-        the reference.  Groups of terms outside this engine raise CpmError.
+        the reference (fixed: any value >= 0).  Groups of terms outside this
+        engine raise CpmError.
         """
         ct = int(cell_type)
         unsupported = []
-        if fixed not in (-1, 0):
-            unsupported.append("fixed")
         if lambda_chemotaxis != -1:
             unsupported.append("lambda_chemotaxis")
         if (lambda_persistence != -1 and persistence_diffusion != -1
@@ -373,8 +382,6 @@ class Cpm(_Engine):
             unsupported.append("persistence")
         if lambda_act != -1 and max_act != -1:
             unsupported.append("act")
-        if other_cell_type != -1 and stickiness != -1:
-            unsupported.append("stickiness")
         if unsupported:
             raise CpmError(CPM_ERR_UNSUPPORTED,
                            "terms not modelled by this engine: " + ", ".join(unsupported))
@@ -382,9 +389,13 @@ class Cpm(_Engine):
             self._call("cpm_set_perimeter", ct, int(target_perimeter), float(lambda_perimeter))
         if lambda_area != -1 and target_area != -1:
             self._call("cpm_set_area", ct, int(target_area), float(lambda_area))
+        if fixed >= 0:
+            self._call("cpm_set_fixed", ct, int(fixed))
         if other_cell_type != -1 and adhesion != -1:
             self._call("cpm_set_adhesion", ct, int(other_cell_type), float(adhesion),
                        1 if set_adhesion_symmetric else 0)
+        if other_cell_type != -1 and stickiness != -1:
+            self._call("cpm_set_stickiness", ct, int(other_cell_type), float(stickiness))
 
     def set_temperature(self, temperature):
         self._call("cpm_set_temperature", float(temperature))
@@ -494,6 +505,19 @@ class Batch(_Engine):
         else:
             self._call("cpm_set_perimeter_r", int(replica), int(cell_type), int(target),
                        float(lam))
+
+    def set_fixed(self, replica, cell_type, fixed=True):
+        if replica is None:
+            self._call("cpm_set_fixed", int(cell_type), 1 if fixed else 0)
+        else:
+            self._call("cpm_set_fixed_r", int(replica), int(cell_type), 1 if fixed else 0)
+
+    def set_stickiness(self, replica, cell_type, other, S):
+        if replica is None:
+            self._call("cpm_set_stickiness", int(cell_type), int(other), float(S))
+        else:
+            self._call("cpm_set_stickiness_r", int(replica), int(cell_type), int(other),
+                       float(S))
 
     def set_adhesion(self, replica, cell_type, other, J, symmetric=True):
         if replica is None:

@@ -40,6 +40,8 @@ class Workload:
     temperature: float
     mcs: int
     meta: dict = field(default_factory=dict)
+    stick: np.ndarray = None     # float32 [ntypes, ntypes] stickiness, or None
+    fixed: np.ndarray = None     # bool [ntypes]: fixed (unmovable) types, or None
 
     @property
     def ndim(self):
@@ -69,11 +71,23 @@ class Workload:
             engine.set_temperature(self.temperature)
         else:
             engine.set_temperature(replica, self.temperature)
+        for a in range(nt):
+            if self.fixed is not None and self.fixed[a]:
+                if replica is None:
+                    engine._call("cpm_set_fixed", a, 1)
+                else:
+                    engine.set_fixed(replica, a, True)
+            for b in range(nt):
+                if self.stick is not None and self.stick[a, b] != 0:
+                    if replica is None:
+                        engine._call("cpm_set_stickiness", a, b, float(self.stick[a, b]))
+                    else:
+                        engine.set_stickiness(replica, a, b, float(self.stick[a, b]))
 
     def oracle_kwargs(self):
         return dict(J=self.J, lam_area=self.lam_area, tgt_area=self.tgt_area,
                     lam_perim=self.lam_perim, tgt_perim=self.tgt_perim,
-                    temperature=self.temperature)
+                    temperature=self.temperature, stick=self.stick, fixed=self.fixed)
 
 
 def _params(nt, J, lam_area=0.0, tgt_area=0, lam_perim=0.0, tgt_perim=0):

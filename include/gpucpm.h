@@ -110,6 +110,21 @@ int cpm_set_adhesion(cpm_handle* h, int type, int other, float J,
 int cpm_set_adhesion_r(cpm_handle* h, int replica, int type, int other,
                        float J, int symmetric);
 
+/* Replaces Cpm::setFixed (src/cpm.cu:150-153).  Cells of a fixed type never
+ * move: an attempt whose target belongs to one does nothing, and one whose
+ * source belongs to one proposes the medium instead (src/kernels2d.cu:
+ * 280-290, src/kernels3d.cu:251-261).  fixed != 0 sets, 0 clears. */
+int cpm_set_fixed(cpm_handle* h, int type, int fixed);
+int cpm_set_fixed_r(cpm_handle* h, int replica, int type, int fixed);
+
+/* Replaces Cpm::setStickiness (src/cpm.cu:145-148): S[type][other], added
+ * to the adhesion energy of the configuration before the copy only
+ * (src/kernels2d.cu:399-400).  Not symmetric, as in the reference.  float
+ * here (the reference stores short, src/settings.h:22). */
+int cpm_set_stickiness(cpm_handle* h, int type, int other, float S);
+int cpm_set_stickiness_r(cpm_handle* h, int replica, int type, int other,
+                         float S);
+
 /* ---- lattice ---------------------------------------------------------- */
 
 /* Replaces Cpm::addCell (src/cpm.cu:160-174): the next id (1, 2, ...) of
@@ -304,6 +319,8 @@ typedef struct {
     float lambda_perimeter[CPM_MAX_TYPES];
     int target_perimeter[CPM_MAX_TYPES];
     float temperature;
+    float stickiness[CPM_MAX_TYPES * CPM_MAX_TYPES]; /* as cpm_set_stickiness */
+    int fixed[CPM_MAX_TYPES];                        /* as cpm_set_fixed */
 } cpm_static_params;
 
 /* No counterpart in the reference.  Runs `mcs` Monte Carlo steps of the same

@@ -27,6 +27,8 @@ class Params(ctypes.Structure):
         ("temperature", ctypes.c_float),
         ("seed", ctypes.c_uint64),
         ("stream", ctypes.c_uint32),
+        ("stick", ctypes.c_float * (MAX_TYPES * MAX_TYPES)),
+        ("fixed_mask", ctypes.c_uint32),
     ]
 
 
@@ -91,12 +93,14 @@ class OracleSim:
 
     `lattice` is a uint32 array of shape (ny, nx) or (nz, ny, nx) holding
     id | type << 24.  Parameters follow the engine's conventions: J[a][b] is
-    the adhesion seen by a site of type a next to a site of type b.
+    the adhesion seen by a site of type a next to a site of type b; stick
+    (optional, [a][b]) the stickiness, fixed (optional, per type) the
+    unmovable types.
     """
 
     def __init__(self, lattice, ncells, J, lam_area, tgt_area,
                  lam_perim=None, tgt_perim=None, temperature=1.0, seed=0,
-                 stream=0):
+                 stream=0, stick=None, fixed=None):
         lat = np.ascontiguousarray(lattice, dtype=np.uint32).copy()
         self.ndim = lat.ndim
         self.lattice = lat
@@ -126,6 +130,16 @@ class OracleSim:
         p.temperature = float(temperature)
         p.seed = int(seed)
         p.stream = int(stream)
+        Sm = np.zeros((MAX_TYPES, MAX_TYPES), np.float32)
+        if stick is not None:
+            Sin = np.asarray(stick, np.float32)
+            Sm[:Sin.shape[0], :Sin.shape[1]] = Sin
+        p.stick[:] = Sm.ravel().tolist()
+        mask = 0
+        for t, f in enumerate(np.zeros(0) if fixed is None else np.asarray(fixed).ravel()):
+            if f:
+                mask |= 1 << t
+        p.fixed_mask = mask
         self.params = p
         n1 = self.ncells + 1
         self.area = np.zeros(n1, np.int32)

@@ -16,6 +16,10 @@
 //     uniformly random Moore neighbour as source, as in the shared-memory
 //     branch :212-226), 3D src/kernels3d.cu:203-243
 //   * early out when source id == target id: src/kernels2d.cu:276
+//   * fixed types (target fixed: no change; source fixed: the medium is
+//     proposed instead): src/kernels2d.cu:280-290, src/kernels3d.cu:251-261
+//   * stickiness added to the old configuration's adhesion:
+//     src/kernels2d.cu:399-400, src/kernels3d.cu:413-414
 //   * adhesion, perimeter, area dH:  src/kernels2d.cu:346-519,
 //     src/kernels3d.cu:368-541 (same term order: adhesion, perimeter source,
 //     perimeter target, area source, area target)
@@ -67,6 +71,11 @@ struct Params {
   float temperature;
   uint64_t seed;
   uint32_t stream;
+  // stickiness S[own][neighbour], added to the old configuration's
+  // adhesion (src/kernels2d.cu:399-400); fixed types (bit t), which never
+  // move (src/kernels2d.cu:280-290)
+  float stick[kMaxTypes * kMaxTypes];
+  uint32_t fixed_mask;
 };
 
 // ---- Philox4x32-10 --------------------------------------------------------
@@ -200,7 +209,7 @@ void add_score(const ScoreSpec& sp, const uint32_t* nb, int N, uint32_t s, uint3
 // evaluated and rejected attempt, 2 for an accepted one (lattice written,
 // *acc filled).  With `sp`, adds the attempt's score to sc[8].
 inline int attempt(const Params& p, uint32_t* lat, const Tables& tb, int x,
-                   int y, int z, uint64_t phase, bool perim_on,
+                   int y, int z, uint64_t phase, bool perim_on, bool stick_on,
                    Accepted* acc, const ScoreSpec* sp = nullptr,
                    double* sc = nullptr) {
   const int nx = p.nx, ny = p.ny, nz = p.nz;
@@ -226,8 +235,15 @@ inline int attempt(const Params& p, uint32_t* lat, const Tables& tb, int x,
                    (uint32_t)(phase >> 32)};
   philox4x32_10(r, (uint32_t)p.seed, (uint32_t)(p.seed >> 32));
   const int kdir = (int)(((uint64_t)r[0] * (uint64_t)N) >> 32);
-  const uint32_t s = nb[kdir];
+  uint32_t s = nb[kdir];
   if (s == t) return 0;
+  // a target of a fixed type never changes; a source of a fixed type
+  // proposes the medium instead
+  if ((p.fixed_mask >> ((t >> 24) & (kMaxTypes - 1))) & 1u) return 0;
+  if ((p.fixed_mask >> ((s >> 24) & (kMaxTypes - 1))) & 1u) {
+    s = 0;
+    if (s == t) return 0;
+  }
 
   const int ts = (int)(s >> 24), tt = (int)(t >> 24);
   float e_old = 0.0f, e_new = 0.0f;
@@ -238,6 +254,12 @@ inline int attempt(const Params& p, uint32_t* lat, const Tables& tb, int x,
     if (nb[k] != s) e_new = e_new + p.J[ts * kMaxTypes + tn];
     cnt_s += nb[k] == s;
     cnt_t += nb[k] == t;
+  }
+  if (stick_on) {  // the old configuration's stickiness, as one term
+    float e_st = 0.0f;
+    for (int k = 0; k < N; ++k)
+      if (nb[k] != t) e_st = e_st + p.stick[tt * kMaxTypes + (int)(nb[k] >> 24)];
+    e_old = e_old + e_st;
   }
   float dH = e_new - e_old;
   const int dps = N - 2 * cnt_s;  // source cell gains the target site
@@ -392,6 +414,8 @@ int run_impl(const orc_params* pp, uint32_t* lat, int32_t* area, int32_t* perim,
   const int nx = p.nx, ny = p.ny, nz = p.ndim == 3 ? p.nz : 1;
   const int nslots = p.ndim == 2 ? 9 : 27;
   const bool perim_on = perimeter_enabled(p);
+  bool stick_on = false;
+  for (int k = 0; k < kMaxTypes * kMaxTypes; ++k) stick_on = stick_on || p.stick[k] != 0.0f;
   Tables tb{area, perim, csum};
   if (nthreads <= 0) nthreads = omp_get_max_threads();
   std::vector<std::vector<Accepted>> logs(nthreads);
@@ -422,7 +446,7 @@ int run_impl(const orc_params* pp, uint32_t* lat, int32_t* area, int32_t* perim,
               for (int i = 0; i < ncx; ++i) {
                 const int x = class_coord(nx, cx, i);
                 Accepted acc;
-                const int res = attempt(p, lat, tb, x, y, z, phase, perim_on,
+                const int res = attempt(p, lat, tb, x, y, z, phase, perim_on, stick_on,
                                         &acc, sp, sc);
                 if (res >= 1) ++e;
                 if (res == 2) {

@@ -33,8 +33,10 @@ def lib():
         L.ref_set_perimeter.argtypes = [i, i, d]
         L.ref_set_adhesion.argtypes = [i, i, i]
         L.ref_set_temperature.argtypes = [i]
+        L.ref_set_stickiness.argtypes = [i, i, i]
+        L.ref_set_fixed.argtypes = [i, i]
         L.ref_push.argtypes = [ctypes.c_void_p]
-        L.ref_run.argtypes = [i] * 14
+        L.ref_run.argtypes = [i] * 15
         L.ref_pull.argtypes = [ctypes.c_void_p]
         L.ref_tables.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.ref_max_coop_blocks.argtypes = [i, i, i, ctypes.POINTER(i)]
@@ -55,6 +57,7 @@ class RefGpu:
                             int(round(temperature))))
         self.dimension, self.ndim, self.ncells = int(dimension), int(dimensionality), int(ncells)
         self.perimeter = False
+        self.fixed = False
 
     def set_area(self, t, target, lam):
         _check(lib().ref_set_area(int(t), int(target), float(lam)))
@@ -65,6 +68,13 @@ class RefGpu:
 
     def set_adhesion(self, a, b, J):
         _check(lib().ref_set_adhesion(int(a), int(b), int(round(J))))
+
+    def set_stickiness(self, a, b, S):
+        _check(lib().ref_set_stickiness(int(a), int(b), int(round(S))))
+
+    def set_fixed(self, t, fixed=True):
+        _check(lib().ref_set_fixed(int(t), 1 if fixed else 0))
+        self.fixed = self.fixed or bool(fixed)
 
     def apply(self, w):
         """Parameters of a gpucpm.workloads.Workload, rounded as the
@@ -77,6 +87,11 @@ class RefGpu:
                 self.set_area(a, int(w.tgt_area[a]), float(w.lam_area[a]))
             if w.lam_perim[a] != 0:
                 self.set_perimeter(a, int(w.tgt_perim[a]), float(w.lam_perim[a]))
+            if w.fixed is not None and w.fixed[a]:
+                self.set_fixed(a)
+            for b in range(nt):
+                if w.stick is not None and w.stick[a, b] != 0:
+                    self.set_stickiness(a, b, w.stick[a, b])
         _check(lib().ref_set_temperature(int(round(w.temperature))))
 
     def push(self, lattice):
@@ -92,7 +107,8 @@ class RefGpu:
                              positions_per_thread, positions_per_checkerboard,
                              updates_per_checkerboard_switch, updates_per_barrier,
                              int(iterations), int(inner), int(shared),
-                             1 if self.perimeter else 0, int(centroid_tracking), int(seed)))
+                             1 if self.perimeter else 0, int(centroid_tracking), int(seed),
+                             1 if self.fixed else 0))
 
     def synchronize(self):
         _check(lib().ref_synchronize())

@@ -172,6 +172,14 @@ int ref_set_adhesion(int type, int other, int J) {
   g.settings.types[other].adhesion[type] = (short)J;
   return upload_settings();
 }
+int ref_set_stickiness(int type, int other, int S) {  // Cpm::setStickiness, src/cpm.cu:145-148
+  g.settings.types[type].stickiness[other] = (short)S;
+  return upload_settings();
+}
+int ref_set_fixed(int type, int fixed) {  // Cpm::setFixed, src/cpm.cu:150-153
+  g.settings.types[type].fixed = fixed;
+  return upload_settings();
+}
 int ref_set_temperature(int T) {
   g.settings.temperature = T;
   return upload_settings();
@@ -200,16 +208,18 @@ int ref_push(const uint32_t* lattice) {
   return 0;
 }
 
-// Cpm::run (src/cpm.cu:291-517), cooperative path.  `perimeter` selects the
-// perimeter-toggle variant as partial_dispatch=1 would (any lambda != 0);
-// act, persistence, chemotaxis and fixed toggles are off.
+// Cpm::run (src/cpm.cu:291-517), cooperative path.  `perimeter` and `fixed`
+// select the toggle variants as partial_dispatch=1 would (any perimeter
+// lambda != 0, any fixed type, src/cpm.cu:308-320); act, persistence and
+// chemotaxis toggles are off.
 int ref_run(int cell_sync, int block_sync, int global_sync, int threads_per_block,
             int positions_per_thread, int positions_per_checkerboard,
             int updates_per_checkerboard_switch, int updates_per_barrier, int iterations,
             int inner_iterations, int shared, int perimeter, int centroid_tracking,
-            int seed) {
+            int seed, int fixed) {
   DRV(cuCtxSetCurrent(g.ctx));
-  int toggles[7] = {shared ? 1 : 0, 0, perimeter ? 1 : 0, 0, 0, 0, centroid_tracking ? 1 : 0};
+  int toggles[7] = {shared ? 1 : 0, 0, perimeter ? 1 : 0, 0, 0, fixed ? 1 : 0,
+                    centroid_tracking ? 1 : 0};
   CUfunction f;
   const std::string name = kernel_name(g.ndim, toggles);
   DRV(cuModuleGetFunction(&f, g.mod, name.c_str()));

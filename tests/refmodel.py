@@ -27,11 +27,14 @@ def next_random(seed):
 
 
 def reference_dh(lat, ax, ay, sx, sy, area, perim, J, lam_a, tgt_a, lam_p, tgt_p,
-                 perimeter_on=True):
+                 perimeter_on=True, stick=None, s=None):
     """dH of copying (sx, sy) into (ax, ay) as src/kernels2d.cu:346-519
-    computes it: integer adhesion sums, double lambda terms."""
+    computes it: integer adhesion sums (stickiness added to the old
+    configuration's, :399-400), double lambda terms.  `s` overrides the
+    source value (the medium that a fixed source type proposes)."""
     n = lat.shape[0]
-    s, t = int(lat[sy, sx]), int(lat[ay, ax])
+    t = int(lat[ay, ax])
+    s = int(lat[sy, sx]) if s is None else s
     ts, tt = s >> 24, t >> 24
     e_old = e_new = 0
     ops = nps = opt = npt = 0
@@ -42,7 +45,7 @@ def reference_dh(lat, ax, ay, sx, sy, area, perim, J, lam_a, tgt_a, lam_p, tgt_p
             v = int(lat[(ay + j) % n, (ax + i) % n])
             tv = v >> 24
             if t != v:
-                e_old += J[tt][tv]
+                e_old += J[tt][tv] + (int(stick[tt][tv]) if stick is not None else 0)
             if s != v:
                 e_new += J[ts][tv]
             ops += v == s
@@ -67,8 +70,12 @@ def reference_dh(lat, ax, ay, sx, sy, area, perim, J, lam_a, tgt_a, lam_p, tgt_p
 
 
 def sequential_run(lat, area, perim, J, lam_a, tgt_a, lam_p, tgt_p, T, seed, mcs,
-                   perimeter_on=True):
-    """The reference's one-thread run (in place); returns the accept count."""
+                   perimeter_on=True, stick=None, fixed=None):
+    """The reference's one-thread run (in place); returns the accept count.
+    fixed (per type): the checks of src/kernels2d.cu:280-290, after the
+    id comparison; a fixed source becomes the medium and is still evaluated
+    (and accepted, as a no-op, when the target is the medium too)."""
+
     D = lat.shape[0]
     seed = next_random(0 + seed)  # calculateIndex(0, 0) + seed
     accepted = 0
@@ -88,8 +95,13 @@ def sequential_run(lat, area, perim, J, lam_a, tgt_a, lam_p, tgt_p, T, seed, mcs
             s, t = int(lat[y, x]), int(lat[ny, nx])
             if s == t:
                 continue
+            if fixed is not None:
+                if fixed[t >> 24]:
+                    continue
+                if fixed[s >> 24]:
+                    s = 0
             dH, dps, dpt = reference_dh(lat, nx, ny, x, y, area, perim, J, lam_a, tgt_a,
-                                        lam_p, tgt_p, perimeter_on)
+                                        lam_p, tgt_p, perimeter_on, stick, s)
             e = np.float32(dH)
             seed = next_random(seed)
             r = np.float32(seed / M)

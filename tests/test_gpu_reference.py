@@ -66,19 +66,30 @@ def test_table_recount_matches_reference(engine_lib, case):
     np.testing.assert_array_equal(perim, rp.astype(np.int32))
 
 
-@pytest.mark.parametrize("D,perimeter,seed", [(16, False, 12345), (16, True, 777),
-                                              (32, True, 31337)])
-def test_one_thread_reference_run_equals_restatement(engine_lib, D, perimeter, seed):
-    w = W.random_small((D, D), D * D // 20, seed=D + seed % 97, temperature=6.0,
+@pytest.mark.parametrize("D,perimeter,seed,terms", [(16, False, 12345, False),
+                                                    (16, True, 777, False),
+                                                    (32, True, 31337, False),
+                                                    (32, True, 4242, True)])
+def test_one_thread_reference_run_equals_restatement(engine_lib, D, perimeter, seed, terms):
+    """`terms`: with stickiness and a fixed type (src/kernels2d.cu:280-290,
+    399-400), which the reference applies in its fixed-toggle variant."""
+    nt = 3 if terms else 2
+    w = W.random_small((D, D), D * D // 20, ntypes=nt, seed=D + seed % 97, temperature=6.0,
                        perim=perimeter)
     J = np.rint(w.J).astype(int)
-    lam_a = [0.0, 1.0, 1.0]
-    tgt_a = [0, 20, 20]
-    lam_p = [0.0, 0.5, 0.5] if perimeter else [0.0, 0.0, 0.0]
-    tgt_p = [0, 18, 18]
+    lam_a = [0.0] + [1.0] * nt
+    tgt_a = [0] + [20] * nt
+    lam_p = ([0.0] + [0.5] * nt) if perimeter else [0.0] * (nt + 1)
+    tgt_p = [0] + [18] * nt
+    stick = fixed = None
+    if terms:
+        stick = np.zeros((nt + 1, nt + 1), np.float32)
+        stick[1, 2], stick[2, 1], stick[1, 0], stick[0, 2] = 3, 2, 4, 1
+        fixed = np.array([False, False, False, True])
     wi = W.Workload("one_thread", w.lattice, w.ncells, J.astype(np.float32),
                     np.array(lam_a, np.float32), np.array(tgt_a, np.int32),
-                    np.array(lam_p, np.float32), np.array(tgt_p, np.int32), 6.0, 0)
+                    np.array(lam_p, np.float32), np.array(tgt_p, np.int32), 6.0, 0,
+                    stick=stick, fixed=fixed)
     ref = _ref(wi)
     a0, p0 = ref.tables()
     mcs = 3
@@ -91,7 +102,7 @@ def test_one_thread_reference_run_equals_restatement(engine_lib, D, perimeter, s
     lat = w.lattice.copy()
     area, perim = a0.astype(np.int64), p0.astype(np.int64)
     acc = refmodel.sequential_run(lat, area, perim, J, lam_a, tgt_a, lam_p, tgt_p, 6.0,
-                                  seed, mcs, perimeter_on=perimeter)
+                                  seed, mcs, perimeter_on=perimeter, stick=stick, fixed=fixed)
     assert acc > 10
     np.testing.assert_array_equal(got, lat)
     np.testing.assert_array_equal(ra.astype(np.int64), area)

@@ -1,0 +1,130 @@
+"""Fixed cell types and stickiness (src/kernels2d.cu:280-290, 399-400;
+src/kernels3d.cu:251-261, 413-414), and per-replica parameter records.
+
+Bit-exact against the CPU oracle: a fixed target never changes, a fixed
+source proposes the medium, stickiness is added to the old configuration's
+adhesion only.  Batches whose replicas start from one shared parameter record
+and then diverge (copy on write) must still follow each replica's own
+parameters."""
+import numpy as np
+import pytest
+
+import oracle
+from gpucpm import workloads as W
+from test_gpu_parity import assert_same, finish, make_engine
+
+pytestmark = pytest.mark.gpu
+
+
+def _with_terms(w, fixed_type, sticky, seed):
+    nt = w.J.shape[0]
+    g = np.random.default_rng(seed)
+    w.stick = np.zeros((nt, nt), np.float32)
+    for a, b in sticky:
+        w.stick[a, b] = float(g.integers(1, 8))
+    w.fixed = np.zeros(nt, bool)
+    if fixed_type is not None:
+        w.fixed[fixed_type] = True
+    return w
+
+
+@pytest.mark.parametrize("shape,ncells,T,mcs", [((64, 60), 40, 8.0, 20),
+                                                 ((35, 33), 25, 5.0, 25),
+                                                 ((14, 15, 13), 20, 8.0, 5)])
+def test_fixed_and_sticky_match_oracle(engine_lib, shape, ncells, T, mcs):
+    w = W.random_small(shape, ncells, ntypes=3, seed=90 + len(shape), temperature=T)
+    _with_terms(w, 3, [(1, 2), (2, 1), (1, 0), (2, 3), (3, 1)], seed=4)
+    lat0 = w.lattice.copy()
+    e = make_engine(w, seed=12)
+    e.run_mcs(mcs)
+    finish(e)
+    sim = oracle.OracleSim(w.lattice, w.ncells, **w.oracle_kwargs(), seed=12).run(mcs)
+    assert_same(e, sim)
+    # the fixed type's sites are exactly where they were
+    fixed_sites = (lat0 >> 24) == 3
+    assert fixed_sites.any()
+    np.testing.assert_array_equal(e.lattice(0).view(np.uint32)[fixed_sites], lat0[fixed_sites])
+    assert int(sim.counters[2]) > 0
+
+
+def test_replica_parameters_copy_on_write(engine_lib):
+    """All replicas share one record until single replicas change; each must
+    follow its own parameters under both dispatches."""
+    import gpucpm
+    base = [W.random_small((48, 40), 30, ntypes=3, seed=200 + i, temperature=7.0)
+            for i in range(4)]
+    for d in (gpucpm.DISPATCH_GRID, gpucpm.DISPATCH_REPLICA):
+        b = gpucpm.Batch(2, [w.lattice.shape[::-1] for w in base], [w.ncells for w in base])
+        for r, w in enumerate(base):
+            b.lattice(r)[...] = w.lattice.view(np.int32)
+        w0 = base[0]
+        nt = w0.J.shape[0]
+        # shared settings for every replica
+        for a in range(nt):
+            for c in range(nt):
+                b.set_adhesion(None, a, c, float(w0.J[a, c]), symmetric=False)
+            b.set_area(None, a, int(w0.tgt_area[a]), float(w0.lam_area[a]))
+            b.set_perimeter(None, a, int(w0.tgt_perim[a]), float(w0.lam_perim[a]))
+        b.set_temperature(None, 7.0)
+        # then per-replica changes
+        b.set_fixed(1, 3, True)
+        b.set_stickiness(2, 1, 2, 4.0)
+        b.set_temperature(3, 11.0)
+        b.set_stickiness(None, 2, 1, 1.0)  # all replicas again
+        b.set_seed(5, 50)
+        b.set_dispatch(d)
+        b.push_to_gpu()
+        b.run_mcs(12)
+        b.synchronize()
+        b.pull_from_gpu()
+        for r, w in enumerate(base):
+            stick = np.zeros((nt, nt), np.float32)
+            stick[2, 1] = 1.0
+            fixed = np.zeros(nt, bool)
+            T = 7.0
+            if r == 1:
+                fixed[3] = True
+            if r == 2:
+                stick[1, 2] = 4.0
+            if r == 3:
+                T = 11.0
+            sim = oracle.OracleSim(w.lattice, w.ncells, w0.J, w0.lam_area, w0.tgt_area,
+                                   w0.lam_perim, w0.tgt_perim, temperature=T, seed=5,
+                                   stream=50 + r, stick=stick, fixed=fixed).run(12)
+            np.testing.assert_array_equal(b.lattice(r).view(np.uint32), sim.lattice)
+            area, perim, cs = b.tables(r)
+            np.testing.assert_array_equal(area, sim.area)
+            np.testing.assert_array_equal(cs, sim.csum)
+
+
+def test_set_constraints_fixed_and_stickiness(engine_lib):
+    """The reference's keywords reach the engine (src/python_wrapper.cpp:89-91,
+    122-125): fixed takes effect on its own, stickiness with other_cell_type."""
+    import gpucpm
+    sim = gpucpm.Cpm(64, 2, 12, 10, False)
+    for k in range(12):
+        sim.add_cell(1 + k % 3, 5 + 5 * k, 10 + 4 * (k % 5))
+    sim.set_constraints(cell_type=1, lambda_area=2, target_area=60)
+    sim.set_constraints(cell_type=2, lambda_area=2, target_area=60)
+    sim.set_constraints(cell_type=3, fixed=1)
+    sim.set_constraints(cell_type=0, other_cell_type=1, adhesion=12)
+    sim.set_constraints(cell_type=0, other_cell_type=2, adhesion=8)
+    sim.set_constraints(cell_type=1, other_cell_type=2, adhesion=6)
+    sim.set_constraints(cell_type=1, other_cell_type=0, stickiness=3)
+    lat0 = sim.get_state().view(np.uint32).copy()
+    sim.push_to_gpu()
+    sim.run(cell_sync=0, block_sync=0, global_sync=1, threads_per_block=4,
+            positions_per_thread=8, positions_per_checkerboard=4,
+            updates_per_checkerboard_switch=1, updates_per_barrier=1,
+            iterations=100, inner_iterations=100)
+    sim.synchronize()
+    sim.pull_from_gpu()
+    J = np.zeros((4, 4), np.float32)
+    J[0, 1] = J[1, 0] = 12
+    J[0, 2] = J[2, 0] = 8
+    J[1, 2] = J[2, 1] = 6
+    S = np.zeros((4, 4), np.float32)
+    S[1, 0] = 3
+    ref = oracle.OracleSim(lat0, 12, J, [0, 2, 2, 0], [0, 60, 60, 0], temperature=10.0,
+                           stick=S, fixed=[False, False, False, True]).run(100)
+    np.testing.assert_array_equal(sim.get_state().view(np.uint32), ref.lattice)

@@ -86,11 +86,15 @@ def test_invalid_lattices_rejected():
         _sim(lat, 3)  # one id, two types
 
 
-def _reference_dh(lat, ax, ay, sx, sy, area, perim, J, lam_a, tgt_a, lam_p, tgt_p):
+def _reference_dh(lat, ax, ay, sx, sy, area, perim, J, lam_a, tgt_a, lam_p, tgt_p,
+                  stick=None, s=None):
     """dH of copying (sx, sy) into (ax, ay), restated from the reference
-    (src/kernels2d.cu:346-519): integer adhesion sums, double lambda terms."""
+    (src/kernels2d.cu:346-519): integer adhesion sums (stickiness added to
+    the old configuration's, :399-400), double lambda terms.  `s` overrides
+    the source value (the medium proposed by a fixed source type)."""
     n = lat.shape[0]
-    s, t = int(lat[sy, sx]), int(lat[ay, ax])
+    t = int(lat[ay, ax])
+    s = int(lat[sy, sx]) if s is None else s
     ts, tt = s >> 24, t >> 24
     e_old = e_new = 0
     ops = nps = opt = npt = 0
@@ -101,7 +105,7 @@ def _reference_dh(lat, ax, ay, sx, sy, area, perim, J, lam_a, tgt_a, lam_p, tgt_
             v = int(lat[(ay + j) % n, (ax + i) % n])
             tv = v >> 24
             if t != v:
-                e_old += J[tt][tv]
+                e_old += J[tt][tv] + (stick[tt][tv] if stick is not None else 0)
             if s != v:
                 e_new += J[ts][tv]
             ops += v == s
@@ -124,17 +128,24 @@ def _reference_dh(lat, ax, ay, sx, sy, area, perim, J, lam_a, tgt_a, lam_p, tgt_
     return e
 
 
-def test_first_mcs_matches_reference_dh_formula():
+@pytest.mark.parametrize("case", ["plain", "fixed_sticky"])
+def test_first_mcs_matches_reference_dh_formula(case):
     """Replay one MCS in Python with the reference's dH formula and the same
-    Philox draws, and compare the result with the oracle."""
-    w = W.random_small((16, 16), 10, seed=11, temperature=6.0)
+    Philox draws, and compare the result with the oracle.  The second case
+    adds stickiness and a fixed type (src/kernels2d.cu:280-290, 399-400)."""
+    w = W.random_small((16, 16), 10, ntypes=3, seed=11, temperature=6.0)
     J = np.rint(w.J).astype(int)            # integer J: both sides exact
-    lam_a = [1.0] * 3
-    lam_p = [0.5] * 3
-    tgt_a, tgt_p = [0, 20, 20], [0, 18, 18]
+    lam_a = [1.0] * 4
+    lam_p = [0.5] * 4
+    tgt_a, tgt_p = [0, 20, 20, 20], [0, 18, 18, 18]
     T = 6.0
+    stick = fixed = None
+    if case == "fixed_sticky":
+        stick = np.zeros((4, 4), int)
+        stick[1, 2], stick[2, 1], stick[1, 0], stick[2, 3] = 3, 5, 2, 4
+        fixed = [False, False, False, True]
     sim = oracle.OracleSim(w.lattice, w.ncells, J.astype(np.float32), lam_a, tgt_a,
-                           lam_p, tgt_p, temperature=T, seed=7)
+                           lam_p, tgt_p, temperature=T, seed=7, stick=stick, fixed=fixed)
     lat = w.lattice.copy()
     area, perim = sim.area.copy(), sim.perim.copy()
     n = 16
@@ -155,12 +166,20 @@ def test_first_mcs_matches_reference_dh_formula():
                     k = (r[0] * 8) >> 32
                     if vals[k] == t:
                         continue
+                    s = vals[k]
+                    if fixed is not None:
+                        if fixed[t >> 24]:
+                            continue
+                        if fixed[s >> 24]:
+                            s = 0
+                            if s == t:
+                                continue
                     sx, sy = nbs[k][0] % n, nbs[k][1] % n
                     dH = _reference_dh(lat, x, y, sx, sy, area, perim, J, lam_a,
-                                       tgt_a, lam_p, tgt_p)
+                                       tgt_a, lam_p, tgt_p, stick, s)
                     u = ((r[1] >> 8) | 1) * 2.0 ** -24
                     if dH < 0 or u < math.exp(-dH / T):
-                        changes.append((x, y, vals[k], t, vals))
+                        changes.append((x, y, s, t, vals))
             for x, y, s, t, vals in changes:
                 lat[y, x] = s
                 accepted += 1
