@@ -708,11 +708,10 @@ int cpm_device_lattice_r(cpm_handle* h, int r, uint32_t** dptr) {
   return CPM_OK;
 }
 
-int cpm_push(cpm_handle* h) {
-  CPM_BIND(h);
+namespace {
+// Tables of every replica recomputed from the device lattice.
+int recount_tables(cpm_handle* h) {
   h->pushed = false;
-  CPM_CUDA(h, cudaMemcpyAsync(h->d_lat, h->h_lat, sizeof(uint32_t) * h->total_sites,
-                              cudaMemcpyHostToDevice, h->stream));
   for (int b = 0; b < 2; ++b) {
     CPM_CUDA(h, cudaMemsetAsync(h->d_ap[b], 0, sizeof(unsigned long long) * h->rows, h->stream));
     CPM_CUDA(h, cudaMemsetAsync(h->d_cs[b], 0, sizeof(long long) * h->rows * h->ndim, h->stream));
@@ -735,10 +734,109 @@ int cpm_push(cpm_handle* h) {
   if (int rc = read_error_word(h, &w)) return rc;
   if (w) {
     CPM_CUDA(h, cudaMemsetAsync(h->d_ctl, 0, sizeof(uint32_t) * kCtlWords, h->stream));
-    return h->fail(CPM_ERR_INVALID, "push_to_gpu rejected the lattice: %s",
+    return h->fail(CPM_ERR_INVALID, "the lattice was rejected: %s",
                    describe_errors(w).c_str());
   }
   h->pushed = true;
+  return CPM_OK;
+}
+}  // namespace
+
+int cpm_push(cpm_handle* h) {
+  CPM_BIND(h);
+  h->pushed = false;
+  CPM_CUDA(h, cudaMemcpyAsync(h->d_lat, h->h_lat, sizeof(uint32_t) * h->total_sites,
+                              cudaMemcpyHostToDevice, h->stream));
+  return recount_tables(h);
+}
+
+int cpm_recount(cpm_handle* h) {
+  CPM_BIND(h);
+  return recount_tables(h);
+}
+
+int cpm_set_centroid_sums_r(cpm_handle* h, int r, const int64_t* centroid_sums) {
+  if (int rc = check_replica(h, r)) return rc;
+  CPM_BIND(h);
+  if (!centroid_sums) return h->fail(CPM_ERR_INVALID, "centroid_sums is NULL");
+  if (!h->pushed) return h->fail(CPM_ERR_STATE, "set centroid sums after a successful push");
+  const DevReplica& R = h->reps[r];
+  const size_t bytes = sizeof(long long) * ((size_t)R.ncells + 1) * h->ndim;
+  for (int b = 0; b < 2; ++b)
+    CPM_CUDA(h, cudaMemcpyAsync(h->d_cs[b] + R.cell_off * h->ndim, centroid_sums, bytes,
+                                cudaMemcpyHostToDevice, h->stream));
+  CPM_CUDA(h, cudaStreamSynchronize(h->stream));  // the caller's buffer may go
+  return CPM_OK;
+}
+
+int cpm_get_params_r(const cpm_handle* h, int r, cpm_static_params* out) {
+  if (!h || !out || r < 0 || r >= h->nrep) return CPM_ERR_INVALID;
+  const DevParams& p = h->psets[h->reps[r].pset];
+  std::memcpy(out->J, p.J, sizeof out->J);
+  std::memcpy(out->lambda_area, p.lam_area, sizeof out->lambda_area);
+  std::memcpy(out->target_area, p.tgt_area, sizeof out->target_area);
+  std::memcpy(out->lambda_perimeter, p.lam_perim, sizeof out->lambda_perimeter);
+  std::memcpy(out->target_perimeter, p.tgt_perim, sizeof out->target_perimeter);
+  out->temperature = p.temperature;
+  std::memcpy(out->stickiness, p.stick, sizeof out->stickiness);
+  for (int k = 0; k < kMaxTypes; ++k) out->fixed[k] = (p.fixed_mask >> k) & 1u;
+  return CPM_OK;
+}
+
+namespace {
+int set_params(cpm_handle* h, int r, const cpm_static_params* in) {
+  if (!h) return CPM_ERR_INVALID;
+  if (!in) return h->fail(CPM_ERR_INVALID, "params is NULL");
+  if (!std::isfinite(in->temperature))
+    return h->fail(CPM_ERR_INVALID, "temperature must be finite");
+  auto fill = [&](DevParams& p) {
+    std::memcpy(p.J, in->J, sizeof p.J);
+    std::memcpy(p.lam_area, in->lambda_area, sizeof p.lam_area);
+    std::memcpy(p.tgt_area, in->target_area, sizeof p.tgt_area);
+    std::memcpy(p.lam_perim, in->lambda_perimeter, sizeof p.lam_perim);
+    std::memcpy(p.tgt_perim, in->target_perimeter, sizeof p.tgt_perim);
+    p.temperature = in->temperature;
+    std::memcpy(p.stick, in->stickiness, sizeof p.stick);
+    p.fixed_mask = 0;
+    for (int k = 0; k < kMaxTypes; ++k)
+      if (in->fixed[k]) p.fixed_mask |= 1u << k;
+  };
+  if (r == -1) {  // every field of every replica: one shared record
+    DevParams p;
+    default_params(p, in->temperature);
+    fill(p);
+    h->psets.assign(1, p);
+    h->pset_refs.assign(1, h->nrep);
+    for (auto& R : h->reps) R.pset = 0;
+    h->reps_dirty = true;
+    h->params_dirty = true;
+    return CPM_OK;
+  }
+  return for_replicas(h, r, fill);
+}
+}  // namespace
+
+int cpm_set_params(cpm_handle* h, const cpm_static_params* in) { return set_params(h, -1, in); }
+int cpm_set_params_r(cpm_handle* h, int r, const cpm_static_params* in) {
+  return set_params(h, r < 0 ? -2 : r, in);
+}
+
+int cpm_get_param_index(const cpm_handle* h, int* out) {
+  if (!h || !out) return CPM_ERR_INVALID;
+  for (int r = 0; r < h->nrep; ++r) out[r] = h->reps[r].pset;
+  return CPM_OK;
+}
+
+int cpm_get_device(const cpm_handle* h, int* device) {
+  if (!h || !device) return CPM_ERR_INVALID;
+  *device = h->device;
+  return CPM_OK;
+}
+
+int cpm_get_seed(const cpm_handle* h, uint64_t* seed, uint32_t* stream_id) {
+  if (!h) return CPM_ERR_INVALID;
+  if (seed) *seed = h->seed;
+  if (stream_id) *stream_id = h->stream_id;
   return CPM_OK;
 }
 

@@ -98,6 +98,17 @@ class StaticParams(ctypes.Structure):
                 ("fixed", ctypes.c_int * MAX_TYPES)]
 
 
+class _DeviceArray:
+    """__cuda_array_interface__ (version 3) of engine-owned device memory;
+    a tensor made from it holds this object, which holds the engine."""
+
+    def __init__(self, ptr, shape, owner, typestr="<i4"):
+        self._owner = owner
+        self.__cuda_array_interface__ = {"shape": tuple(int(v) for v in shape),
+                                         "typestr": typestr, "data": (int(ptr), False),
+                                         "version": 3, "strides": None, "stream": None}
+
+
 _lib = None
 
 
@@ -161,6 +172,14 @@ def library():
         "cpm_set_variant": [H, ctypes.c_int],
         "cpm_sweep_config": [H, ip, ip, ip, ip, ip, ip, ip],
         "cpm_set_dispatch": [H, ctypes.c_int],
+        "cpm_recount": [H],
+        "cpm_set_centroid_sums_r": [H, ctypes.c_int, ctypes.c_void_p],
+        "cpm_get_params_r": [H, ctypes.c_int, ctypes.POINTER(StaticParams)],
+        "cpm_set_params_r": [H, ctypes.c_int, ctypes.POINTER(StaticParams)],
+        "cpm_set_params": [H, ctypes.POINTER(StaticParams)],
+        "cpm_get_param_index": [H, ctypes.c_void_p],
+        "cpm_get_seed": [H, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint32)],
+        "cpm_get_device": [H, ctypes.POINTER(ctypes.c_int)],
         "cpm_run_scores": [H, ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int,
                            ctypes.POINTER(ScoreSpec)],
         "cpm_observe_heterotypic": [H, ctypes.c_void_p],
@@ -226,6 +245,67 @@ class _Engine:
         buf = (ctypes.c_int32 * n.value).from_address(ptr.value)
         buf._owner = self  # the array keeps this engine (and its memory) alive
         return np.ctypeslib.as_array(buf).reshape(shape)
+
+    def host_lattice(self, replica=0):
+        """Writable host view of a replica's lattice ([y, x] / [z, y, x])."""
+        return self._host_view(replica, self._replica_shape(replica))
+
+    def device_lattice(self, replica=0):
+        """Zero-copy torch.int32 CUDA tensor of a replica's device lattice
+        (shape as host_lattice; values id | type << 24).  It shows the state
+        after the last completed run: call synchronize() first.  Writing to
+        it changes the engine's lattice; call recount() afterwards so that
+        the tables describe it again.  The tensor keeps the engine alive."""
+        import torch
+        view = _DeviceArray(self.device_lattice_ptr(replica), self._replica_shape(replica), self)
+        return torch.as_tensor(view, device=torch.device("cuda", self.device))
+
+    @property
+    def device(self):
+        d = ctypes.c_int()
+        self._call("cpm_get_device", ctypes.byref(d))
+        return d.value
+
+    def recount(self):
+        """Revalidate the device lattices and recompute all tables from
+        them (push_to_gpu without the host copy)."""
+        self._call("cpm_recount")
+
+    def set_centroid_sums(self, replica, centroid_sums):
+        """Restore a replica's centroid sums (as tables() returned them),
+        after a push: they depend on the path, area and perimeter do not."""
+        cs = np.ascontiguousarray(centroid_sums, dtype=np.int64)
+        if cs.shape != (self._ncells(replica) + 1, self.dimensionality):
+            raise CpmError(CPM_ERR_INVALID, f"centroid sums must have shape "
+                           f"{(self._ncells(replica) + 1, self.dimensionality)}")
+        self._call("cpm_set_centroid_sums_r", int(replica), cs.ctypes.data)
+
+    def get_params(self, replica=0):
+        """A replica's parameters as a StaticParams record."""
+        p = StaticParams()
+        self._call("cpm_get_params_r", int(replica), ctypes.byref(p))
+        return p
+
+    def set_params(self, replica, params):
+        """Set a replica's parameters from a StaticParams record (replica
+        None: every replica)."""
+        if replica is None:
+            self._call("cpm_set_params", ctypes.byref(params))
+        else:
+            self._call("cpm_set_params_r", int(replica), ctypes.byref(params))
+
+    def param_index(self):
+        """Per replica, the parameter record it uses (equal values share)."""
+        out = np.empty(self.n_replicas, np.int32)
+        self._call("cpm_get_param_index", out.ctypes.data)
+        return out
+
+    @property
+    def seed(self):
+        """(seed, stream_id) of the Philox stream."""
+        s, k = ctypes.c_uint64(), ctypes.c_uint32()
+        self._call("cpm_get_seed", ctypes.byref(s), ctypes.byref(k))
+        return s.value, k.value
 
     def device_lattice_ptr(self, replica=0):
         """Device address of a replica's lattice (uint32, row-major)."""
@@ -360,6 +440,9 @@ class Cpm(_Engine):
     def _ncells(self, replica):
         return self.number_of_cells
 
+    def _replica_shape(self, replica):
+        return self._shape
+
     def set_constraints(self, cell_type, *, other_cell_type=-1,
                         lambda_perimeter=-1, target_perimeter=-1,
                         lambda_area=-1, target_area=-1, lambda_act=-1,
@@ -481,6 +564,9 @@ class Batch(_Engine):
 
     def _ncells(self, replica):
         return self.ncells[replica]
+
+    def _replica_shape(self, replica):
+        return tuple(reversed(self.sizes[replica]))
 
     def lattice(self, replica):
         """Writable host view of one replica's lattice ([y, x] / [z, y, x])."""

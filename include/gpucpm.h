@@ -40,6 +40,7 @@ extern "C" {
 #define CPM_MAX_TYPES 32
 
 typedef struct cpm_handle cpm_handle;
+typedef struct cpm_static_params cpm_static_params; /* defined below */
 
 /* Counters of one run, summed over all replicas (see cpm_get_counters). */
 typedef struct {
@@ -152,6 +153,38 @@ int cpm_push(cpm_handle* h);
 /* Replaces Cpm::retreiveCellIdsFromGpu (src/cpm.cu:531-540): copies every
  * device lattice back into the host buffers.  Synchronous. */
 int cpm_pull(cpm_handle* h);
+
+/* ---- state I/O and resume (no counterpart in the reference, whose state
+ *      lives only in H2D / D2H round trips, src/cpm.cu:531-597) ---------- */
+
+/* cpm_push without the host copy: revalidates every device lattice and
+ * recomputes the tables from it, for callers that changed the lattice in
+ * place on the device (e.g. through a view of cpm_device_lattice_r).
+ * Synchronous. */
+int cpm_recount(cpm_handle* h);
+
+/* Replace replica r's centroid sums (as cpm_get_tables_r returned them) on
+ * the device.  Area and perimeter are exact functions of the lattice, which
+ * push / recount recompute; centroid sums also record which periodic image
+ * each site joined as, so an exact resume restores them after the push.
+ * Needs a successful push.  Synchronous. */
+int cpm_set_centroid_sums_r(cpm_handle* h, int replica, const int64_t* centroid_sums);
+
+/* A replica's parameters as one record (the layout of cpm_static_params
+ * below): read, write for one replica, or write for every replica. */
+int cpm_get_params_r(const cpm_handle* h, int replica, cpm_static_params* out);
+int cpm_set_params_r(cpm_handle* h, int replica, const cpm_static_params* in);
+int cpm_set_params(cpm_handle* h, const cpm_static_params* in);
+
+/* out[r] (n_replicas ints) = the parameter record replica r uses; replicas
+ * with equal values share all parameters (so a checkpoint stores each
+ * record once). */
+int cpm_get_param_index(const cpm_handle* h, int* out);
+
+/* The Philox key and stream id set by cpm_set_seed / the CUDA device the
+ * handle lives on. */
+int cpm_get_seed(const cpm_handle* h, uint64_t* seed, uint32_t* stream_id);
+int cpm_get_device(const cpm_handle* h, int* device);
 
 /* ---- sweeps ----------------------------------------------------------- */
 
@@ -309,10 +342,11 @@ int cpm_lr_backward(const float* scores, const float* dl_do, const float* obs,
 #define CPM_STATIC_MAX_SITES (1 << 18)
 #define CPM_STATIC_MAX_CELLS 16383
 
-/* Parameters of cpm_sweep_static, in the conventions of the setters above:
+/* One replica's parameters (cpm_get_params_r / cpm_set_params_r) and the
+ * parameters of cpm_sweep_static, in the conventions of the setters above:
  * J[a * CPM_MAX_TYPES + b] is the adhesion a site of type a feels from a
  * neighbour of type b; index 0 of the per-type arrays is the medium. */
-typedef struct {
+struct cpm_static_params {
     float J[CPM_MAX_TYPES * CPM_MAX_TYPES];
     float lambda_area[CPM_MAX_TYPES];
     int target_area[CPM_MAX_TYPES];
@@ -321,7 +355,7 @@ typedef struct {
     float temperature;
     float stickiness[CPM_MAX_TYPES * CPM_MAX_TYPES]; /* as cpm_set_stickiness */
     int fixed[CPM_MAX_TYPES];                        /* as cpm_set_fixed */
-} cpm_static_params;
+};
 
 /* No counterpart in the reference.  Runs `mcs` Monte Carlo steps of the same
  * sweep as cpm_run on one lattice that lives entirely in caller-owned device
