@@ -56,6 +56,10 @@ struct cpm_handle {
   long long rows = 0;
 
   uint32_t* h_lat = nullptr;  // pinned, all replicas back to back
+  // chemotaxis field (allocated on first use): host doubles as the
+  // reference keeps them, device floats; layout of SweepArgs::field
+  std::vector<double> h_field;
+  float* d_field = nullptr;
   uint32_t* d_lat = nullptr;
   unsigned long long* d_ap[2] = {nullptr, nullptr};  // packed (area, perimeter)
   long long* d_cs[2] = {nullptr, nullptr};
@@ -143,6 +147,7 @@ int class_count_h(int n, int c) {
 void free_all(cpm_handle* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   cudaFreeHost(h->h_lat);
+  cudaFree(h->d_field);
   cudaFree(h->d_lat);
   for (int b = 0; b < 2; ++b) {
     cudaFree(h->d_ap[b]);
@@ -506,6 +511,12 @@ int upload_params(cpm_handle* h) {
     p.stick_on = 0;
     for (int k = 0; k < kMaxTypes * kMaxTypes; ++k)
       if (p.stick[k] != 0.0f) p.stick_on = 1;
+    p.chemo_on = 0;
+    for (int k = 0; k < kMaxTypes; ++k)
+      if (p.chemo[k] != 0.0f) p.chemo_on = 1;
+    if (p.chemo_on && !h->d_field)
+      return h->fail(CPM_ERR_STATE, "chemotaxis is set but the engine has no field "
+                                    "(create it with the field flag or call cpm_host_field_r)");
   }
   if (m > h->params_cap) {
     CPM_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -551,6 +562,7 @@ SweepArgs sweep_args(const cpm_handle* h, int v, int d) {
   const cpm_handle::Config& c = h->cfg[v];
   a.dlist = h->d_dlist;
   a.block_local = d == CPM_DISPATCH_REPLICA ? 1 : 0;
+  a.field = h->d_field;
   a.list_cap = a.block_local ? c.list_cap_local : c.list_cap;
   a.rep_order = h->d_rep_order;
   a.ctl = h->d_ctl;
@@ -598,14 +610,23 @@ extern "C" {
 
 int cpm_create(int dimension, int dimensionality, int number_of_cells,
                float temperature, int flags, cpm_handle** out) {
-  if (flags != 0) {
-    g_create_error = "flags must be 0 (field / act lattices are not supported)";
+  if (flags & ~CPM_FLAG_FIELD) {
+    g_create_error = "unknown flags (only CPM_FLAG_FIELD is supported; act lattices are not)";
     if (out) *out = nullptr;
     return CPM_ERR_UNSUPPORTED;
   }
   const int nz = dimensionality == 3 ? dimension : 1;
-  return build_engine(1, dimensionality, &dimension, &dimension, &nz,
-                      &number_of_cells, temperature, out);
+  const int rc = build_engine(1, dimensionality, &dimension, &dimension, &nz,
+                              &number_of_cells, temperature, out);
+  if (rc == CPM_OK && (flags & CPM_FLAG_FIELD)) {
+    if (int rc2 = cpm_host_field_r(*out, 0, nullptr, nullptr)) {
+      g_create_error = cpm_last_error(*out);
+      cpm_destroy(*out);
+      *out = nullptr;
+      return rc2;
+    }
+  }
+  return rc;
 }
 
 int cpm_create_box(int nx, int ny, int nz, int dimensionality,
@@ -691,6 +712,44 @@ int cpm_add_cell(cpm_handle* h, int type, int x, int y, int z) {
   return CPM_OK;
 }
 
+int cpm_host_field_r(cpm_handle* h, int r, double** ptr, int64_t* nvalues) {
+  if (int rc = check_replica(h, r)) return rc;
+  CPM_BIND(h);
+  if (!h->d_field) {
+    const size_t n = (size_t)h->total_sites * h->ndim;
+    try {
+      h->h_field.assign(n, 0.0);
+    } catch (...) {
+      return h->fail(CPM_ERR_ALLOC, "host field allocation failed");
+    }
+    CPM_CUDA(h, cudaMalloc((void**)&h->d_field, sizeof(float) * (n ? n : 1)));
+    CPM_CUDA(h, cudaMemsetAsync(h->d_field, 0, sizeof(float) * (n ? n : 1), h->stream));
+    if (h->graph_exec) {  // captured without a field
+      cudaGraphExecDestroy(h->graph_exec);
+      h->graph_exec = nullptr;
+    }
+  }
+  const DevReplica& R = h->reps[r];
+  if (ptr) *ptr = h->h_field.data() + (size_t)h->ndim * R.lat_off;
+  if (nvalues) *nvalues = (int64_t)h->ndim * R.nx * R.ny * R.nz;
+  return CPM_OK;
+}
+
+namespace {
+int set_chemotaxis(cpm_handle* h, int r, int type, float lambda) {
+  if (!h) return CPM_ERR_INVALID;
+  if (int rc = check_type(h, type)) return rc;
+  if (!std::isfinite(lambda)) return h->fail(CPM_ERR_INVALID, "lambda must be finite");
+  return for_replicas(h, r, [&](DevParams& p) { p.chemo[type] = lambda; });
+}
+}  // namespace
+int cpm_set_chemotaxis(cpm_handle* h, int type, float lambda) {
+  return set_chemotaxis(h, -1, type, lambda);
+}
+int cpm_set_chemotaxis_r(cpm_handle* h, int r, int type, float lambda) {
+  return set_chemotaxis(h, r < 0 ? -2 : r, type, lambda);
+}
+
 int cpm_host_lattice_r(cpm_handle* h, int r, uint32_t** ptr, int64_t* nsites) {
   if (int rc = check_replica(h, r)) return rc;
   const DevReplica& R = h->reps[r];
@@ -747,6 +806,12 @@ int cpm_push(cpm_handle* h) {
   h->pushed = false;
   CPM_CUDA(h, cudaMemcpyAsync(h->d_lat, h->h_lat, sizeof(uint32_t) * h->total_sites,
                               cudaMemcpyHostToDevice, h->stream));
+  if (h->d_field) {  // the field goes along, as in Cpm::moveCellIdsToGpu
+    std::vector<float> f(h->h_field.begin(), h->h_field.end());
+    CPM_CUDA(h, cudaMemcpyAsync(h->d_field, f.data(), sizeof(float) * f.size(),
+                                cudaMemcpyHostToDevice, h->stream));
+    CPM_CUDA(h, cudaStreamSynchronize(h->stream));  // `f` lives on this frame
+  }
   return recount_tables(h);
 }
 

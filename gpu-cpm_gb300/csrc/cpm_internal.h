@@ -112,6 +112,11 @@ struct DevParams {
   int perim_on;         // any lam_perim != 0
   unsigned fixed_mask;  // bit t: cells of type t never move (src/kernels2d.cu:280-290)
   int stick_on;         // any stickiness != 0
+  // chemotaxis lambda per type: dH -= lambda (d . field at the source), d the
+  // unit copy direction (src/kernels2d.cu:302-334, src/kernels3d.cu:275-324)
+  float chemo[kMaxTypes];
+  int chemo_on;         // any chemo != 0
+  int pad[3];
 };
 
 struct DevReplica {
@@ -174,6 +179,9 @@ struct SweepArgs {
   // replicas in rep_order and runs all their phases with block barriers.
   int block_local;
   const int* rep_order;  // [nrep] replicas by decreasing site count
+  // chemotaxis field, float: replica r's component k of site i at
+  // field[ndim * lat_off + k * sites_r + i] (null when no field exists)
+  const float* field;
   // Monte Carlo time of the first MCS: tick0, or *tick_ptr when tick_ptr is
   // set (graph replays); in the latter case block 0 advances *tick_ptr by
   // mcs when the launch ends.

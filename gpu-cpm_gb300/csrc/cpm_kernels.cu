@@ -148,6 +148,50 @@ SweepShape shape_of() {
   return s;
 }
 
+// Chemotaxis: unit copy direction (target minus source) dotted with the
+// field at the source site, every step rounded as written (the oracle
+// repeats it).  As in the reference, the direction is the raw difference of
+// the wrapped coordinates in 2D (src/kernels2d.cu:302-309) and the nearest
+// image in 3D (src/kernels3d.cu:275-299).  F: the replica's field, `sites`
+// values per component.
+template <int NDIM>
+__device__ __forceinline__ float chemo_dot(const float* F, long long sites, int x, int y,
+                                           int z, int kdir, int nx, int ny, int nz) {
+  int ox, oy, oz;  // source offset from the target, neighbour order of Stage
+  if (NDIM == 2) {
+    const int m = kdir + (kdir >= 4);
+    oz = 0;
+    oy = m / 3 - 1;
+    ox = m % 3 - 1;
+  } else {
+    const int m = kdir + (kdir >= 13);
+    oz = m / 9 - 1;
+    oy = (m / 3) % 3 - 1;
+    ox = m % 3 - 1;
+  }
+  auto wrapc = [](int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); };
+  const int sx = wrapc(x + ox, nx), sy = wrapc(y + oy, ny), sz = NDIM == 3 ? wrapc(z + oz, nz) : 0;
+  int dx = x - sx, dy = y - sy, dz = z - sz;
+  if (NDIM == 3) {
+    if (dx > nx / 2) dx -= nx;
+    if (dx < -(nx / 2)) dx += nx;
+    if (dy > ny / 2) dy -= ny;
+    if (dy < -(ny / 2)) dy += ny;
+    if (dz > nz / 2) dz -= nz;
+    if (dz < -(nz / 2)) dz += nz;
+  }
+  const float fx = (float)dx, fy = (float)dy, fz = (float)dz;
+  float s2 = __fmul_rn(fx, fx);
+  s2 = __fmaf_rn(fy, fy, s2);
+  if (NDIM == 3) s2 = __fmaf_rn(fz, fz, s2);
+  const float len = __fsqrt_rn(s2);
+  const long long site = ((long long)sz * ny + sy) * nx + sx;
+  float c = __fmul_rn(__fdiv_rn(fx, len), __ldg(F + site));
+  c = __fmaf_rn(__fdiv_rn(fy, len), __ldg(F + sites + site), c);
+  if (NDIM == 3) c = __fmaf_rn(__fdiv_rn(fz, len), __ldg(F + 2 * sites + site), c);
+  return c;
+}
+
 // Per-phase view of the double-buffered tables.
 template <int NDIM>
 struct PhaseTables {
@@ -309,6 +353,7 @@ __global__ void __launch_bounds__(kSweepThreadsMax, 1)
     const DevParams* P = a.params + __ldg(&a.reps[r].pset);
     const unsigned fixed_mask = __ldg(&P->fixed_mask);
     const bool stick_on = __ldg(&P->stick_on) != 0;
+    const bool chemo_on = __ldg(&P->chemo_on) != 0;
     const int nx = __ldg(&a.reps[r].nx), ny = __ldg(&a.reps[r].ny),
               nz = __ldg(&a.reps[r].nz), ncells = __ldg(&a.reps[r].ncells);
     const long long lat_off = __ldg(&a.reps[r].lat_off);
@@ -474,6 +519,25 @@ __global__ void __launch_bounds__(kSweepThreadsMax, 1)
             e_old = __fadd_rn(e_old, e_st);
           }
           float dH = __fsub_rn(e_new, e_old);
+          {
+            // chemotaxis first, as in the reference's sum; lambda of the
+            // source type, of the target type for a medium source
+            float chemo = 0.0f;
+            if (chemo_on) {  // uniform over the tile
+              const float lam = __ldg(&P->chemo[ts ? ts : tt]);
+              if (lam != 0.0f) {
+                const int qx = q % G::CX, qy = (q / G::CX) % G::CY,
+                          qz = q / (G::CX * G::CY);
+                const int x = class_coord(nx, cx, i0 + qx);
+                const int y = class_coord(ny, cy, j0 + qy);
+                const int z = NDIM == 3 ? class_coord(nz, cz, l0 + qz) : 0;
+                const long long sites = (long long)nx * ny * nz;
+                chemo = __fmul_rn(-lam, chemo_dot<NDIM>(a.field + NDIM * lat_off, sites, x, y,
+                                                          z, kdir, nx, ny, nz));
+              }
+            }
+            dH = __fadd_rn(chemo, dH);
+          }
           const int dps = NB - 2 * cnt_s;
           const int dpt = 2 * cnt_t - NB;
           if (PERIM && __ldg(&P->perim_on)) {

@@ -22,10 +22,13 @@ Differences from the reference, all deliberate:
   * stickiness accepts floats; fixed and stickiness apply whatever the
     run() toggles (the reference applies fixed types only when
     partial_dispatch is off or some type is fixed, src/cpm.cu:308-320,
-    which for a non-zero fixed flag is the same).
-The act, chemotaxis and persistence terms are not part of this engine:
-setting them raises CpmError, and get_act_state / get_field return zero
-arrays of the reference's shapes.
+    which for a non-zero fixed flag is the same);
+  * the chemotaxis field is float on the device (the reference keeps
+    doubles) and the chemotaxis energy is summed in FP32, rounded step by
+    step; get_field's array exists whether or not has_field was set.
+The act and persistence terms are not part of this engine: setting them
+raises CpmError, and get_act_state returns a zero array of the reference's
+shape.
 """
 import ctypes
 import os
@@ -44,6 +47,7 @@ CPM_ERR_STATE = 4
 CPM_ERR_TIMEOUT = 5
 CPM_ERR_UNSUPPORTED = 6
 MAX_TYPES = 32
+CPM_FLAG_FIELD = 1
 DISPATCH_GRID = 0
 DISPATCH_REPLICA = 1
 
@@ -143,6 +147,10 @@ def library():
         "cpm_set_adhesion_r": [H, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                ctypes.c_float, ctypes.c_int],
         "cpm_set_fixed": [H, ctypes.c_int, ctypes.c_int],
+        "cpm_set_chemotaxis": [H, ctypes.c_int, ctypes.c_float],
+        "cpm_set_chemotaxis_r": [H, ctypes.c_int, ctypes.c_int, ctypes.c_float],
+        "cpm_host_field_r": [H, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p),
+                             ctypes.POINTER(ctypes.c_int64)],
         "cpm_set_fixed_r": [H, ctypes.c_int, ctypes.c_int, ctypes.c_int],
         "cpm_set_stickiness": [H, ctypes.c_int, ctypes.c_int, ctypes.c_float],
         "cpm_set_stickiness_r": [H, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float],
@@ -245,6 +253,17 @@ class _Engine:
         buf = (ctypes.c_int32 * n.value).from_address(ptr.value)
         buf._owner = self  # the array keeps this engine (and its memory) alive
         return np.ctypeslib.as_array(buf).reshape(shape)
+
+    def field(self, replica=0):
+        """Writable host view of a replica's chemotaxis field, float64
+        [ndim, (nz,) ny, nx] (component k = x, y, z), zero until written;
+        pushed with the lattice."""
+        ptr, n = ctypes.c_void_p(), ctypes.c_int64()
+        self._call("cpm_host_field_r", int(replica), ctypes.byref(ptr), ctypes.byref(n))
+        buf = (ctypes.c_double * n.value).from_address(ptr.value)
+        buf._owner = self
+        return np.ctypeslib.as_array(buf).reshape((self.dimensionality,)
+                                                  + tuple(self._replica_shape(replica)))
 
     def host_lattice(self, replica=0):
         """Writable host view of a replica's lattice ([y, x] / [z, y, x])."""
@@ -428,8 +447,8 @@ class Cpm(_Engine):
         lib = library()
         h = ctypes.c_void_p()
         _check(lib.cpm_create(int(dimension), int(dimensionality),
-                              int(number_of_cells), float(temperature), 0,
-                              ctypes.byref(h)), None)
+                              int(number_of_cells), float(temperature),
+                              CPM_FLAG_FIELD if has_field else 0, ctypes.byref(h)), None)
         super().__init__(h)
         self.dimension = int(dimension)
         self.number_of_cells = int(number_of_cells)
@@ -458,8 +477,6 @@ class Cpm(_Engine):
         """
         ct = int(cell_type)
         unsupported = []
-        if lambda_chemotaxis != -1:
-            unsupported.append("lambda_chemotaxis")
         if (lambda_persistence != -1 and persistence_diffusion != -1
                 and persistence_time != -1):
             unsupported.append("persistence")
@@ -474,6 +491,8 @@ class Cpm(_Engine):
             self._call("cpm_set_area", ct, int(target_area), float(lambda_area))
         if fixed >= 0:
             self._call("cpm_set_fixed", ct, int(fixed))
+        if lambda_chemotaxis != -1:
+            self._call("cpm_set_chemotaxis", ct, float(lambda_chemotaxis))
         if other_cell_type != -1 and adhesion != -1:
             self._call("cpm_set_adhesion", ct, int(other_cell_type), float(adhesion),
                        1 if set_adhesion_symmetric else 0)
@@ -536,7 +555,9 @@ class Cpm(_Engine):
         return np.zeros(self._shape, np.int32)
 
     def get_field(self):
-        return np.zeros((self.dimensionality,) + self._shape, np.float64)
+        """Writable float64 view of the chemotaxis field, shape (d, D, D[, D])
+        as the reference's (src/python_wrapper.cpp:274-290)."""
+        return self.field(0)
 
 
 class Batch(_Engine):
@@ -591,6 +612,12 @@ class Batch(_Engine):
         else:
             self._call("cpm_set_perimeter_r", int(replica), int(cell_type), int(target),
                        float(lam))
+
+    def set_chemotaxis(self, replica, cell_type, lam):
+        if replica is None:
+            self._call("cpm_set_chemotaxis", int(cell_type), float(lam))
+        else:
+            self._call("cpm_set_chemotaxis_r", int(replica), int(cell_type), float(lam))
 
     def set_fixed(self, replica, cell_type, fixed=True):
         if replica is None:

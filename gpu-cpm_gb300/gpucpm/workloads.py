@@ -42,6 +42,8 @@ class Workload:
     meta: dict = field(default_factory=dict)
     stick: np.ndarray = None     # float32 [ntypes, ntypes] stickiness, or None
     fixed: np.ndarray = None     # bool [ntypes]: fixed (unmovable) types, or None
+    chemo: np.ndarray = None     # float32 [ntypes]: chemotaxis lambdas, or None
+    field: np.ndarray = None     # float64 [ndim, (nz,) ny, nx] chemotaxis field, or None
 
     @property
     def ndim(self):
@@ -71,7 +73,15 @@ class Workload:
             engine.set_temperature(self.temperature)
         else:
             engine.set_temperature(replica, self.temperature)
+        if self.field is not None:
+            view = engine.field(0 if replica is None else replica)
+            view[...] = self.field
         for a in range(nt):
+            if self.chemo is not None and self.chemo[a] != 0:
+                if replica is None:
+                    engine._call("cpm_set_chemotaxis", a, float(self.chemo[a]))
+                else:
+                    engine.set_chemotaxis(replica, a, float(self.chemo[a]))
             if self.fixed is not None and self.fixed[a]:
                 if replica is None:
                     engine._call("cpm_set_fixed", a, 1)
@@ -87,7 +97,8 @@ class Workload:
     def oracle_kwargs(self):
         return dict(J=self.J, lam_area=self.lam_area, tgt_area=self.tgt_area,
                     lam_perim=self.lam_perim, tgt_perim=self.tgt_perim,
-                    temperature=self.temperature, stick=self.stick, fixed=self.fixed)
+                    temperature=self.temperature, stick=self.stick, fixed=self.fixed,
+                    chemo=self.chemo, field=self.field)
 
 
 def _params(nt, J, lam_area=0.0, tgt_area=0, lam_perim=0.0, tgt_perim=0):

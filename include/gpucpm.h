@@ -54,9 +54,10 @@ typedef struct {
 /* Replaces Cpm::Cpm (src/cpm.cu:176-261) as reached through PyCpm_init
  * (src/python_wrapper.cpp:27-41).  Argument order follows the Python
  * constructor (dimension, dimensionality, number_of_cells, temperature).
- * `flags` is reserved (has_field / has_act are out-of-scope terms) and must
- * be 0.  Allocates the device lattice and the cell tables for ids
- * 0..number_of_cells on the current CUDA device. */
+ * `flags`: CPM_FLAG_FIELD allocates the chemotaxis field (has_field); act
+ * lattices (has_act) are not supported.  Allocates the device lattice and
+ * the cell tables for ids 0..number_of_cells on the current CUDA device. */
+#define CPM_FLAG_FIELD 1
 int cpm_create(int dimension, int dimensionality, int number_of_cells,
                float temperature, int flags, cpm_handle** out);
 
@@ -111,6 +112,17 @@ int cpm_set_adhesion(cpm_handle* h, int type, int other, float J,
 int cpm_set_adhesion_r(cpm_handle* h, int replica, int type, int other,
                        float J, int symmetric);
 
+/* Replaces Cpm::setChemotaxis (src/cpm.cu:155-158): lambda of a type.  An
+ * attempt adds -lambda * (d . F) to dH, with d the unit copy direction
+ * (source to target) and F the field at the source site; lambda is the
+ * source type's, or the target type's when the source is the medium
+ * (src/kernels2d.cu:302-334, src/kernels3d.cu:275-324).  Needs a field.
+ * As in the reference, d is the raw difference of the wrapped coordinates
+ * in 2D (so it points the other way across the lattice seam) and the
+ * nearest-image difference in 3D. */
+int cpm_set_chemotaxis(cpm_handle* h, int type, float lambda);
+int cpm_set_chemotaxis_r(cpm_handle* h, int replica, int type, float lambda);
+
 /* Replaces Cpm::setFixed (src/cpm.cu:150-153).  Cells of a fixed type never
  * move: an attempt whose target belongs to one does nothing, and one whose
  * source belongs to one proposes the medium instead (src/kernels2d.cu:
@@ -139,6 +151,13 @@ int cpm_add_cell(cpm_handle* h, int type, int x, int y, int z);
 int cpm_host_lattice(cpm_handle* h, uint32_t** ptr, int64_t* nsites);
 int cpm_host_lattice_r(cpm_handle* h, int replica, uint32_t** ptr,
                        int64_t* nsites);
+
+/* Replaces Cpm::getField (src/cpm.cu:527-529) behind get_field
+ * (src/python_wrapper.cpp:274-290): the host chemotaxis field of replica r,
+ * `dimensionality` components of one value per site ([k][z][y][x] doubles,
+ * component k = x, y, z), allocated with zeros on the first call.  Pushed
+ * with the lattice (as float); the sweep never writes it. */
+int cpm_host_field_r(cpm_handle* h, int replica, double** ptr, int64_t* nvalues);
 
 /* Device lattice of a replica (row-major uint32), for zero-copy readers. */
 int cpm_device_lattice_r(cpm_handle* h, int replica, uint32_t** dptr);

@@ -29,6 +29,8 @@ class Params(ctypes.Structure):
         ("stream", ctypes.c_uint32),
         ("stick", ctypes.c_float * (MAX_TYPES * MAX_TYPES)),
         ("fixed_mask", ctypes.c_uint32),
+        ("chemo", ctypes.c_float * MAX_TYPES),
+        ("field", ctypes.c_void_p),
     ]
 
 
@@ -95,12 +97,13 @@ class OracleSim:
     id | type << 24.  Parameters follow the engine's conventions: J[a][b] is
     the adhesion seen by a site of type a next to a site of type b; stick
     (optional, [a][b]) the stickiness, fixed (optional, per type) the
-    unmovable types.
+    unmovable types, chemo (optional, per type) the chemotaxis lambdas and
+    field (optional, [ndim, (nz,) ny, nx]) the chemotaxis field.
     """
 
     def __init__(self, lattice, ncells, J, lam_area, tgt_area,
                  lam_perim=None, tgt_perim=None, temperature=1.0, seed=0,
-                 stream=0, stick=None, fixed=None):
+                 stream=0, stick=None, fixed=None, chemo=None, field=None):
         lat = np.ascontiguousarray(lattice, dtype=np.uint32).copy()
         self.ndim = lat.ndim
         self.lattice = lat
@@ -140,6 +143,13 @@ class OracleSim:
             if f:
                 mask |= 1 << t
         p.fixed_mask = mask
+        fill(p.chemo, chemo, np.float32)
+        self.field = None
+        if field is not None:  # [ndim, (nz,) ny, nx], rounded to float as the engine does
+            self.field = np.ascontiguousarray(field, dtype=np.float32)
+            if self.field.shape != (self.ndim,) + lat.shape:
+                raise ValueError("field must have shape (ndim,) + lattice shape")
+            p.field = self.field.ctypes.data
         self.params = p
         n1 = self.ncells + 1
         self.area = np.zeros(n1, np.int32)

@@ -76,7 +76,53 @@ struct Params {
   // move (src/kernels2d.cu:280-290)
   float stick[kMaxTypes * kMaxTypes];
   uint32_t fixed_mask;
+  // chemotaxis lambda per type and the field ([k][z][y][x] floats, or null)
+  // (src/kernels2d.cu:302-334, src/kernels3d.cu:275-324)
+  float chemo[kMaxTypes];
+  const float* field;
 };
+
+// Unit copy direction (target minus source) dotted with the field at the
+// source site: the raw difference of wrapped coordinates in 2D
+// (src/kernels2d.cu:302-309), the nearest image in 3D (src/kernels3d.cu:
+// 275-299); FP32, rounded step by step.
+float chemo_dot(const Params& p, int x, int y, int z, int kdir) {
+  int ox, oy, oz;
+  if (p.ndim == 2) {
+    const int m = kdir + (kdir >= 4);
+    oz = 0;
+    oy = m / 3 - 1;
+    ox = m % 3 - 1;
+  } else {
+    const int m = kdir + (kdir >= 13);
+    oz = m / 9 - 1;
+    oy = (m / 3) % 3 - 1;
+    ox = m % 3 - 1;
+  }
+  const int nx = p.nx, ny = p.ny, nz = p.ndim == 3 ? p.nz : 1;
+  auto wrapc = [](int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); };
+  const int sx = wrapc(x + ox, nx), sy = wrapc(y + oy, ny), sz = p.ndim == 3 ? wrapc(z + oz, nz) : 0;
+  int dx = x - sx, dy = y - sy, dz = z - sz;
+  if (p.ndim == 3) {
+    if (dx > nx / 2) dx -= nx;
+    if (dx < -(nx / 2)) dx += nx;
+    if (dy > ny / 2) dy -= ny;
+    if (dy < -(ny / 2)) dy += ny;
+    if (dz > nz / 2) dz -= nz;
+    if (dz < -(nz / 2)) dz += nz;
+  }
+  const float fx = (float)dx, fy = (float)dy, fz = (float)dz;
+  float s2 = fx * fx;
+  s2 = std::fma(fy, fy, s2);
+  if (p.ndim == 3) s2 = std::fma(fz, fz, s2);
+  const float len = std::sqrt(s2);
+  const int64_t sites = (int64_t)nx * ny * nz;
+  const int64_t site = ((int64_t)sz * ny + sy) * nx + sx;
+  float c = (fx / len) * p.field[site];
+  c = std::fma(fy / len, p.field[sites + site], c);
+  if (p.ndim == 3) c = std::fma(fz / len, p.field[2 * sites + site], c);
+  return c;
+}
 
 // ---- Philox4x32-10 --------------------------------------------------------
 inline void philox_round(uint32_t c[4], uint32_t k0, uint32_t k1) {
@@ -262,6 +308,12 @@ inline int attempt(const Params& p, uint32_t* lat, const Tables& tb, int x,
     e_old = e_old + e_st;
   }
   float dH = e_new - e_old;
+  {
+    float chemo = 0.0f;
+    const float lam = p.chemo[ts ? ts : tt];
+    if (lam != 0.0f && p.field) chemo = -lam * chemo_dot(p, x, y, z, kdir);
+    dH = chemo + dH;
+  }
   const int dps = N - 2 * cnt_s;  // source cell gains the target site
   const int dpt = 2 * cnt_t - N;  // target cell loses it
   const uint32_t is = s & 0xFFFFFFu, it = t & 0xFFFFFFu;

@@ -35,8 +35,10 @@ def lib():
         L.ref_set_temperature.argtypes = [i]
         L.ref_set_stickiness.argtypes = [i, i, i]
         L.ref_set_fixed.argtypes = [i, i]
+        L.ref_set_chemotaxis.argtypes = [i, d]
+        L.ref_set_field.argtypes = [ctypes.c_void_p]
         L.ref_push.argtypes = [ctypes.c_void_p]
-        L.ref_run.argtypes = [i] * 15
+        L.ref_run.argtypes = [i] * 16
         L.ref_pull.argtypes = [ctypes.c_void_p]
         L.ref_tables.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.ref_max_coop_blocks.argtypes = [i, i, i, ctypes.POINTER(i)]
@@ -58,6 +60,7 @@ class RefGpu:
         self.dimension, self.ndim, self.ncells = int(dimension), int(dimensionality), int(ncells)
         self.perimeter = False
         self.fixed = False
+        self.chemotaxis = False
 
     def set_area(self, t, target, lam):
         _check(lib().ref_set_area(int(t), int(target), float(lam)))
@@ -71,6 +74,15 @@ class RefGpu:
 
     def set_stickiness(self, a, b, S):
         _check(lib().ref_set_stickiness(int(a), int(b), int(round(S))))
+
+    def set_chemotaxis(self, t, lam):
+        _check(lib().ref_set_chemotaxis(int(t), float(lam)))
+        self.chemotaxis = self.chemotaxis or lam != 0
+
+    def set_field(self, field):
+        """Chemotaxis field [ndim, D, D(, D)] (doubles, as the reference keeps it)."""
+        f = np.ascontiguousarray(field, dtype=np.float64)
+        _check(lib().ref_set_field(f.ctypes.data))
 
     def set_fixed(self, t, fixed=True):
         _check(lib().ref_set_fixed(int(t), 1 if fixed else 0))
@@ -89,10 +101,14 @@ class RefGpu:
                 self.set_perimeter(a, int(w.tgt_perim[a]), float(w.lam_perim[a]))
             if w.fixed is not None and w.fixed[a]:
                 self.set_fixed(a)
+            if w.chemo is not None and w.chemo[a] != 0:
+                self.set_chemotaxis(a, float(w.chemo[a]))
             for b in range(nt):
                 if w.stick is not None and w.stick[a, b] != 0:
                     self.set_stickiness(a, b, w.stick[a, b])
         _check(lib().ref_set_temperature(int(round(w.temperature))))
+        if w.field is not None:
+            self.set_field(w.field)
 
     def push(self, lattice):
         lat = np.ascontiguousarray(lattice, dtype=np.uint32)
@@ -108,7 +124,7 @@ class RefGpu:
                              updates_per_checkerboard_switch, updates_per_barrier,
                              int(iterations), int(inner), int(shared),
                              1 if self.perimeter else 0, int(centroid_tracking), int(seed),
-                             1 if self.fixed else 0))
+                             1 if self.fixed else 0, 1 if self.chemotaxis else 0))
 
     def synchronize(self):
         _check(lib().ref_synchronize())

@@ -62,7 +62,7 @@ struct State {
   int dim = 0, ndim = 2, ncells = 0;
   long long sites = 0;
   CUdeviceptr cellIds = 0, areas = 0, writeAreas = 0, circumferences = 0,
-              centroids = 0, analytics = 0, acts = 0;
+              centroids = 0, analytics = 0, acts = 0, field = 0;
   int mcs = 0;
   std::string err;
 } g;
@@ -99,7 +99,7 @@ int upload_settings() {
 
 void free_buffers() {
   CUdeviceptr* bufs[] = {&g.cellIds, &g.areas, &g.writeAreas, &g.circumferences,
-                         &g.centroids, &g.analytics, &g.acts};
+                         &g.centroids, &g.analytics, &g.acts, &g.field};
   for (CUdeviceptr* b : bufs)
     if (*b) {
       cuMemFree(*b);
@@ -176,6 +176,18 @@ int ref_set_stickiness(int type, int other, int S) {  // Cpm::setStickiness, src
   g.settings.types[type].stickiness[other] = (short)S;
   return upload_settings();
 }
+int ref_set_chemotaxis(int type, double lambda) {  // Cpm::setChemotaxis, src/cpm.cu:155-158
+  g.settings.types[type].chemotaxis = lambda;
+  return upload_settings();
+}
+// The field Cpm::moveCellIdsToGpu copies along (src/cpm.cu:542-544): doubles,
+// component-major [ndim][sites].
+int ref_set_field(const double* host) {
+  DRV(cuCtxSetCurrent(g.ctx));
+  if (!g.field) DRV(cuMemAlloc(&g.field, 8 * g.ndim * g.sites));
+  DRV(cuMemcpyHtoD(g.field, host, 8 * g.ndim * g.sites));
+  return 0;
+}
 int ref_set_fixed(int type, int fixed) {  // Cpm::setFixed, src/cpm.cu:150-153
   g.settings.types[type].fixed = fixed;
   return upload_settings();
@@ -216,15 +228,15 @@ int ref_run(int cell_sync, int block_sync, int global_sync, int threads_per_bloc
             int positions_per_thread, int positions_per_checkerboard,
             int updates_per_checkerboard_switch, int updates_per_barrier, int iterations,
             int inner_iterations, int shared, int perimeter, int centroid_tracking,
-            int seed, int fixed) {
+            int seed, int fixed, int chemotaxis) {
   DRV(cuCtxSetCurrent(g.ctx));
-  int toggles[7] = {shared ? 1 : 0, 0, perimeter ? 1 : 0, 0, 0, fixed ? 1 : 0,
-                    centroid_tracking ? 1 : 0};
+  int toggles[7] = {shared ? 1 : 0, 0, perimeter ? 1 : 0, 0, chemotaxis ? 1 : 0,
+                    fixed ? 1 : 0, centroid_tracking ? 1 : 0};
   CUfunction f;
   const std::string name = kernel_name(g.ndim, toggles);
   DRV(cuModuleGetFunction(&f, g.mod, name.c_str()));
   int sharedDim = g.ndim == 2 ? 64 : 32;
-  CUdeviceptr field = 0, prefDirs = 0;
+  CUdeviceptr field = g.field, prefDirs = 0;
   bool bsync = block_sync, gsync = global_sync, csync = cell_sync, inside = false;
   bool globalCheckerboard = false;
   int gX = 0, gY = 0, gZ = 0;

@@ -27,11 +27,14 @@ def next_random(seed):
 
 
 def reference_dh(lat, ax, ay, sx, sy, area, perim, J, lam_a, tgt_a, lam_p, tgt_p,
-                 perimeter_on=True, stick=None, s=None):
+                 perimeter_on=True, stick=None, s=None, chemo=None):
     """dH of copying (sx, sy) into (ax, ay) as src/kernels2d.cu:346-519
     computes it: integer adhesion sums (stickiness added to the old
     configuration's, :399-400), double lambda terms.  `s` overrides the
-    source value (the medium that a fixed source type proposes)."""
+    source value (the medium that a fixed source type proposes).  `chemo`
+    is the chemotaxis term (:325-334), computed first; the reference's
+    energy is a float, so with it every addition is rounded to float (the
+    other terms are integers or half-integers, exact either way)."""
     n = lat.shape[0]
     t = int(lat[ay, ax])
     s = int(lat[sy, sx]) if s is None else s
@@ -52,25 +55,30 @@ def reference_dh(lat, ax, ay, sx, sy, area, perim, J, lam_a, tgt_a, lam_p, tgt_p
             nps += v != s
             opt += v != t
             npt += v == t
-    e = float(e_new - e_old)
+    f32 = np.float32
+    e = float(e_new - e_old) if chemo is None else float(f32(f32(chemo) + f32(e_new - e_old)))
     if perimeter_on:
         if s:
             P = int(perim[s & 0xFFFFFF])
             Pn = P - ops + nps
             e += lam_p[ts] * ((Pn - tgt_p[ts]) ** 2 - (P - tgt_p[ts]) ** 2)
+            e = e if chemo is None else float(f32(e))
         if t:
             P = int(perim[t & 0xFFFFFF])
             Pn = P - opt + npt
             e += lam_p[tt] * ((Pn - tgt_p[tt]) ** 2 - (P - tgt_p[tt]) ** 2)
+            e = e if chemo is None else float(f32(e))
     if s:
         e += lam_a[ts] * (1 + 2 * int(area[s & 0xFFFFFF]) - 2 * tgt_a[ts])
+        e = e if chemo is None else float(f32(e))
     if t:
         e += lam_a[tt] * (1 - 2 * int(area[t & 0xFFFFFF]) + 2 * tgt_a[tt])
+        e = e if chemo is None else float(f32(e))
     return e, (nps - ops), (npt - opt)
 
 
 def sequential_run(lat, area, perim, J, lam_a, tgt_a, lam_p, tgt_p, T, seed, mcs,
-                   perimeter_on=True, stick=None, fixed=None):
+                   perimeter_on=True, stick=None, fixed=None, chemo=None, field=None):
     """The reference's one-thread run (in place); returns the accept count.
     fixed (per type): the checks of src/kernels2d.cu:280-290, after the
     id comparison; a fixed source becomes the medium and is still evaluated
@@ -100,8 +108,19 @@ def sequential_run(lat, area, perim, J, lam_a, tgt_a, lam_p, tgt_p, T, seed, mcs
                     continue
                 if fixed[s >> 24]:
                     s = 0
+            chem = None
+            if chemo is not None:
+                # src/kernels2d.cu:302-334: direction from the wrapped
+                # coordinates (float), field at the source, double product
+                lam = chemo[s >> 24] if (s >> 24) else chemo[t >> 24]
+                chem = 0.0
+                if lam != 0:
+                    dx, dy = np.float32(nx - x), np.float32(ny - y)
+                    dl = np.float32(math.sqrt(np.float32(dx * dx + dy * dy)))
+                    dx, dy = np.float32(dx / dl), np.float32(dy / dl)
+                    chem = -lam * (float(dx) * field[0][y, x] + float(dy) * field[1][y, x])
             dH, dps, dpt = reference_dh(lat, nx, ny, x, y, area, perim, J, lam_a, tgt_a,
-                                        lam_p, tgt_p, perimeter_on, stick, s)
+                                        lam_p, tgt_p, perimeter_on, stick, s, chem)
             e = np.float32(dH)
             seed = next_random(seed)
             r = np.float32(seed / M)

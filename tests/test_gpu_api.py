@@ -138,8 +138,11 @@ def test_unsupported_terms_and_bad_arguments(engine_lib):
     sim = gpucpm.Cpm(32, 2, 4, 10, False)
     with pytest.raises(gpucpm.CpmError, match="act"):
         sim.set_constraints(cell_type=1, lambda_act=10, max_act=20)
-    with pytest.raises(gpucpm.CpmError, match="chemotaxis"):
-        sim.set_constraints(cell_type=1, lambda_chemotaxis=1.0)
+    with pytest.raises(gpucpm.CpmError, match="persistence"):
+        sim.set_constraints(cell_type=1, lambda_persistence=1.0, persistence_diffusion=0.5,
+                            persistence_time=10)
+    # chemotaxis needs the field, which exists (zero) once asked for
+    sim.set_constraints(cell_type=1, lambda_chemotaxis=1.0)
     with pytest.raises(gpucpm.CpmError):
         sim.set_constraints(cell_type=40, lambda_area=1, target_area=4)
     with pytest.raises(gpucpm.CpmError):

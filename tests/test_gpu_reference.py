@@ -66,14 +66,16 @@ def test_table_recount_matches_reference(engine_lib, case):
     np.testing.assert_array_equal(perim, rp.astype(np.int32))
 
 
-@pytest.mark.parametrize("D,perimeter,seed,terms", [(16, False, 12345, False),
-                                                    (16, True, 777, False),
-                                                    (32, True, 31337, False),
-                                                    (32, True, 4242, True)])
+@pytest.mark.parametrize("D,perimeter,seed,terms", [(16, False, 12345, None),
+                                                    (16, True, 777, None),
+                                                    (32, True, 31337, None),
+                                                    (32, True, 4242, "fixed_sticky"),
+                                                    (32, False, 2024, "chemotaxis")])
 def test_one_thread_reference_run_equals_restatement(engine_lib, D, perimeter, seed, terms):
     """`terms`: with stickiness and a fixed type (src/kernels2d.cu:280-290,
-    399-400), which the reference applies in its fixed-toggle variant."""
-    nt = 3 if terms else 2
+    399-400), run by the reference's fixed-toggle variant; or with a
+    chemotaxis field (:302-334), run by its chemotaxis-toggle variant."""
+    nt = 3 if terms == "fixed_sticky" else 2
     w = W.random_small((D, D), D * D // 20, ntypes=nt, seed=D + seed % 97, temperature=6.0,
                        perim=perimeter)
     J = np.rint(w.J).astype(int)
@@ -81,15 +83,19 @@ def test_one_thread_reference_run_equals_restatement(engine_lib, D, perimeter, s
     tgt_a = [0] + [20] * nt
     lam_p = ([0.0] + [0.5] * nt) if perimeter else [0.0] * (nt + 1)
     tgt_p = [0] + [18] * nt
-    stick = fixed = None
-    if terms:
+    stick = fixed = chemo = field = None
+    if terms == "fixed_sticky":
         stick = np.zeros((nt + 1, nt + 1), np.float32)
         stick[1, 2], stick[2, 1], stick[1, 0], stick[0, 2] = 3, 2, 4, 1
         fixed = np.array([False, False, False, True])
+    if terms == "chemotaxis":
+        chemo = np.array([0.0, 3.0, -2.0], np.float32)
+        g = np.random.default_rng(seed)
+        field = g.uniform(-2.0, 2.0, (2, D, D))
     wi = W.Workload("one_thread", w.lattice, w.ncells, J.astype(np.float32),
                     np.array(lam_a, np.float32), np.array(tgt_a, np.int32),
                     np.array(lam_p, np.float32), np.array(tgt_p, np.int32), 6.0, 0,
-                    stick=stick, fixed=fixed)
+                    stick=stick, fixed=fixed, chemo=chemo, field=field)
     ref = _ref(wi)
     a0, p0 = ref.tables()
     mcs = 3
@@ -102,7 +108,8 @@ def test_one_thread_reference_run_equals_restatement(engine_lib, D, perimeter, s
     lat = w.lattice.copy()
     area, perim = a0.astype(np.int64), p0.astype(np.int64)
     acc = refmodel.sequential_run(lat, area, perim, J, lam_a, tgt_a, lam_p, tgt_p, 6.0,
-                                  seed, mcs, perimeter_on=perimeter, stick=stick, fixed=fixed)
+                                  seed, mcs, perimeter_on=perimeter, stick=stick, fixed=fixed,
+                                  chemo=chemo, field=field)
     assert acc > 10
     np.testing.assert_array_equal(got, lat)
     np.testing.assert_array_equal(ra.astype(np.int64), area)

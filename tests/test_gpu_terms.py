@@ -128,3 +128,60 @@ def test_set_constraints_fixed_and_stickiness(engine_lib):
     ref = oracle.OracleSim(lat0, 12, J, [0, 2, 2, 0], [0, 60, 60, 0], temperature=10.0,
                            stick=S, fixed=[False, False, False, True]).run(100)
     np.testing.assert_array_equal(sim.get_state().view(np.uint32), ref.lattice)
+
+
+def _smooth_field(shape, seed):
+    g = np.random.default_rng(seed)
+    nd = len(shape)
+    f = np.zeros((nd,) + tuple(shape))
+    grids = np.meshgrid(*[np.arange(n) for n in shape], indexing="ij")
+    for k in range(nd):
+        for _ in range(3):
+            kv = [g.integers(1, 3) * 2 * np.pi / n for n in shape]
+            ph = g.uniform(0, 2 * np.pi)
+            f[k] += g.uniform(0.5, 2.0) * np.sin(sum(a * x for a, x in zip(kv, grids)) + ph)
+    return f
+
+
+@pytest.mark.parametrize("shape,mcs", [((64, 56), 20), ((33, 37), 25), ((14, 12, 15), 5)])
+def test_chemotaxis_matches_oracle(engine_lib, shape, mcs):
+    """The chemotaxis term (src/kernels2d.cu:302-334, src/kernels3d.cu:
+    275-324) against the oracle, bit for bit, including the 2D seam."""
+    w = W.random_small(shape, 30 if len(shape) == 2 else 20, ntypes=2, seed=70 + len(shape),
+                       temperature=8.0)
+    w.chemo = np.array([0.0, 4.0, -2.5], np.float32)
+    w.field = _smooth_field(shape, seed=3)
+    e = make_engine(w, seed=21)
+    e.run_mcs(mcs)
+    finish(e)
+    sim = oracle.OracleSim(w.lattice, w.ncells, **w.oracle_kwargs(), seed=21).run(mcs)
+    assert_same(e, sim)
+    # and the term changes the dynamics
+    w0 = W.random_small(shape, 30 if len(shape) == 2 else 20, ntypes=2, seed=70 + len(shape),
+                        temperature=8.0)
+    plain = oracle.OracleSim(w0.lattice, w0.ncells, **w0.oracle_kwargs(), seed=21).run(mcs)
+    assert (plain.lattice != sim.lattice).any()
+
+
+def test_chemotaxis_moves_cells_up_the_field(engine_lib):
+    """A uniform field along +x with lambda > 0 drives cells toward +x."""
+    import gpucpm
+    drift = {}
+    for lam in (0.0, 20.0):
+        sim = gpucpm.Cpm(128, 2, 4, 10, True)
+        for k in range(4):
+            sim.add_cell(1, 40 + 12 * k, 30 + 20 * k)
+        sim.set_constraints(cell_type=1, lambda_area=5, target_area=80)
+        sim.set_constraints(cell_type=0, other_cell_type=1, adhesion=10)
+        sim.set_constraints(cell_type=1, lambda_chemotaxis=lam)
+        f = sim.get_field()
+        assert f.shape == (2, 128, 128)
+        f[0] = 1.0
+        sim.push_to_gpu()
+        sim.run_mcs(60)
+        sim.synchronize()
+        c0 = sim.get_centroids()[:, 0].copy()
+        sim.run_mcs(300)
+        sim.synchronize()
+        drift[lam] = float(np.mean(sim.get_centroids()[:, 0] - c0))
+    assert drift[20.0] > drift[0.0] + 5.0, drift
