@@ -56,11 +56,18 @@ def parse_args():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--workload", default="tissue_2d",
                    choices=["tissue_2d", "tissue_2d_8192", "tissue_3d", "sorting_2d",
-                            "ensemble", "gradient", "gradient_check"])
+                            "ensemble", "sorting_batch", "gradient", "gradient_check"])
     p.add_argument("--replicas", type=int, default=None,
                    help="replicas of --workload ensemble (256) / gradient (512)")
     p.add_argument("--mcs", type=int, default=None, help="MCS per step")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-loop", action="store_true",
+                   help="batches: skip timing the per-replica launch loop")
+    p.add_argument("--variant", type=int, default=None,
+                   help="tile variant instead of the autotuner's choice (profiling runs: "
+                        "timing under a profiler can change the tuner's pick)")
+    p.add_argument("--dispatch", choices=["grid", "replica"], default=None,
+                   help="batches: dispatch instead of the autotuner's choice")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-reference-gpu", action="store_true",
                    help="skip timing the reference's own CUDA sweep on this GPU")
@@ -345,7 +352,11 @@ def run_ours(args, world, rank, local):
     sim.set_stream(stream.cuda_stream)
     sim.push_to_gpu()
     # the engine's own autotuner picks the tile variant (state is restored)
-    variant, tuned_ms = sim.autotune(probe_mcs=2)
+    if args.variant is None:
+        variant, tuned_ms = sim.autotune(probe_mcs=2)
+    else:
+        sim.set_variant(args.variant)
+        variant, tuned_ms = args.variant, None
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
 
     for _ in range(args.warmup):
@@ -439,12 +450,17 @@ def run_ours(args, world, rank, local):
 
 
 def run_ensemble(args, world, rank, local):
-    """Ragged ensemble: all replicas in one graph-captured persistent launch
+    """Batches: all replicas in one graph-captured persistent launch
     (batched) against the same replicas as a per-replica launch loop.
 
+      ensemble       256 ragged replicas, side log-uniform in [64, 1024],
+                     per-replica parameters (~193 MB of lattice)
+      sorting_batch  512 replicas of the 256x256 two-type sorting lattice
+                     (2600 cells of area 25; the forward of the gradient
+                     workload without scores, 134 MB of lattice)
+
     Each rank runs its own ensemble (replica stream ids offset by rank).  The
-    total lattice (~193 MB for 256 replicas) exceeds L2, so no flush is
-    needed between steps.
+    total lattice exceeds L2, so no flush is needed between steps.
     """
     import numpy as np
     import torch
@@ -454,8 +470,10 @@ def run_ensemble(args, world, rank, local):
 
     torch.cuda.set_device(local)
     gpucpm.set_device(local)
-    nrep = args.replicas or 256
-    ws = W.ensemble_2d(nrep=nrep, seed=3)
+    sorting = args.workload == "sorting_batch"
+    nrep = args.replicas or (512 if sorting else 256)
+    ws = ([W.sorting_grid(n=256, ncells=2600, seed=0)] * nrep if sorting
+          else W.ensemble_2d(nrep=nrep, seed=3))
     mcs = args.mcs or 500
     sizes = [w.lattice.shape[::-1] for w in ws]
     stream = torch.cuda.Stream()
@@ -467,7 +485,15 @@ def run_ensemble(args, world, rank, local):
     b.set_seed(0, rank * nrep)
     b.set_stream(stream.cuda_stream)
     b.push_to_gpu()
-    variant, tuned_ms = b.autotune(probe_mcs=2)
+    if args.variant is None and args.dispatch is None:
+        variant, tuned_ms = b.autotune(probe_mcs=2)
+    else:
+        if args.variant is not None:
+            b.set_variant(args.variant)
+        if args.dispatch is not None:
+            b.set_dispatch(gpucpm.DISPATCH_REPLICA if args.dispatch == "replica"
+                           else gpucpm.DISPATCH_GRID)
+        variant, tuned_ms = b.sweep_config()["variant"], None
     for _ in range(args.warmup):
         b.run_graph(mcs)
     b.synchronize()
@@ -494,30 +520,32 @@ def run_ensemble(args, world, rank, local):
 
     # The same replicas as a per-replica launch loop: one single-lattice
     # engine per replica, launched back to back on one stream.
-    engines = []
-    for r, w in enumerate(ws):
-        n = w.lattice.shape
-        e = gpucpm.create_box(n[1], n[0], 1, 2, w.ncells, w.temperature)
-        e.lattice(0)[...] = w.lattice.view(np.int32)
-        w.apply(e, replica=0)
-        e.set_seed(0, rank * nrep + r)
-        e.set_stream(stream.cuda_stream)
-        e.push_to_gpu()
-        engines.append(e)
-    for e in engines:
-        e.run_mcs(2)  # warm-up
-    torch.cuda.synchronize()
-    t0 = torch.cuda.Event(enable_timing=True)
-    t1 = torch.cuda.Event(enable_timing=True)
-    with torch.cuda.stream(stream):
-        t0.record(stream)
+    loop_ms = None
+    engines = [] if not args.no_loop else None
+    if engines is not None:
+        for r, w in enumerate(ws):
+            n = w.lattice.shape
+            e = gpucpm.create_box(n[1], n[0], 1, 2, w.ncells, w.temperature)
+            e.lattice(0)[...] = w.lattice.view(np.int32)
+            w.apply(e, replica=0)
+            e.set_seed(0, rank * nrep + r)
+            e.set_stream(stream.cuda_stream)
+            e.push_to_gpu()
+            engines.append(e)
         for e in engines:
-            e.run_mcs(mcs)
-        t1.record(stream)
-    for e in engines:
-        e.synchronize()
-    torch.cuda.synchronize()
-    loop_ms = dist_max(world, t0.elapsed_time(t1) / 1e3) * 1e3
+            e.run_mcs(2)  # warm-up
+        torch.cuda.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            t0.record(stream)
+            for e in engines:
+                e.run_mcs(mcs)
+            t1.record(stream)
+        for e in engines:
+            e.synchronize()
+        torch.cuda.synchronize()
+        loop_ms = dist_max(world, t0.elapsed_time(t1) / 1e3) * 1e3
 
     if rank != 0:
         return
@@ -527,11 +555,16 @@ def run_ensemble(args, world, rank, local):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": batched_ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "u32+f32", "data": "synthetic (seeded Voronoi replicas)",
-            "config": {"workload": f"ensemble_2d {nrep} replicas, side log-uniform "
-                                   f"[64,1024] ({min(side)}..{max(side)}), cells = side^2/50, "
-                                   "per-replica J~U[2,20], lambda~U[0.5,2], T~U[5,30]",
+            "dtype": "u32+f32",
+            "data": "synthetic (seeded sorting grid)" if sorting else
+                    "synthetic (seeded Voronoi replicas)",
+            "config": {"workload": (f"sorting_batch {nrep} replicas of sorting_grid 256x256, "
+                                    "2600 cells of target area 25" if sorting else
+                                    f"ensemble_2d {nrep} replicas, side log-uniform "
+                                    f"[64,1024] ({min(side)}..{max(side)}), cells = side^2/50, "
+                                    "per-replica J~U[2,20], lambda~U[0.5,2], T~U[5,30]"),
                        "sites": sites, "mcs_per_step": mcs, "tile_variant": variant,
+                       "dispatch": b.sweep_config()["dispatch"],
                        "l2": "inputs larger than L2 (no flush)", "seed": 0},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak,
@@ -539,10 +572,10 @@ def run_ensemble(args, world, rank, local):
                          "algorithmic_bytes_per_launch": BYTES_PER_ATTEMPT * sites * mcs,
                          "kernel": "sweep_kernel (one graph-captured launch per step)"},
             "gpu_launches": int(launches),
-            "batched_vs_loop": {"batched_ms": batched_ms, "loop_ms": loop_ms,
-                                "speedup": loop_ms / batched_ms,
-                                "loop": "one single-lattice engine per replica, "
-                                        "launched back to back on one stream"},
+            "batched_vs_loop": None if loop_ms is None else {
+                "batched_ms": batched_ms, "loop_ms": loop_ms, "speedup": loop_ms / batched_ms,
+                "loop": "one single-lattice engine per replica, launched back to back "
+                        "on one stream"},
             "autotune": {"variant": variant, "probe_ms_per_mcs": tuned_ms},
             "step_ms": step_ms, "e2e": None}
     print(json.dumps(line), flush=True)
@@ -672,7 +705,7 @@ def main():
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
-    elif args.workload == "ensemble":
+    elif args.workload in ("ensemble", "sorting_batch"):
         run_ensemble(args, world, rank, local)
     elif args.workload in ("gradient", "gradient_check"):
         run_gradient(args, world, rank, local)
