@@ -55,6 +55,48 @@ __device__ __forceinline__ float exp_neg(float x) {
   return __fmul_rn(p, __int_as_float((k + 127) << 23));
 }
 
+// log2(v) for v >= 1 in FP32 (act model): v = m 2^e with m in
+// [1/sqrt(2), sqrt(2)); log2(m) = (2 / ln 2) atanh(z), z = (m - 1)/(m + 1),
+// |z| <= 0.1716, by the odd series z + z^3/3 + ... + z^11/11 in Horner form.
+// About 1 ulp from the exact value; the oracle repeats it step for step.
+__device__ __forceinline__ float log2_pos(float v) {
+  const unsigned b = __float_as_uint(v);
+  int e = (int)((b >> 23) & 0xFFu) - 127;
+  float m = __uint_as_float((b & 0x7FFFFFu) | (127u << 23));
+  if (m > 1.41421356f) {
+    m = __fmul_rn(m, 0.5f);
+    e += 1;
+  }
+  const float z = __fdiv_rn(__fsub_rn(m, 1.0f), __fadd_rn(m, 1.0f));
+  const float z2 = __fmul_rn(z, z);
+  float p = __fdiv_rn(1.0f, 11.0f);
+  p = __fmaf_rn(p, z2, __fdiv_rn(1.0f, 9.0f));
+  p = __fmaf_rn(p, z2, __fdiv_rn(1.0f, 7.0f));
+  p = __fmaf_rn(p, z2, 0.2f);
+  p = __fmaf_rn(p, z2, __fdiv_rn(1.0f, 3.0f));
+  p = __fmaf_rn(p, z2, 1.0f);
+  return __fadd_rn((float)e, __fmul_rn(__fmul_rn(z, p), 2.8853900817779268f));
+}
+
+// 2^y in FP32 for y in [-126, 127] (act model): y = k + f, |f| <= 1/2;
+// 2^f = e^r with r = f ln 2 (ln 2 in two parts), by the Taylor series to
+// degree 7; 2^k applied through the exponent field.
+__device__ __forceinline__ float exp2_own(float y) {
+  const float kf = rintf(y);
+  const float f = __fsub_rn(y, kf);
+  const float r = __fmaf_rn(f, 0x1.62e430p-1f, __fmul_rn(f, -0x1.05c610p-29f));
+  float p = __fdiv_rn(1.0f, 5040.0f);
+  p = __fmaf_rn(p, r, __fdiv_rn(1.0f, 720.0f));
+  p = __fmaf_rn(p, r, __fdiv_rn(1.0f, 120.0f));
+  p = __fmaf_rn(p, r, __fdiv_rn(1.0f, 24.0f));
+  p = __fmaf_rn(p, r, __fdiv_rn(1.0f, 6.0f));
+  p = __fmaf_rn(p, r, 0.5f);
+  p = __fmaf_rn(p, r, 1.0f);
+  p = __fmaf_rn(p, r, 1.0f);
+  const int k = (int)kf;
+  return __fmul_rn(p, __int_as_float((k + 127) << 23));
+}
+
 // Checkerboard classes along one axis of length n: class 0 holds the even
 // coordinates below n - (n & 1), class 1 the odd ones, class 2 the last
 // coordinate of an odd axis.  An axis of length 1 (z in 2D) has one class.

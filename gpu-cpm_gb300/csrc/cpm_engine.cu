@@ -60,6 +60,14 @@ struct cpm_handle {
   // reference keeps them, device floats; layout of SweepArgs::field
   std::vector<double> h_field;
   float* d_field = nullptr;
+  // act model (allocated on first use): MCS of the last copy into each site,
+  // and the per-block lists of copies deferred to the end of their phase
+  std::vector<uint32_t> h_act;
+  uint32_t* d_act = nullptr;
+  unsigned long long* d_pend_site = nullptr;
+  uint32_t* d_pend_val = nullptr;
+  long long pend_entries = 0;  // capacity of the pending arrays (all blocks)
+  bool act_active = false;     // some replica's record has an act lambda
   uint32_t* d_lat = nullptr;
   unsigned long long* d_ap[2] = {nullptr, nullptr};  // packed (area, perimeter)
   long long* d_cs[2] = {nullptr, nullptr};
@@ -148,6 +156,9 @@ void free_all(cpm_handle* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   cudaFreeHost(h->h_lat);
   cudaFree(h->d_field);
+  cudaFree(h->d_act);
+  cudaFree(h->d_pend_site);
+  cudaFree(h->d_pend_val);
   cudaFree(h->d_lat);
   for (int b = 0; b < 2; ++b) {
     cudaFree(h->d_ap[b]);
@@ -350,6 +361,8 @@ int build_engine(int n, int ndim, const int* nx, const int* ny, const int* nz,
     c.list_cap_local = n > 1 ? 2LL * nt * max_rep_tiles : 0;  // batches only
     dlist_entries = std::max(dlist_entries, c.list_cap_local * 2 * c.grid_local);
   }
+  // act runs defer one copy per attempt at most: half a dirty list's entries
+  h->pend_entries = dlist_entries / 4 + 1;
   e = cudaMalloc((void**)&h->d_dlist, sizeof(uint32_t) * dlist_entries);
   if (e != cudaSuccess) {
     g_create_error = std::string("dirty-list allocation failed: ") + cudaGetErrorString(e);
@@ -485,6 +498,26 @@ int read_error_word(cpm_handle* h, uint32_t* word) {
   return CPM_OK;
 }
 
+// The act lattice (zeros) and the pending lists, on first use.
+int ensure_act(cpm_handle* h) {
+  if (!h->d_act) {
+    const size_t n = (size_t)h->total_sites;
+    try {
+      h->h_act.assign(n, 0u);
+    } catch (...) {
+      return h->fail(CPM_ERR_ALLOC, "host act lattice allocation failed");
+    }
+    CPM_CUDA(h, cudaMalloc((void**)&h->d_act, sizeof(uint32_t) * (n ? n : 1)));
+    CPM_CUDA(h, cudaMemsetAsync(h->d_act, 0, sizeof(uint32_t) * (n ? n : 1), h->stream));
+  }
+  if (!h->d_pend_site) {
+    CPM_CUDA(h, cudaMalloc((void**)&h->d_pend_site,
+                           sizeof(unsigned long long) * h->pend_entries));
+    CPM_CUDA(h, cudaMalloc((void**)&h->d_pend_val, sizeof(uint32_t) * h->pend_entries));
+  }
+  return CPM_OK;
+}
+
 int upload_params(cpm_handle* h) {
   if (!h->params_dirty && !h->reps_dirty) return CPM_OK;
   // Drop records no replica uses and renumber the rest.
@@ -517,6 +550,21 @@ int upload_params(cpm_handle* h) {
     if (p.chemo_on && !h->d_field)
       return h->fail(CPM_ERR_STATE, "chemotaxis is set but the engine has no field "
                                     "(create it with the field flag or call cpm_host_field_r)");
+    p.act_on = 0;
+    for (int k = 0; k < kMaxTypes; ++k)
+      if (p.act_lambda[k] != 0.0f) p.act_on = 1;
+  }
+  bool act = false;
+  for (const auto& p : h->psets) act = act || p.act_on;
+  if (act) {
+    if (int rc = ensure_act(h)) return rc;
+  }
+  if (act != h->act_active) {  // another kernel, other arguments
+    h->act_active = act;
+    if (h->graph_exec) {
+      cudaGraphExecDestroy(h->graph_exec);
+      h->graph_exec = nullptr;
+    }
   }
   if (m > h->params_cap) {
     CPM_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -550,6 +598,7 @@ bool any_perimeter(const cpm_handle* h) {
 // Kernel arguments of a sweep with tile variant v and dispatch d (tick0 /
 // mcs filled in by the caller).
 SweepArgs sweep_args(const cpm_handle* h, int v, int d) {
+  if (h->act_active) v = 0;  // the act kernels exist for tile variant 0
   SweepArgs a;
   std::memset(&a, 0, sizeof a);
   a.lat = h->d_lat;
@@ -563,6 +612,11 @@ SweepArgs sweep_args(const cpm_handle* h, int v, int d) {
   a.dlist = h->d_dlist;
   a.block_local = d == CPM_DISPATCH_REPLICA ? 1 : 0;
   a.field = h->d_field;
+  a.act = h->d_act;
+  a.act_on = h->act_active ? 1 : 0;
+  a.pend_site = h->d_pend_site;
+  a.pend_val = h->d_pend_val;
+  a.pend_cap = (d == CPM_DISPATCH_REPLICA ? c.list_cap_local : c.list_cap) / 2;
   a.list_cap = a.block_local ? c.list_cap_local : c.list_cap;
   a.rep_order = h->d_rep_order;
   a.ctl = h->d_ctl;
@@ -579,6 +633,7 @@ SweepArgs sweep_args(const cpm_handle* h, int v, int d) {
 }
 
 int grid_of(const cpm_handle* h, int v, int d) {
+  if (h->act_active) v = 0;
   return d == CPM_DISPATCH_REPLICA ? h->cfg[v].grid_local : h->cfg[v].grid;
 }
 
@@ -610,8 +665,8 @@ extern "C" {
 
 int cpm_create(int dimension, int dimensionality, int number_of_cells,
                float temperature, int flags, cpm_handle** out) {
-  if (flags & ~CPM_FLAG_FIELD) {
-    g_create_error = "unknown flags (only CPM_FLAG_FIELD is supported; act lattices are not)";
+  if (flags & ~(CPM_FLAG_FIELD | CPM_FLAG_ACT)) {
+    g_create_error = "unknown flags (CPM_FLAG_FIELD and CPM_FLAG_ACT are the flags)";
     if (out) *out = nullptr;
     return CPM_ERR_UNSUPPORTED;
   }
@@ -620,6 +675,14 @@ int cpm_create(int dimension, int dimensionality, int number_of_cells,
                               &number_of_cells, temperature, out);
   if (rc == CPM_OK && (flags & CPM_FLAG_FIELD)) {
     if (int rc2 = cpm_host_field_r(*out, 0, nullptr, nullptr)) {
+      g_create_error = cpm_last_error(*out);
+      cpm_destroy(*out);
+      *out = nullptr;
+      return rc2;
+    }
+  }
+  if (rc == CPM_OK && (flags & CPM_FLAG_ACT)) {
+    if (int rc2 = cpm_host_act_r(*out, 0, nullptr, nullptr)) {
       g_create_error = cpm_last_error(*out);
       cpm_destroy(*out);
       *out = nullptr;
@@ -736,6 +799,17 @@ int cpm_host_field_r(cpm_handle* h, int r, double** ptr, int64_t* nvalues) {
 }
 
 namespace {
+int set_act(cpm_handle* h, int r, int type, int max_act, float lambda) {
+  if (!h) return CPM_ERR_INVALID;
+  if (int rc = check_type(h, type)) return rc;
+  if (!std::isfinite(lambda)) return h->fail(CPM_ERR_INVALID, "lambda must be finite");
+  if (max_act < 0) return h->fail(CPM_ERR_INVALID, "max_act must be >= 0");
+  return for_replicas(h, r, [&](DevParams& p) {
+    p.act_max[type] = max_act;
+    p.act_lambda[type] = lambda;
+  });
+}
+
 int set_chemotaxis(cpm_handle* h, int r, int type, float lambda) {
   if (!h) return CPM_ERR_INVALID;
   if (int rc = check_type(h, type)) return rc;
@@ -743,6 +817,26 @@ int set_chemotaxis(cpm_handle* h, int r, int type, float lambda) {
   return for_replicas(h, r, [&](DevParams& p) { p.chemo[type] = lambda; });
 }
 }  // namespace
+int cpm_host_act_r(cpm_handle* h, int r, uint32_t** ptr, int64_t* nsites) {
+  if (int rc = check_replica(h, r)) return rc;
+  CPM_BIND(h);
+  if (int rc = ensure_act(h)) return rc;
+  const DevReplica& R = h->reps[r];
+  if (ptr) *ptr = h->h_act.data() + R.lat_off;
+  if (nsites) *nsites = (int64_t)R.nx * R.ny * R.nz;
+  return CPM_OK;
+}
+int cpm_has_act(const cpm_handle* h, int* has) {
+  if (!h || !has) return CPM_ERR_INVALID;
+  *has = h->d_act ? 1 : 0;
+  return CPM_OK;
+}
+int cpm_set_act(cpm_handle* h, int type, int max_act, float lambda) {
+  return set_act(h, -1, type, max_act, lambda);
+}
+int cpm_set_act_r(cpm_handle* h, int r, int type, int max_act, float lambda) {
+  return set_act(h, r < 0 ? -2 : r, type, max_act, lambda);
+}
 int cpm_set_chemotaxis(cpm_handle* h, int type, float lambda) {
   return set_chemotaxis(h, -1, type, lambda);
 }
@@ -806,6 +900,9 @@ int cpm_push(cpm_handle* h) {
   h->pushed = false;
   CPM_CUDA(h, cudaMemcpyAsync(h->d_lat, h->h_lat, sizeof(uint32_t) * h->total_sites,
                               cudaMemcpyHostToDevice, h->stream));
+  if (h->d_act)  // act stamps go along (src/cpm.cu:547-549)
+    CPM_CUDA(h, cudaMemcpyAsync(h->d_act, h->h_act.data(), sizeof(uint32_t) * h->total_sites,
+                                cudaMemcpyHostToDevice, h->stream));
   if (h->d_field) {  // the field goes along, as in Cpm::moveCellIdsToGpu
     std::vector<float> f(h->h_field.begin(), h->h_field.end());
     CPM_CUDA(h, cudaMemcpyAsync(h->d_field, f.data(), sizeof(float) * f.size(),
@@ -909,6 +1006,9 @@ int cpm_pull(cpm_handle* h) {
   CPM_BIND(h);
   CPM_CUDA(h, cudaMemcpyAsync(h->h_lat, h->d_lat, sizeof(uint32_t) * h->total_sites,
                               cudaMemcpyDeviceToHost, h->stream));
+  if (h->d_act)  // and the act stamps (src/cpm.cu:534-536)
+    CPM_CUDA(h, cudaMemcpyAsync(h->h_act.data(), h->d_act, sizeof(uint32_t) * h->total_sites,
+                                cudaMemcpyDeviceToHost, h->stream));
   CPM_CUDA(h, cudaStreamSynchronize(h->stream));
   return CPM_OK;
 }
@@ -1003,14 +1103,17 @@ int cpm_autotune(cpm_handle* h, int probe_mcs, int* chosen, float* ms_per_mcs) {
   const size_t ap_b = sizeof(unsigned long long) * h->rows;
   const size_t cs_b = sizeof(long long) * h->rows * h->ndim;
   const size_t cnt_b = sizeof(unsigned long long) * 2 * h->nrep;
+  const size_t act_b = h->d_act ? lat_b : 0;  // act stamps, when kept
   char* save = nullptr;
-  CPM_CUDA(h, cudaMalloc(&save, lat_b + ap_b + cs_b + cnt_b));
+  CPM_CUDA(h, cudaMalloc(&save, lat_b + ap_b + cs_b + cnt_b + act_b));
   auto copy = [&](bool to_save) -> cudaError_t {
     char* p = save;
-    void* dst[4] = {p, p + lat_b, p + lat_b + ap_b, p + lat_b + ap_b + cs_b};
-    void* src[4] = {h->d_lat, h->d_ap[0], h->d_cs[0], h->d_counters};
-    const size_t n[4] = {lat_b, ap_b, cs_b, cnt_b};
-    for (int i = 0; i < 4; ++i) {
+    void* dst[5] = {p, p + lat_b, p + lat_b + ap_b, p + lat_b + ap_b + cs_b,
+                    p + lat_b + ap_b + cs_b + cnt_b};
+    void* src[5] = {h->d_lat, h->d_ap[0], h->d_cs[0], h->d_counters, h->d_act};
+    const size_t n[5] = {lat_b, ap_b, cs_b, cnt_b, act_b};
+    for (int i = 0; i < 5; ++i) {
+      if (!n[i]) continue;
       cudaError_t e = to_save ? cudaMemcpyAsync(dst[i], src[i], n[i], cudaMemcpyDeviceToDevice, h->stream)
                               : cudaMemcpyAsync(src[i], dst[i], n[i], cudaMemcpyDeviceToDevice, h->stream);
       if (e != cudaSuccess) return e;
@@ -1093,6 +1196,9 @@ int cpm_run_scores(cpm_handle* h, int mcs, float* d_scores, uint64_t score_base,
       return h->fail(CPM_ERR_INVALID, "cpm_run_scores: score types must be < %d", kScoreTypes);
   if (mcs == 0) return CPM_OK;
   if (int rc = upload_params(h)) return rc;
+  if (h->act_active)
+    return h->fail(CPM_ERR_UNSUPPORTED, "cpm_run_scores: scores of runs with the act term "
+                                        "are not supported");
   SweepArgs a = sweep_args(h, h->variant, h->dispatch);
   a.scores = d_scores;
   a.score_base = score_base;

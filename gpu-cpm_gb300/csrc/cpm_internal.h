@@ -116,7 +116,11 @@ struct DevParams {
   // unit copy direction (src/kernels2d.cu:302-334, src/kernels3d.cu:275-324)
   float chemo[kMaxTypes];
   int chemo_on;         // any chemo != 0
-  int pad[3];
+  // act model (src/kernels2d.cu:312-473): lambda and max_act per type
+  int act_on;           // any act_lambda != 0
+  int pad[2];
+  float act_lambda[kMaxTypes];
+  int act_max[kMaxTypes];
 };
 
 struct DevReplica {
@@ -182,6 +186,16 @@ struct SweepArgs {
   // chemotaxis field, float: replica r's component k of site i at
   // field[ndim * lat_off + k * sites_r + i] (null when no field exists)
   const float* field;
+  // Act model: act[i] = the MCS of the last copy into site i.  With act_on
+  // (some record has an act lambda) every accepted copy is deferred: it goes
+  // to the block's pending list (site, value) and is written, with its act
+  // stamp, after the phase's barrier, so that an attempt's reads around its
+  // source (other targets of the slot) see the phase's starting state.
+  uint32_t* act;
+  int act_on;
+  unsigned long long* pend_site;
+  uint32_t* pend_val;
+  long long pend_cap;  // entries of one block's pending list
   // Monte Carlo time of the first MCS: tick0, or *tick_ptr when tick_ptr is
   // set (graph replays); in the latter case block 0 advances *tick_ptr by
   // mcs when the launch ends.

@@ -154,10 +154,16 @@ SweepShape shape_of() {
 // the wrapped coordinates in 2D (src/kernels2d.cu:302-309) and the nearest
 // image in 3D (src/kernels3d.cu:275-299).  F: the replica's field, `sites`
 // values per component.
+__device__ __forceinline__ int wrap_coord(int v, int n) {
+  return v < 0 ? v + n : (v >= n ? v - n : v);
+}
+
+// Coordinates of the source of an attempt: neighbour `kdir` (the order of
+// Stage::nb_offset) of the target (x, y, z), wrapped.
 template <int NDIM>
-__device__ __forceinline__ float chemo_dot(const float* F, long long sites, int x, int y,
-                                           int z, int kdir, int nx, int ny, int nz) {
-  int ox, oy, oz;  // source offset from the target, neighbour order of Stage
+__device__ __forceinline__ void source_coords(int kdir, int x, int y, int z, int nx, int ny,
+                                              int nz, int& sx, int& sy, int& sz) {
+  int ox, oy, oz;
   if (NDIM == 2) {
     const int m = kdir + (kdir >= 4);
     oz = 0;
@@ -169,8 +175,16 @@ __device__ __forceinline__ float chemo_dot(const float* F, long long sites, int 
     oy = (m / 3) % 3 - 1;
     ox = m % 3 - 1;
   }
-  auto wrapc = [](int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); };
-  const int sx = wrapc(x + ox, nx), sy = wrapc(y + oy, ny), sz = NDIM == 3 ? wrapc(z + oz, nz) : 0;
+  sx = wrap_coord(x + ox, nx);
+  sy = wrap_coord(y + oy, ny);
+  sz = NDIM == 3 ? wrap_coord(z + oz, nz) : 0;
+}
+
+template <int NDIM>
+__device__ __forceinline__ float chemo_dot(const float* F, long long sites, int x, int y,
+                                           int z, int kdir, int nx, int ny, int nz) {
+  int sx, sy, sz;
+  source_coords<NDIM>(kdir, x, y, z, nx, ny, nz, sx, sy, sz);
   int dx = x - sx, dy = y - sy, dz = z - sz;
   if (NDIM == 3) {
     if (dx > nx / 2) dx -= nx;
@@ -190,6 +204,37 @@ __device__ __forceinline__ float chemo_dot(const float* F, long long sites, int 
   c = __fmaf_rn(__fdiv_rn(fy, len), __ldg(F + sites + site), c);
   if (NDIM == 3) c = __fmaf_rn(__fdiv_rn(fz, len), __ldg(F + 2 * sites + site), c);
   return c;
+}
+
+// Act model (src/kernels2d.cu:338-473, src/kernels3d.cu:347-470): the
+// geometric mean of max(amax + act[i] - tick, 0) over site (x, y, z) and
+// those of its neighbours that hold `id`, as exp2 of the mean log2 (own
+// log2_pos / exp2_own, summed in neighbour order); 0 when a factor is 0.
+// L and A are the replica's lattice and act stamps, read as they stood when
+// the phase began (copies of an act run are written after the phase).
+template <int NDIM>
+__device__ __forceinline__ float act_mean(const uint32_t* L, const uint32_t* A, int x, int y,
+                                          int z, int nx, int ny, int nz, uint32_t id, int amax,
+                                          long long tick) {
+  auto at = [&](int xx, int yy, int zz) { return ((long long)zz * ny + yy) * nx + xx; };
+  const long long a0 = (long long)amax + (long long)__ldcg(A + at(x, y, z)) - tick;
+  if (a0 <= 0) return 0.0f;
+  float sum = log2_pos((float)a0);
+  int count = 1;
+  const int zlo = NDIM == 3 ? -1 : 0, zhi = NDIM == 3 ? 1 : 0;
+  for (int dz = zlo; dz <= zhi; ++dz)
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dx = -1; dx <= 1; ++dx) {
+        if (!dz && !dy && !dx) continue;
+        const long long n = at(wrap_coord(x + dx, nx), wrap_coord(y + dy, ny),
+                               NDIM == 3 ? wrap_coord(z + dz, nz) : 0);
+        if (__ldcg(L + n) != id) continue;
+        const long long v = (long long)amax + (long long)__ldcg(A + n) - tick;
+        if (v <= 0) return 0.0f;
+        sum = __fadd_rn(sum, log2_pos((float)v));
+        ++count;
+      }
+  return exp2_own(__fdiv_rn(sum, (float)count));
 }
 
 // Per-phase view of the double-buffered tables.
@@ -271,7 +316,10 @@ __device__ __forceinline__ void flush_scores(const SweepArgs& a, float* sc, int 
   for (int k = 0; k < kScoreRegs; ++k) sc[k] = 0.0f;
 }
 
-template <int NDIM, bool PERIM, int V, bool SCORE>
+// ACT: the act-model instantiation (variant 0, no scores): act term, and
+// every accepted copy deferred to the end of its phase.  Kept apart so that
+// the other kernels carry none of its registers.
+template <int NDIM, bool PERIM, int V, bool SCORE, bool ACT = false>
 __global__ void __launch_bounds__(kSweepThreadsMax, 1)
     sweep_kernel(const SweepArgs a) {
   using G = TileGeom<NDIM, V>;
@@ -284,6 +332,7 @@ __global__ void __launch_bounds__(kSweepThreadsMax, 1)
   __shared__ unsigned s_cnt[2];
   __shared__ unsigned long long s_tick0;
   __shared__ int s_claim;
+  __shared__ unsigned s_pend;  // (act runs) entries on this block's pending list
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int wpb = blockDim.x >> 5;  // warps (tiles in flight) per block
@@ -305,6 +354,7 @@ __global__ void __launch_bounds__(kSweepThreadsMax, 1)
   int sc_rep = -1;
   unsigned long long sc_tick = 0;
   if (tid < 2) s_cnt[tid] = 0;
+  if (tid == 0) s_pend = 0;
   // Every block reads *tick_ptr before its first barrier arrival, and block
   // 0 advances it only after its last barrier, so all blocks see one value.
   if (tid == 0) s_tick0 = a.tick_ptr ? __ldcg(a.tick_ptr) : a.tick0;
@@ -332,6 +382,18 @@ __global__ void __launch_bounds__(kSweepThreadsMax, 1)
                  prv ? a.cs[1] : a.cs[0]);
   };
 
+  // (act runs) the phase's deferred copies and their act stamps, written by
+  // the block that made them; callers put a barrier before and after.
+  auto apply_pending = [&](unsigned long long tick) {
+    const unsigned n = min(s_pend, (unsigned)a.pend_cap);  // see kErrListFull
+    const long long base = (long long)blockIdx.x * a.pend_cap;
+    for (unsigned j = tid; j < n; j += blockDim.x) {
+      const unsigned long long site = __ldcg(a.pend_site + base + j);
+      a.lat[site] = __ldcg(a.pend_val + base + j);
+      a.act[site] = (uint32_t)tick;
+    }
+  };
+
   // One warp tile of replica r (its `local`-th tile of the slot): stage the
   // tile, then boundary test, source pick and dH / test / commit.
   auto run_tile = [&](const PhaseTables<NDIM>& pt, const int r, const int local,
@@ -354,6 +416,7 @@ __global__ void __launch_bounds__(kSweepThreadsMax, 1)
     const unsigned fixed_mask = __ldg(&P->fixed_mask);
     const bool stick_on = __ldg(&P->stick_on) != 0;
     const bool chemo_on = __ldg(&P->chemo_on) != 0;
+    const bool act_rec = ACT && __ldg(&P->act_on) != 0;
     const int nx = __ldg(&a.reps[r].nx), ny = __ldg(&a.reps[r].ny),
               nz = __ldg(&a.reps[r].nz), ncells = __ldg(&a.reps[r].ncells);
     const long long lat_off = __ldg(&a.reps[r].lat_off);
@@ -536,6 +599,32 @@ __global__ void __launch_bounds__(kSweepThreadsMax, 1)
                                                           z, kdir, nx, ny, nz));
               }
             }
+            // act next: lambda and max of the target type, of the source type
+            // for a medium target
+            if (ACT && act_rec) {  // uniform over the tile
+              const int ta = tt ? tt : ts;
+              const float lam = __ldg(&P->act_lambda[ta]);
+              const int amax_a = __ldg(&P->act_max[ta]);
+              if (lam != 0.0f && amax_a != 0) {
+                const int qx = q % G::CX, qy = (q / G::CX) % G::CY,
+                          qz = q / (G::CX * G::CY);
+                const int x = class_coord(nx, cx, i0 + qx);
+                const int y = class_coord(ny, cy, j0 + qy);
+                const int z = NDIM == 3 ? class_coord(nz, cz, l0 + qz) : 0;
+                int sx, sy, sz;
+                source_coords<NDIM>(kdir, x, y, z, nx, ny, nz, sx, sy, sz);
+                const uint32_t* A = a.act + lat_off;
+                const long long tk = (long long)tick;
+                const float tgt = t ? act_mean<NDIM>(L, A, x, y, z, nx, ny, nz, t,
+                                                     __ldg(&P->act_max[tt]), tk)
+                                    : 0.0f;
+                const float src = s ? act_mean<NDIM>(L, A, sx, sy, sz, nx, ny, nz, s,
+                                                     __ldg(&P->act_max[ts]), tk)
+                                    : 0.0f;
+                chemo = __fadd_rn(chemo, __fmul_rn(__fdiv_rn(-lam, (float)amax_a),
+                                                   __fsub_rn(src, tgt)));
+              }
+            }
             dH = __fadd_rn(chemo, dH);
           }
           const int dps = NB - 2 * cnt_s;
@@ -624,7 +713,19 @@ __global__ void __launch_bounds__(kSweepThreadsMax, 1)
             const int x = class_coord(nx, cx, i0 + qx);
             const int y = class_coord(ny, cy, j0 + qy);
             const int z = NDIM == 3 ? class_coord(nz, cz, l0 + qz) : 0;
-            L[((long long)z * ny + y) * nx + x] = s;
+            const long long site = ((long long)z * ny + y) * nx + x;
+            if (ACT) {  // written after the phase
+              const unsigned j = atomicAdd(&s_pend, 1u);
+              if ((long long)j < a.pend_cap) {
+                const long long e = (long long)blockIdx.x * a.pend_cap + j;
+                a.pend_site[e] = (unsigned long long)(lat_off + site);
+                a.pend_val[e] = s;
+              } else {
+                atomicOr(err, kErrListFull);  // reported, never written past the end
+              }
+            } else {
+              L[site] = s;
+            }
             const int crd[3] = {x, y, z};
             const int dim[3] = {nx, ny, nz};
             long long img[NDIM];
@@ -696,6 +797,12 @@ __global__ void __launch_bounds__(kSweepThreadsMax, 1)
         __syncthreads();
         if (tid == 0) s_cnt[prv] = 0;
         if (!grid_barrier(a.ctl, ++episode, &s_ok)) return;
+        if (ACT) {  // the slot's copies land before the next slot reads
+          apply_pending(tick);
+          __syncthreads();
+          if (tid == 0) s_pend = 0;
+          if (!grid_barrier(a.ctl, ++episode, &s_ok)) return;
+        }
       }
     }
     // Final replay: the last phase's deltas into the copy it read, so that
@@ -730,6 +837,11 @@ __global__ void __launch_bounds__(kSweepThreadsMax, 1)
             run_tile(pt, r, local, cx, cy, cz, tick, phase);
           __syncthreads();
           if (tid == 0) s_cnt[prv] = 0;
+          if (ACT) {
+            apply_pending(tick);
+            __syncthreads();
+            if (tid == 0) s_pend = 0;
+          }
           __syncthreads();
         }
       }
@@ -835,7 +947,12 @@ __global__ void barrier_probe(uint32_t* ctl, unsigned long long timeout_ns) {
 }
 
 template <int NDIM, int V>
-const void* sweep_fn_v(bool perim, bool scores) {
+const void* sweep_fn_v(bool perim, bool scores, bool act) {
+  if constexpr (V == 0) {
+    if (act)
+      return perim ? (const void*)sweep_kernel<NDIM, true, 0, false, true>
+                   : (const void*)sweep_kernel<NDIM, false, 0, false, true>;
+  }
   if constexpr (NDIM == 2) {
     if (scores)
       return perim ? (const void*)sweep_kernel<NDIM, true, V, true>
@@ -845,19 +962,21 @@ const void* sweep_fn_v(bool perim, bool scores) {
                : (const void*)sweep_kernel<NDIM, false, V, false>;
 }
 
-// Score launches exist for 2D lattices (the differentiable ensembles).
-const void* sweep_fn(int ndim, bool perim, int variant, bool scores) {
+// Score launches exist for 2D lattices (the differentiable ensembles), act
+// launches for variant 0 without scores (the engine sees to both).
+const void* sweep_fn(int ndim, bool perim, int variant, bool scores, bool act) {
+  if (act) variant = 0;
   if (ndim == 2) {
     switch (variant) {
-      case 1: return sweep_fn_v<2, 1>(perim, scores);
-      case 2: return sweep_fn_v<2, 2>(perim, scores);
-      default: return sweep_fn_v<2, 0>(perim, scores);
+      case 1: return sweep_fn_v<2, 1>(perim, scores, false);
+      case 2: return sweep_fn_v<2, 2>(perim, scores, false);
+      default: return sweep_fn_v<2, 0>(perim, act ? false : scores, act);
     }
   }
   switch (variant) {
-    case 1: return sweep_fn_v<3, 1>(perim, false);
-    case 2: return sweep_fn_v<3, 2>(perim, false);
-    default: return sweep_fn_v<3, 0>(perim, false);
+    case 1: return sweep_fn_v<3, 1>(perim, false, false);
+    case 2: return sweep_fn_v<3, 2>(perim, false, false);
+    default: return sweep_fn_v<3, 0>(perim, false, act);
   }
 }
 
@@ -1009,7 +1128,7 @@ SweepShape sweep_shape(int ndim, int variant) {
 
 int sweep_max_blocks_per_sm(int ndim, bool perim, int variant, bool scores) {
   const SweepShape sh = sweep_shape(ndim, variant);
-  const void* fn = sweep_fn(ndim, perim, variant, scores);
+  const void* fn = sweep_fn(ndim, perim, variant, scores, false);
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)sh.smem) != cudaSuccess)
     return 0;
@@ -1022,9 +1141,10 @@ int sweep_max_blocks_per_sm(int ndim, bool perim, int variant, bool scores) {
 
 cudaError_t launch_sweep(int ndim, bool perim, int variant, const SweepArgs& a,
                          int grid, cudaStream_t s, bool scores) {
+  if (a.act_on) variant = 0;  // the act kernels are built for variant 0
   const SweepShape sh = sweep_shape(ndim, variant);
-  const void* fn = sweep_fn(ndim, perim, variant, scores);
-  if (scores) {  // the score kernels get their shared-memory attribute on first use
+  const void* fn = sweep_fn(ndim, perim, variant, scores && !a.act_on, a.act_on != 0);
+  if (scores || a.act_on) {  // these kernels get their shared-memory attribute on first use
     const cudaError_t e = cudaFuncSetAttribute(
         fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem);
     if (e != cudaSuccess) return e;

@@ -26,9 +26,11 @@ Differences from the reference, all deliberate:
   * the chemotaxis field is float on the device (the reference keeps
     doubles) and the chemotaxis energy is summed in FP32, rounded step by
     step; get_field's array exists whether or not has_field was set.
-The act and persistence terms are not part of this engine: setting them
-raises CpmError, and get_act_state returns a zero array of the reference's
-shape.
+  * the act model's geometric means use this library's own FP32 log2 /
+    exp2 (the reference uses the fast __powf), and copies of runs with an
+    act lambda are written at the end of their phase (see cpm_set_act).
+The persistence term is not part of this engine: setting it raises
+CpmError.
 """
 import ctypes
 import os
@@ -48,6 +50,7 @@ CPM_ERR_TIMEOUT = 5
 CPM_ERR_UNSUPPORTED = 6
 MAX_TYPES = 32
 CPM_FLAG_FIELD = 1
+CPM_FLAG_ACT = 2
 DISPATCH_GRID = 0
 DISPATCH_REPLICA = 1
 
@@ -148,6 +151,11 @@ def library():
                                ctypes.c_float, ctypes.c_int],
         "cpm_set_fixed": [H, ctypes.c_int, ctypes.c_int],
         "cpm_set_chemotaxis": [H, ctypes.c_int, ctypes.c_float],
+        "cpm_set_act": [H, ctypes.c_int, ctypes.c_int, ctypes.c_float],
+        "cpm_set_act_r": [H, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float],
+        "cpm_host_act_r": [H, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p),
+                           ctypes.POINTER(ctypes.c_int64)],
+        "cpm_has_act": [H, ctypes.POINTER(ctypes.c_int)],
         "cpm_set_chemotaxis_r": [H, ctypes.c_int, ctypes.c_int, ctypes.c_float],
         "cpm_host_field_r": [H, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p),
                              ctypes.POINTER(ctypes.c_int64)],
@@ -264,6 +272,22 @@ class _Engine:
         buf._owner = self
         return np.ctypeslib.as_array(buf).reshape((self.dimensionality,)
                                                   + tuple(self._replica_shape(replica)))
+
+    def act_lattice(self, replica=0):
+        """Writable host view (int32, as the reference's get_act_state) of a
+        replica's act stamps: the MCS of the last copy into each site."""
+        ptr, n = ctypes.c_void_p(), ctypes.c_int64()
+        self._call("cpm_host_act_r", int(replica), ctypes.byref(ptr), ctypes.byref(n))
+        buf = (ctypes.c_int32 * n.value).from_address(ptr.value)
+        buf._owner = self
+        return np.ctypeslib.as_array(buf).reshape(tuple(self._replica_shape(replica)))
+
+    @property
+    def act_exists(self):
+        """Whether the act stamps are allocated (has_act, or first use)."""
+        v = ctypes.c_int()
+        self._call("cpm_has_act", ctypes.byref(v))
+        return bool(v.value)
 
     def host_lattice(self, replica=0):
         """Writable host view of a replica's lattice ([y, x] / [z, y, x])."""
@@ -448,7 +472,8 @@ class Cpm(_Engine):
         h = ctypes.c_void_p()
         _check(lib.cpm_create(int(dimension), int(dimensionality),
                               int(number_of_cells), float(temperature),
-                              CPM_FLAG_FIELD if has_field else 0, ctypes.byref(h)), None)
+                              (CPM_FLAG_FIELD if has_field else 0)
+                              | (CPM_FLAG_ACT if has_act else 0), ctypes.byref(h)), None)
         super().__init__(h)
         self.dimension = int(dimension)
         self.number_of_cells = int(number_of_cells)
@@ -480,8 +505,6 @@ class Cpm(_Engine):
         if (lambda_persistence != -1 and persistence_diffusion != -1
                 and persistence_time != -1):
             unsupported.append("persistence")
-        if lambda_act != -1 and max_act != -1:
-            unsupported.append("act")
         if unsupported:
             raise CpmError(CPM_ERR_UNSUPPORTED,
                            "terms not modelled by this engine: " + ", ".join(unsupported))
@@ -491,6 +514,8 @@ class Cpm(_Engine):
             self._call("cpm_set_area", ct, int(target_area), float(lambda_area))
         if fixed >= 0:
             self._call("cpm_set_fixed", ct, int(fixed))
+        if lambda_act != -1 and max_act != -1:
+            self._call("cpm_set_act", ct, int(max_act), float(lambda_act))
         if lambda_chemotaxis != -1:
             self._call("cpm_set_chemotaxis", ct, float(lambda_chemotaxis))
         if other_cell_type != -1 and adhesion != -1:
@@ -552,7 +577,9 @@ class Cpm(_Engine):
         return out
 
     def get_act_state(self):
-        return np.zeros(self._shape, np.int32)
+        """Writable int32 view of the act stamps, shape (D, D[, D]) as the
+        reference's (src/python_wrapper.cpp:310-326)."""
+        return self.act_lattice(0)
 
     def get_field(self):
         """Writable float64 view of the chemotaxis field, shape (d, D, D[, D])
@@ -612,6 +639,12 @@ class Batch(_Engine):
         else:
             self._call("cpm_set_perimeter_r", int(replica), int(cell_type), int(target),
                        float(lam))
+
+    def set_act(self, replica, cell_type, max_act, lam):
+        if replica is None:
+            self._call("cpm_set_act", int(cell_type), int(max_act), float(lam))
+        else:
+            self._call("cpm_set_act_r", int(replica), int(cell_type), int(max_act), float(lam))
 
     def set_chemotaxis(self, replica, cell_type, lam):
         if replica is None:

@@ -44,6 +44,8 @@ class Workload:
     fixed: np.ndarray = None     # bool [ntypes]: fixed (unmovable) types, or None
     chemo: np.ndarray = None     # float32 [ntypes]: chemotaxis lambdas, or None
     field: np.ndarray = None     # float64 [ndim, (nz,) ny, nx] chemotaxis field, or None
+    act_lambda: np.ndarray = None  # float32 [ntypes]: act lambdas, or None
+    act_max: np.ndarray = None     # int32 [ntypes]: act maxima, or None
 
     @property
     def ndim(self):
@@ -77,6 +79,12 @@ class Workload:
             view = engine.field(0 if replica is None else replica)
             view[...] = self.field
         for a in range(nt):
+            if self.act_lambda is not None and self.act_lambda[a] != 0:
+                mx = int(self.act_max[a]) if self.act_max is not None else 0
+                if replica is None:
+                    engine._call("cpm_set_act", a, mx, float(self.act_lambda[a]))
+                else:
+                    engine.set_act(replica, a, mx, float(self.act_lambda[a]))
             if self.chemo is not None and self.chemo[a] != 0:
                 if replica is None:
                     engine._call("cpm_set_chemotaxis", a, float(self.chemo[a]))
@@ -98,7 +106,8 @@ class Workload:
         return dict(J=self.J, lam_area=self.lam_area, tgt_area=self.tgt_area,
                     lam_perim=self.lam_perim, tgt_perim=self.tgt_perim,
                     temperature=self.temperature, stick=self.stick, fixed=self.fixed,
-                    chemo=self.chemo, field=self.field)
+                    chemo=self.chemo, field=self.field, act_lambda=self.act_lambda,
+                    act_max=self.act_max)
 
 
 def _params(nt, J, lam_area=0.0, tgt_area=0, lam_perim=0.0, tgt_perim=0):

@@ -54,10 +54,11 @@ typedef struct {
 /* Replaces Cpm::Cpm (src/cpm.cu:176-261) as reached through PyCpm_init
  * (src/python_wrapper.cpp:27-41).  Argument order follows the Python
  * constructor (dimension, dimensionality, number_of_cells, temperature).
- * `flags`: CPM_FLAG_FIELD allocates the chemotaxis field (has_field); act
- * lattices (has_act) are not supported.  Allocates the device lattice and
+ * `flags`: CPM_FLAG_FIELD allocates the chemotaxis field (has_field),
+ * CPM_FLAG_ACT the act stamps (has_act).  Allocates the device lattice and
  * the cell tables for ids 0..number_of_cells on the current CUDA device. */
 #define CPM_FLAG_FIELD 1
+#define CPM_FLAG_ACT 2
 int cpm_create(int dimension, int dimensionality, int number_of_cells,
                float temperature, int flags, cpm_handle** out);
 
@@ -111,6 +112,27 @@ int cpm_set_adhesion(cpm_handle* h, int type, int other, float J,
                      int symmetric);
 int cpm_set_adhesion_r(cpm_handle* h, int replica, int type, int other,
                        float J, int symmetric);
+
+/* Replaces Cpm::setAct (src/cpm.cu:131-135).  An attempt adds
+ * -lambda / max_act * (A_source - A_target) to dH (src/kernels2d.cu:312-473,
+ * src/kernels3d.cu:301-470), lambda and max_act of the target type (of the
+ * source type for a medium target).  A_site is the geometric mean of
+ * max(max_act + act - mcs, 0) over the site and its neighbours of the same
+ * cell (0 for the medium), act being the MCS of the last copy into a site;
+ * here computed as exp2 of the mean log2 with this library's own FP32 log2 /
+ * exp2.  Copies of runs with an act lambda are written at the end of their
+ * phase, so that every attempt reads the phase's starting state; such runs
+ * use tile variant 0 and cannot accumulate scores. */
+int cpm_set_act(cpm_handle* h, int type, int max_act, float lambda);
+int cpm_set_act_r(cpm_handle* h, int replica, int type, int max_act, float lambda);
+
+/* Replaces Cpm::getActData (src/cpm.cu:523-525) behind get_act_state
+ * (src/python_wrapper.cpp:310-326): replica r's act stamps (the MCS of the
+ * last copy into each site, row-major), allocated with zeros on the first
+ * call (or at cpm_create with CPM_FLAG_ACT) and pushed / pulled with the
+ * lattice.  cpm_has_act tells whether they exist. */
+int cpm_host_act_r(cpm_handle* h, int replica, uint32_t** ptr, int64_t* nsites);
+int cpm_has_act(const cpm_handle* h, int* has);
 
 /* Replaces Cpm::setChemotaxis (src/cpm.cu:155-158): lambda of a type.  An
  * attempt adds -lambda * (d . F) to dH, with d the unit copy direction

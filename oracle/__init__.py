@@ -31,6 +31,9 @@ class Params(ctypes.Structure):
         ("fixed_mask", ctypes.c_uint32),
         ("chemo", ctypes.c_float * MAX_TYPES),
         ("field", ctypes.c_void_p),
+        ("act_lambda", ctypes.c_float * MAX_TYPES),
+        ("act_max", ctypes.c_int * MAX_TYPES),
+        ("act", ctypes.c_void_p),
     ]
 
 
@@ -65,6 +68,9 @@ def lib():
         l.orc_philox4x32_10.argtypes = [u32p, u32p, u32p]
         l.orc_exp_neg.argtypes = [ctypes.c_float]
         l.orc_exp_neg.restype = ctypes.c_float
+        for name in ("orc_log2_pos", "orc_exp2"):
+            getattr(l, name).argtypes = [ctypes.c_float]
+            getattr(l, name).restype = ctypes.c_float
         l.orc_init_tables.argtypes = [ctypes.POINTER(Params), ctypes.c_void_p,
                                       ctypes.c_void_p, ctypes.c_void_p,
                                       ctypes.c_void_p]
@@ -90,6 +96,14 @@ def exp_neg(x: float) -> float:
     return float(lib().orc_exp_neg(float(x)))
 
 
+def log2_pos(v: float) -> float:
+    return float(lib().orc_log2_pos(float(v)))
+
+
+def exp2(y: float) -> float:
+    return float(lib().orc_exp2(float(y)))
+
+
 class OracleSim:
     """One lattice plus its cell tables, advanced by the CPU oracle.
 
@@ -97,13 +111,16 @@ class OracleSim:
     id | type << 24.  Parameters follow the engine's conventions: J[a][b] is
     the adhesion seen by a site of type a next to a site of type b; stick
     (optional, [a][b]) the stickiness, fixed (optional, per type) the
-    unmovable types, chemo (optional, per type) the chemotaxis lambdas and
-    field (optional, [ndim, (nz,) ny, nx]) the chemotaxis field.
+    unmovable types, chemo (optional, per type) the chemotaxis lambdas,
+    field (optional, [ndim, (nz,) ny, nx]) the chemotaxis field, act_lambda /
+    act_max (optional, per type) the act model and act (optional) its
+    starting stamps (kept in self.act).
     """
 
     def __init__(self, lattice, ncells, J, lam_area, tgt_area,
                  lam_perim=None, tgt_perim=None, temperature=1.0, seed=0,
-                 stream=0, stick=None, fixed=None, chemo=None, field=None):
+                 stream=0, stick=None, fixed=None, chemo=None, field=None,
+                 act_lambda=None, act_max=None, act=None):
         lat = np.ascontiguousarray(lattice, dtype=np.uint32).copy()
         self.ndim = lat.ndim
         self.lattice = lat
@@ -150,6 +167,14 @@ class OracleSim:
             if self.field.shape != (self.ndim,) + lat.shape:
                 raise ValueError("field must have shape (ndim,) + lattice shape")
             p.field = self.field.ctypes.data
+        fill(p.act_lambda, act_lambda, np.float32)
+        fill(p.act_max, act_max, np.int32)
+        self.act = None
+        if act is not None or (act_lambda is not None and np.any(np.asarray(act_lambda) != 0)):
+            # act stamps (MCS of the last copy into each site), zero to start
+            self.act = (np.zeros(lat.shape, np.uint32) if act is None
+                        else np.ascontiguousarray(act, dtype=np.uint32).copy())
+            p.act = self.act.ctypes.data
         self.params = p
         n1 = self.ncells + 1
         self.area = np.zeros(n1, np.int32)

@@ -80,7 +80,85 @@ struct Params {
   // (src/kernels2d.cu:302-334, src/kernels3d.cu:275-324)
   float chemo[kMaxTypes];
   const float* field;
+  // act model (src/kernels2d.cu:312-473): lambda and max per type, and the
+  // act stamps (MCS of the last copy into each site, or null)
+  float act_lambda[kMaxTypes];
+  int act_max[kMaxTypes];
+  uint32_t* act;
 };
+
+// log2(v), v >= 1, and 2^y in FP32, the library's own (act model): log2 by
+// the atanh series after reducing the mantissa to [1/sqrt(2), sqrt(2)),
+// 2^y by Cody-Waite reduction and Taylor terms to degree 7.  Written step
+// for step as the sweep kernel's log2_pos / exp2_own.
+float log2_pos(float v) {
+  uint32_t b;
+  std::memcpy(&b, &v, 4);
+  int e = (int)((b >> 23) & 0xFFu) - 127;
+  const uint32_t mb = (b & 0x7FFFFFu) | (127u << 23);
+  float m;
+  std::memcpy(&m, &mb, 4);
+  if (m > 1.41421356f) {
+    m = m * 0.5f;
+    e += 1;
+  }
+  const float z = (m - 1.0f) / (m + 1.0f);
+  const float z2 = z * z;
+  float p = 1.0f / 11.0f;
+  p = std::fma(p, z2, 1.0f / 9.0f);
+  p = std::fma(p, z2, 1.0f / 7.0f);
+  p = std::fma(p, z2, 0.2f);
+  p = std::fma(p, z2, 1.0f / 3.0f);
+  p = std::fma(p, z2, 1.0f);
+  return (float)e + (z * p) * 2.8853900817779268f;
+}
+
+float exp2_own(float y) {
+  const float kf = std::nearbyint(y);
+  const float f = y - kf;
+  const float r = std::fma(f, 0x1.62e430p-1f, f * -0x1.05c610p-29f);
+  float p = 1.0f / 5040.0f;
+  p = std::fma(p, r, 1.0f / 720.0f);
+  p = std::fma(p, r, 1.0f / 120.0f);
+  p = std::fma(p, r, 1.0f / 24.0f);
+  p = std::fma(p, r, 1.0f / 6.0f);
+  p = std::fma(p, r, 0.5f);
+  p = std::fma(p, r, 1.0f);
+  p = std::fma(p, r, 1.0f);
+  const int k = (int)kf;
+  const uint32_t bits = (uint32_t)(k + 127) << 23;
+  float s;
+  std::memcpy(&s, &bits, 4);
+  return p * s;
+}
+
+// Geometric mean of max(amax + act[i] - tick, 0) over site (x, y, z) and its
+// neighbours holding `id` (src/kernels2d.cu:338-473), as exp2 of the mean
+// log2 in neighbour order; 0 when a factor is 0.
+float act_mean(const Params& p, const uint32_t* lat, int x, int y, int z, uint32_t id,
+               int amax, int64_t tick) {
+  const int nx = p.nx, ny = p.ny, nz = p.ndim == 3 ? p.nz : 1;
+  auto at = [&](int xx, int yy, int zz) { return ((int64_t)zz * ny + yy) * nx + xx; };
+  auto wrapc = [](int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); };
+  const int64_t a0 = (int64_t)amax + (int64_t)p.act[at(x, y, z)] - tick;
+  if (a0 <= 0) return 0.0f;
+  float sum = log2_pos((float)a0);
+  int count = 1;
+  const int zlo = p.ndim == 3 ? -1 : 0, zhi = p.ndim == 3 ? 1 : 0;
+  for (int dz = zlo; dz <= zhi; ++dz)
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dx = -1; dx <= 1; ++dx) {
+        if (!dz && !dy && !dx) continue;
+        const int64_t n = at(wrapc(x + dx, nx), wrapc(y + dy, ny),
+                             p.ndim == 3 ? wrapc(z + dz, nz) : 0);
+        if (lat[n] != id) continue;
+        const int64_t v = (int64_t)amax + (int64_t)p.act[n] - tick;
+        if (v <= 0) return 0.0f;
+        sum = sum + log2_pos((float)v);
+        ++count;
+      }
+  return exp2_own(sum / (float)count);
+}
 
 // Unit copy direction (target minus source) dotted with the field at the
 // source site: the raw difference of wrapped coordinates in 2D
@@ -195,6 +273,7 @@ inline int64_t image(int xc, int n, int64_t a, int64_t S) {
 }
 
 struct Accepted {
+  int64_t site;   // written after the phase, as all of the phase's copies
   uint32_t s, t;  // full site values (id | type << 24)
   int dps, dpt;
   int64_t img_s[3], img_t[3];
@@ -312,6 +391,31 @@ inline int attempt(const Params& p, uint32_t* lat, const Tables& tb, int x,
     float chemo = 0.0f;
     const float lam = p.chemo[ts ? ts : tt];
     if (lam != 0.0f && p.field) chemo = -lam * chemo_dot(p, x, y, z, kdir);
+    if (p.act) {  // act next: of the target type, of the source type for a medium target
+      const int ta = tt ? tt : ts;
+      const float lamA = p.act_lambda[ta];
+      const int amax_a = p.act_max[ta];
+      if (lamA != 0.0f && amax_a != 0) {
+        int ox, oy, oz;
+        if (p.ndim == 2) {
+          const int m = kdir + (kdir >= 4);
+          oz = 0;
+          oy = m / 3 - 1;
+          ox = m % 3 - 1;
+        } else {
+          const int m = kdir + (kdir >= 13);
+          oz = m / 9 - 1;
+          oy = (m / 3) % 3 - 1;
+          ox = m % 3 - 1;
+        }
+        const int sx = wrap(x + ox, nx), sy = wrap(y + oy, ny),
+                  sz = p.ndim == 3 ? wrap(z + oz, nz) : 0;
+        const int64_t tk = (int64_t)(phase / (uint64_t)(p.ndim == 2 ? 9 : 27));
+        const float tgt = t ? act_mean(p, lat, x, y, z, t, p.act_max[tt], tk) : 0.0f;
+        const float src = s ? act_mean(p, lat, sx, sy, sz, s, p.act_max[ts], tk) : 0.0f;
+        chemo = chemo + (-lamA / (float)amax_a) * (src - tgt);
+      }
+    }
     dH = chemo + dH;
   }
   const int dps = N - 2 * cnt_s;  // source cell gains the target site
@@ -357,7 +461,7 @@ inline int attempt(const Params& p, uint32_t* lat, const Tables& tb, int x,
   }
   if (!ok) return 1;
 
-  lat[site] = s;
+  acc->site = site;
   acc->s = s;
   acc->t = t;
   acc->dps = dps;
@@ -397,6 +501,8 @@ void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2],
 }
 
 float orc_exp_neg(float x) { return exp_neg(x); }
+float orc_log2_pos(float v) { return log2_pos(v); }
+float orc_exp2(float y) { return exp2_own(y); }
 
 // Recompute every table from the lattice.  Returns 0, or a bit set of
 // 1: id above ncells, 2: type >= 32, 4: non-zero type on id 0,
@@ -468,6 +574,10 @@ int run_impl(const orc_params* pp, uint32_t* lat, int32_t* area, int32_t* perim,
   const bool perim_on = perimeter_enabled(p);
   bool stick_on = false;
   for (int k = 0; k < kMaxTypes * kMaxTypes; ++k) stick_on = stick_on || p.stick[k] != 0.0f;
+  // act stamps are kept when some type has an act lambda (the sweep then
+  // writes every copy, and its stamp, after its phase)
+  bool act_on = false;
+  for (int k = 0; k < kMaxTypes; ++k) act_on = act_on || (p.act && p.act_lambda[k] != 0.0f);
   Tables tb{area, perim, csum};
   if (nthreads <= 0) nthreads = omp_get_max_threads();
   std::vector<std::vector<Accepted>> logs(nthreads);
@@ -526,6 +636,8 @@ int run_impl(const orc_params* pp, uint32_t* lat, int32_t* area, int32_t* perim,
           // Apply the phase's deltas; integer sums, so order is irrelevant.
           for (auto& log : logs)
             for (const Accepted& c : log) {
+              lat[c.site] = c.s;
+              if (act_on) p.act[c.site] = (uint32_t)tick;
               if (c.s) {
                 const uint32_t is = c.s & 0xFFFFFFu;
                 area[is] += 1;

@@ -41,5 +41,5 @@ def test_invalid_arguments_rejected_before_touching_cuda(engine_lib):
     h = ctypes.c_void_p()
     assert engine_lib.cpm_create(64, 4, 10, 10.0, 0, ctypes.byref(h)) == 1
     assert b"dimensionality" in engine_lib.cpm_last_error(None)
-    assert engine_lib.cpm_create(64, 2, 10, 10.0, 2, ctypes.byref(h)) == 6  # unknown flag
+    assert engine_lib.cpm_create(64, 2, 10, 10.0, 4, ctypes.byref(h)) == 6  # unknown flag
     assert engine_lib.cpm_create(2, 2, 10, 10.0, 0, ctypes.byref(h)) == 1

@@ -136,8 +136,6 @@ def test_push_rejects_invalid_lattices(engine_lib):
 def test_unsupported_terms_and_bad_arguments(engine_lib):
     import gpucpm
     sim = gpucpm.Cpm(32, 2, 4, 10, False)
-    with pytest.raises(gpucpm.CpmError, match="act"):
-        sim.set_constraints(cell_type=1, lambda_act=10, max_act=20)
     with pytest.raises(gpucpm.CpmError, match="persistence"):
         sim.set_constraints(cell_type=1, lambda_persistence=1.0, persistence_diffusion=0.5,
                             persistence_time=10)

@@ -185,3 +185,82 @@ def test_chemotaxis_moves_cells_up_the_field(engine_lib):
         sim.synchronize()
         drift[lam] = float(np.mean(sim.get_centroids()[:, 0] - c0))
     assert drift[20.0] > drift[0.0] + 5.0, drift
+
+
+def _with_act(w, lam, amax):
+    w.act_lambda = np.asarray(lam, np.float32)
+    w.act_max = np.asarray(amax, np.int32)
+    return w
+
+
+@pytest.mark.parametrize("shape,mcs", [((48, 44), 12), ((33, 35), 10), ((12, 14, 13), 4)])
+def test_act_matches_oracle(engine_lib, shape, mcs):
+    """The act model (src/kernels2d.cu:312-473, src/kernels3d.cu:301-470) and
+    its stamps against the oracle, bit for bit: copies of act runs land after
+    their phase in both."""
+    w = W.random_small(shape, 24 if len(shape) == 2 else 16, ntypes=2, seed=110 + len(shape),
+                       temperature=9.0)
+    _with_act(w, [0.0, 30.0, 18.0], [0, 15, 10])
+    e = make_engine(w, seed=8)
+    e.run_mcs(mcs)
+    finish(e)
+    sim = oracle.OracleSim(w.lattice, w.ncells, **w.oracle_kwargs(), seed=8).run(mcs)
+    assert_same(e, sim)
+    np.testing.assert_array_equal(e.act_lattice(0).view(np.uint32), sim.act)
+    assert sim.act.max() == mcs - 1
+
+
+def test_act_batch_replica_dispatch_and_scores_refused(engine_lib):
+    import torch
+
+    import gpucpm
+    ws = [_with_act(W.random_small((40 + 4 * i, 36), 20, ntypes=2, seed=130 + i,
+                                   temperature=8.0), [0.0, 20.0 + 5 * i, 10.0], [0, 12, 9])
+          for i in range(3)]
+    for d in (gpucpm.DISPATCH_GRID, gpucpm.DISPATCH_REPLICA):
+        b = gpucpm.Batch(2, [w.lattice.shape[::-1] for w in ws], [w.ncells for w in ws])
+        for r, w in enumerate(ws):
+            b.lattice(r)[...] = w.lattice.view(np.int32)
+            w.apply(b, replica=r)
+        b.set_seed(6, 20)
+        b.set_dispatch(d)
+        b.push_to_gpu()
+        b.run_mcs(8)
+        b.synchronize()
+        b.pull_from_gpu()
+        for r, w in enumerate(ws):
+            sim = oracle.OracleSim(w.lattice, w.ncells, **w.oracle_kwargs(), seed=6,
+                                   stream=20 + r).run(8)
+            np.testing.assert_array_equal(b.lattice(r).view(np.uint32), sim.lattice)
+            np.testing.assert_array_equal(b.act_lattice(r).view(np.uint32), sim.act)
+            area, perim, cs = b.tables(r)
+            np.testing.assert_array_equal(cs, sim.csum)
+    spec = gpucpm.ScoreSpec.make(((1, 1),))
+    sc = torch.zeros((3, 2, gpucpm.SCORE_MAX), device="cuda")
+    with pytest.raises(gpucpm.CpmError, match="act"):
+        b.run_scores(2, sc.data_ptr(), 0, 2, spec)
+
+
+def test_set_constraints_act_and_get_act_state(engine_lib):
+    """The reference's keywords (src/python_wrapper.cpp:113-115) and its
+    act-state view."""
+    import gpucpm
+    sim = gpucpm.Cpm(64, 2, 6, 10, False, 1, 1)
+    for k in range(6):
+        sim.add_cell(1, 8 + 9 * k, 12 + 7 * k)
+    sim.set_constraints(cell_type=1, lambda_area=5, target_area=60)
+    sim.set_constraints(cell_type=0, other_cell_type=1, adhesion=10)
+    sim.set_constraints(cell_type=1, lambda_act=40, max_act=20)
+    lat0 = sim.get_state().view(np.uint32).copy()
+    sim.push_to_gpu()
+    sim.run_mcs(30)
+    sim.synchronize()
+    sim.pull_from_gpu()
+    st = sim.get_act_state()
+    assert st.dtype == np.int32 and st.shape == (64, 64)
+    J = np.zeros((2, 2), np.float32)
+    J[0, 1] = J[1, 0] = 10
+    ref = oracle.OracleSim(lat0, 6, J, [0, 5], [0, 60], temperature=10.0,
+                           act_lambda=[0, 40], act_max=[0, 20]).run(30)
+    np.testing.assert_array_equal(sim.get_state().view(np.uint32), ref.lattice)
+    np.testing.assert_array_equal(st.view(np.uint32), ref.act)

@@ -364,3 +364,117 @@ def test_oracle_scores_are_derivatives_of_the_decision_log_likelihood(case):
         assert zero_dh > 0
     np.testing.assert_allclose(got, want, rtol=1e-5, atol=1e-6)
     np.testing.assert_array_equal(sim.lattice, lat)
+
+
+def test_own_log2_and_exp2_error_bounds():
+    """The act model's FP32 log2 / exp2 (the sweep kernel's log2_pos /
+    exp2_own, restated in the oracle): within 1.5 ulp of FP32."""
+    vs = np.unique(np.concatenate([np.arange(1, 5000), np.geomspace(1, 1e7, 3000).astype(int)]))
+    worst = 0.0
+    for v in vs:
+        got = oracle.log2_pos(float(v))
+        ref = math.log2(float(np.float32(v)))
+        worst = max(worst, abs(got - ref) / float(np.spacing(np.float32(max(abs(ref), 1.0)))))
+    assert worst <= 1.5, worst
+    worst = 0.0
+    for y in np.linspace(-30.0, 60.0, 9001, dtype=np.float32):
+        got = oracle.exp2(float(y))
+        ref = 2.0 ** float(y)
+        worst = max(worst, abs(got - ref) / float(np.spacing(np.float32(ref))))
+    assert worst <= 1.5, worst
+    assert oracle.exp2(0.0) == 1.0 and oracle.log2_pos(1.0) == 0.0
+
+
+def _act_mean_py(lat, act, x, y, ident, amax, tick):
+    """Geometric mean of max(amax + act - tick, 0) over (x, y) and its
+    neighbours holding `ident`, as exp2 of the FP32 mean log2 (restated)."""
+    n = lat.shape[0]
+    f32 = np.float32
+    a0 = amax + int(act[y, x]) - tick
+    if a0 <= 0:
+        return f32(0.0)
+    s, count = f32(oracle.log2_pos(a0)), 1
+    for dy in (-1, 0, 1):
+        for dx in (-1, 0, 1):
+            if dx == 0 and dy == 0:
+                continue
+            xx, yy = (x + dx) % n, (y + dy) % n
+            if int(lat[yy, xx]) != ident:
+                continue
+            v = amax + int(act[yy, xx]) - tick
+            if v <= 0:
+                return f32(0.0)
+            s = f32(s + f32(oracle.log2_pos(v)))
+            count += 1
+    return f32(oracle.exp2(f32(s / f32(count))))
+
+
+def test_act_mcs_matches_restatement():
+    """One MCS of the act model (src/kernels2d.cu:312-473), replayed in
+    Python from the phase's starting state, against the oracle: act term
+    first, lambda and max of the target type (source type for a medium
+    target), every copy and its stamp written after its phase."""
+    w = W.random_small((20, 20), 12, ntypes=2, seed=31, temperature=8.0)
+    J = np.rint(w.J).astype(int)
+    lam_a, tgt_a = [0.0, 1.0, 1.0], [0, 30, 30]
+    lam_p, tgt_p = [0.0, 0.0, 0.0], [0, 0, 0]
+    act_lambda = np.array([0.0, 40.0, 25.0], np.float32)
+    act_max = np.array([0, 20, 12], np.int32)
+    T, seed = 8.0, 3
+    sim = oracle.OracleSim(w.lattice, w.ncells, J.astype(np.float32), lam_a, tgt_a, lam_p, tgt_p,
+                           temperature=T, seed=seed, act_lambda=act_lambda, act_max=act_max)
+    sim.run(4)  # stamps up to MCS 3
+    assert sim.act.max() == 3
+    lat, act = sim.lattice.copy(), sim.act.copy()
+    area = sim.area.copy()
+    n, tick, f32 = 20, 4, np.float32
+    accepted = 0
+    for cy in (0, 1):
+        for cx in (0, 1):
+            slot = cy * 3 + cx
+            changes = []
+            for y in range(cy, n, 2):
+                for x in range(cx, n, 2):
+                    t = int(lat[y, x])
+                    nbs = [(x + i, y + j) for j in (-1, 0, 1) for i in (-1, 0, 1)
+                           if (i, j) != (0, 0)]
+                    vals = [int(lat[b % n, a % n]) for a, b in nbs]
+                    if all(v == t for v in vals):
+                        continue
+                    r = oracle.philox4x32_10([y * n + x, tick * 9 + slot, 0, 0], [seed, 0])
+                    k = (r[0] * 8) >> 32
+                    s = vals[k]
+                    if s == t:
+                        continue
+                    sx, sy = nbs[k][0] % n, nbs[k][1] % n
+                    ts, tt = s >> 24, t >> 24
+                    e_old = sum(J[tt][v >> 24] for v in vals if v != t)
+                    e_new = sum(J[ts][v >> 24] for v in vals if v != s)
+                    lead = f32(0.0)
+                    ta = tt if tt else ts
+                    if act_lambda[ta] != 0 and act_max[ta] != 0:
+                        tgt = _act_mean_py(lat, act, x, y, t, int(act_max[tt]), tick) if t else f32(0)
+                        src = _act_mean_py(lat, act, sx, sy, s, int(act_max[ts]), tick) if s else f32(0)
+                        lead = f32(lead + f32(f32(-act_lambda[ta] / f32(act_max[ta])) * f32(src - tgt)))
+                    dH = f32(lead + f32(e_new - e_old))
+                    if s:
+                        dH = f32(float(dH) + lam_a[ts] * (1 + 2 * (int(area[s & 0xFFFFFF]) - tgt_a[ts])))
+                    if t:
+                        dH = f32(float(dH) + lam_a[tt] * (1 - 2 * (int(area[t & 0xFFFFFF]) - tgt_a[tt])))
+                    u = f32(((r[1] >> 8) | 1) * 2.0 ** -24)
+                    ok = dH < 0 or u < f32(oracle.exp_neg(float(f32(-dH / f32(T)))))
+                    if ok:
+                        changes.append((x, y, s, t))
+            for x, y, s, t in changes:
+                lat[y, x] = s
+                act[y, x] = tick
+                accepted += 1
+                if s:
+                    area[s & 0xFFFFFF] += 1
+                if t:
+                    area[t & 0xFFFFFF] -= 1
+    sim.run(1)
+    assert accepted > 10
+    np.testing.assert_array_equal(sim.lattice, lat)
+    np.testing.assert_array_equal(sim.act, act)
+    np.testing.assert_array_equal(sim.area, area)
