@@ -68,6 +68,13 @@ struct cpm_handle {
   uint32_t* d_pend_val = nullptr;
   long long pend_entries = 0;  // capacity of the pending arrays (all blocks)
   bool act_active = false;     // some replica's record has an act lambda
+  // 3D persistence (allocated on first use): preferred direction per table
+  // row, and the ring of the cells' mean coordinates after the last runs
+  double* d_prefdir = nullptr;  // [rows][3]
+  double* d_hist = nullptr;     // [hist_size][rows][3]
+  int hist_size = 1;            // the reference's `history` (Cpm constructor)
+  int hist_slot = 0;            // slot the next run's means go to
+  bool persist_active = false;  // 3D and some record has a persistence lambda
   uint32_t* d_lat = nullptr;
   unsigned long long* d_ap[2] = {nullptr, nullptr};  // packed (area, perimeter)
   long long* d_cs[2] = {nullptr, nullptr};
@@ -159,6 +166,8 @@ void free_all(cpm_handle* h) {
   cudaFree(h->d_act);
   cudaFree(h->d_pend_site);
   cudaFree(h->d_pend_val);
+  cudaFree(h->d_prefdir);
+  cudaFree(h->d_hist);
   cudaFree(h->d_lat);
   for (int b = 0; b < 2; ++b) {
     cudaFree(h->d_ap[b]);
@@ -498,6 +507,38 @@ int read_error_word(cpm_handle* h, uint32_t* word) {
   return CPM_OK;
 }
 
+// Persistence buffers on first use: directions drawn from (seed, stream),
+// history filled from the current tables when they exist.
+int ensure_persist(cpm_handle* h) {
+  if (!h->d_prefdir) {
+    CPM_CUDA(h, cudaMalloc((void**)&h->d_prefdir, sizeof(double) * 3 * h->rows));
+    CPM_CUDA(h, launch_init_prefdir(h->d_prefdir, h->d_reps, h->nrep, h->rows, h->seed,
+                                    h->stream_id, h->stream));
+  }
+  if (!h->d_hist) {
+    CPM_CUDA(h, cudaMalloc((void**)&h->d_hist, sizeof(double) * 3 * h->rows * h->hist_size));
+    CPM_CUDA(h, cudaMemsetAsync(h->d_hist, 0, sizeof(double) * 3 * h->rows * h->hist_size,
+                                h->stream));
+    h->hist_slot = 0;
+    if (h->pushed)
+      CPM_CUDA(h, launch_persist_fill(h->d_hist, h->hist_size, h->d_ap[0], h->d_cs[0], h->d_reps,
+                                      h->nrep, h->rows, h->stream));
+  }
+  return CPM_OK;
+}
+
+// After a run of a persistence engine: the cells' means into the history,
+// and the preferred directions updated (src/cpm.cu:486-510).
+int persist_after_run(cpm_handle* h) {
+  if (!h->persist_active) return CPM_OK;
+  CPM_CUDA(h, launch_persist_update(h->d_prefdir, h->d_hist, h->hist_size, h->hist_slot,
+                                    h->d_ap[0], h->d_cs[0], h->d_ctype, h->d_params, h->d_reps,
+                                    h->nrep, h->rows, h->stream));
+  h->launches += 1;
+  h->hist_slot = (h->hist_slot + 1) % h->hist_size;
+  return CPM_OK;
+}
+
 // The act lattice (zeros) and the pending lists, on first use.
 int ensure_act(cpm_handle* h) {
   if (!h->d_act) {
@@ -553,6 +594,21 @@ int upload_params(cpm_handle* h) {
     p.act_on = 0;
     for (int k = 0; k < kMaxTypes; ++k)
       if (p.act_lambda[k] != 0.0f) p.act_on = 1;
+    p.persist_on = 0;
+    for (int k = 0; k < kMaxTypes; ++k)
+      if (p.persist_lambda[k] != 0.0f) p.persist_on = 1;
+  }
+  bool persist = false;
+  for (const auto& p : h->psets) persist = persist || (h->ndim == 3 && p.persist_on);
+  if (persist) {
+    if (int rc = ensure_persist(h)) return rc;
+  }
+  if (persist != h->persist_active) {
+    h->persist_active = persist;
+    if (h->graph_exec) {
+      cudaGraphExecDestroy(h->graph_exec);
+      h->graph_exec = nullptr;
+    }
   }
   bool act = false;
   for (const auto& p : h->psets) act = act || p.act_on;
@@ -598,7 +654,7 @@ bool any_perimeter(const cpm_handle* h) {
 // Kernel arguments of a sweep with tile variant v and dispatch d (tick0 /
 // mcs filled in by the caller).
 SweepArgs sweep_args(const cpm_handle* h, int v, int d) {
-  if (h->act_active) v = 0;  // the act kernels exist for tile variant 0
+  if (h->act_active || h->persist_active) v = 0;  // extended-term kernels: variant 0
   SweepArgs a;
   std::memset(&a, 0, sizeof a);
   a.lat = h->d_lat;
@@ -614,6 +670,7 @@ SweepArgs sweep_args(const cpm_handle* h, int v, int d) {
   a.field = h->d_field;
   a.act = h->d_act;
   a.act_on = h->act_active ? 1 : 0;
+  a.prefdir = h->persist_active ? h->d_prefdir : nullptr;
   a.pend_site = h->d_pend_site;
   a.pend_val = h->d_pend_val;
   a.pend_cap = (d == CPM_DISPATCH_REPLICA ? c.list_cap_local : c.list_cap) / 2;
@@ -633,7 +690,7 @@ SweepArgs sweep_args(const cpm_handle* h, int v, int d) {
 }
 
 int grid_of(const cpm_handle* h, int v, int d) {
-  if (h->act_active) v = 0;
+  if (h->act_active || h->persist_active) v = 0;
   return d == CPM_DISPATCH_REPLICA ? h->cfg[v].grid_local : h->cfg[v].grid;
 }
 
@@ -810,6 +867,18 @@ int set_act(cpm_handle* h, int r, int type, int max_act, float lambda) {
   });
 }
 
+int set_persistence(cpm_handle* h, int r, int type, int time, float diffusion, float lambda) {
+  if (!h) return CPM_ERR_INVALID;
+  if (int rc = check_type(h, type)) return rc;
+  if (!std::isfinite(lambda) || !std::isfinite(diffusion))
+    return h->fail(CPM_ERR_INVALID, "lambda and diffusion must be finite");
+  return for_replicas(h, r, [&](DevParams& p) {
+    p.persist_lambda[type] = lambda;
+    p.persist_diff[type] = diffusion;
+    p.persist_time[type] = time;
+  });
+}
+
 int set_chemotaxis(cpm_handle* h, int r, int type, float lambda) {
   if (!h) return CPM_ERR_INVALID;
   if (int rc = check_type(h, type)) return rc;
@@ -842,6 +911,73 @@ int cpm_set_chemotaxis(cpm_handle* h, int type, float lambda) {
 }
 int cpm_set_chemotaxis_r(cpm_handle* h, int r, int type, float lambda) {
   return set_chemotaxis(h, r < 0 ? -2 : r, type, lambda);
+}
+int cpm_set_persistence(cpm_handle* h, int type, int time, float diffusion, float lambda) {
+  return set_persistence(h, -1, type, time, diffusion, lambda);
+}
+int cpm_set_persistence_r(cpm_handle* h, int r, int type, int time, float diffusion,
+                          float lambda) {
+  return set_persistence(h, r < 0 ? -2 : r, type, time, diffusion, lambda);
+}
+
+int cpm_set_history(cpm_handle* h, int history) {
+  if (!h) return CPM_ERR_INVALID;
+  if (history < 1) return h->fail(CPM_ERR_INVALID, "history must be >= 1");
+  if (history == h->hist_size) return CPM_OK;
+  CPM_BIND(h);
+  h->hist_size = history;
+  if (h->d_hist) {  // reallocated and refilled from the current tables
+    CPM_CUDA(h, cudaStreamSynchronize(h->stream));
+    cudaFree(h->d_hist);
+    h->d_hist = nullptr;
+    return ensure_persist(h);
+  }
+  return CPM_OK;
+}
+
+int cpm_has_persistence(const cpm_handle* h, int* has, int* history) {
+  if (!h) return CPM_ERR_INVALID;
+  if (has) *has = (h->d_prefdir && h->d_hist) ? 1 : 0;
+  if (history) *history = h->hist_size;
+  return CPM_OK;
+}
+
+namespace {
+// Copies of replica r's rows of the persistence state; `to_host` picks the
+// direction.  History slots in the caller's buffer run oldest first.
+int persistence_copy(cpm_handle* h, int r, double* prefdir, double* history, bool to_host) {
+  if (int rc = check_replica(h, r)) return rc;
+  CPM_BIND(h);
+  if (!to_host && h->ndim == 3 && h->pushed) {  // restoring: allocate first
+    if (int rc = ensure_persist(h)) return rc;
+  }
+  if (!h->d_prefdir || !h->d_hist)
+    return h->fail(CPM_ERR_STATE, "the engine has no persistence state");
+  const DevReplica& R = h->reps[r];
+  const size_t n = (size_t)(R.ncells + 1) * 3;
+  const auto kind = to_host ? cudaMemcpyDeviceToHost : cudaMemcpyHostToDevice;
+  auto copy = [&](double* dev, double* host) {
+    return to_host ? cudaMemcpyAsync(host, dev, n * sizeof(double), kind, h->stream)
+                   : cudaMemcpyAsync(dev, host, n * sizeof(double), kind, h->stream);
+  };
+  if (prefdir) CPM_CUDA(h, copy(h->d_prefdir + R.cell_off * 3, prefdir));
+  if (history)
+    for (int k = 0; k < h->hist_size; ++k) {
+      const int slot = (h->hist_slot + k) % h->hist_size;
+      CPM_CUDA(h, copy(h->d_hist + ((size_t)slot * h->rows + R.cell_off) * 3, history + k * n));
+    }
+  CPM_CUDA(h, cudaStreamSynchronize(h->stream));
+  return CPM_OK;
+}
+}  // namespace
+
+int cpm_get_persistence_r(cpm_handle* h, int r, double* prefdir, double* history) {
+  return persistence_copy(h, r, prefdir, history, true);
+}
+int cpm_set_persistence_state_r(cpm_handle* h, int r, const double* prefdir,
+                                const double* history) {
+  return persistence_copy(h, r, const_cast<double*>(prefdir), const_cast<double*>(history),
+                          false);
 }
 
 int cpm_host_lattice_r(cpm_handle* h, int r, uint32_t** ptr, int64_t* nsites) {
@@ -909,7 +1045,13 @@ int cpm_push(cpm_handle* h) {
                                 cudaMemcpyHostToDevice, h->stream));
     CPM_CUDA(h, cudaStreamSynchronize(h->stream));  // `f` lives on this frame
   }
-  return recount_tables(h);
+  if (int rc = recount_tables(h)) return rc;
+  if (h->d_hist) {  // every history slot holds the pushed means (src/cpm.cu:578-583)
+    CPM_CUDA(h, launch_persist_fill(h->d_hist, h->hist_size, h->d_ap[0], h->d_cs[0], h->d_reps,
+                                    h->nrep, h->rows, h->stream));
+    h->hist_slot = 0;
+  }
+  return CPM_OK;
 }
 
 int cpm_recount(cpm_handle* h) {
@@ -942,6 +1084,12 @@ int cpm_get_params_r(const cpm_handle* h, int r, cpm_static_params* out) {
   out->temperature = p.temperature;
   std::memcpy(out->stickiness, p.stick, sizeof out->stickiness);
   for (int k = 0; k < kMaxTypes; ++k) out->fixed[k] = (p.fixed_mask >> k) & 1u;
+  std::memcpy(out->chemotaxis, p.chemo, sizeof out->chemotaxis);
+  std::memcpy(out->act_lambda, p.act_lambda, sizeof out->act_lambda);
+  std::memcpy(out->act_max, p.act_max, sizeof out->act_max);
+  std::memcpy(out->persistence_lambda, p.persist_lambda, sizeof out->persistence_lambda);
+  std::memcpy(out->persistence_diffusion, p.persist_diff, sizeof out->persistence_diffusion);
+  std::memcpy(out->persistence_time, p.persist_time, sizeof out->persistence_time);
   return CPM_OK;
 }
 
@@ -951,6 +1099,12 @@ int set_params(cpm_handle* h, int r, const cpm_static_params* in) {
   if (!in) return h->fail(CPM_ERR_INVALID, "params is NULL");
   if (!std::isfinite(in->temperature))
     return h->fail(CPM_ERR_INVALID, "temperature must be finite");
+  for (int k = 0; k < kMaxTypes; ++k) {
+    if (!std::isfinite(in->chemotaxis[k]) || !std::isfinite(in->act_lambda[k]) ||
+        !std::isfinite(in->persistence_lambda[k]) || !std::isfinite(in->persistence_diffusion[k]))
+      return h->fail(CPM_ERR_INVALID, "lambdas and diffusion must be finite");
+    if (in->act_max[k] < 0) return h->fail(CPM_ERR_INVALID, "act_max must be >= 0");
+  }
   auto fill = [&](DevParams& p) {
     std::memcpy(p.J, in->J, sizeof p.J);
     std::memcpy(p.lam_area, in->lambda_area, sizeof p.lam_area);
@@ -962,6 +1116,12 @@ int set_params(cpm_handle* h, int r, const cpm_static_params* in) {
     p.fixed_mask = 0;
     for (int k = 0; k < kMaxTypes; ++k)
       if (in->fixed[k]) p.fixed_mask |= 1u << k;
+    std::memcpy(p.chemo, in->chemotaxis, sizeof p.chemo);
+    std::memcpy(p.act_lambda, in->act_lambda, sizeof p.act_lambda);
+    std::memcpy(p.act_max, in->act_max, sizeof p.act_max);
+    std::memcpy(p.persist_lambda, in->persistence_lambda, sizeof p.persist_lambda);
+    std::memcpy(p.persist_diff, in->persistence_diffusion, sizeof p.persist_diff);
+    std::memcpy(p.persist_time, in->persistence_time, sizeof p.persist_time);
   };
   if (r == -1) {  // every field of every replica: one shared record
     DevParams p;
@@ -1037,7 +1197,7 @@ int cpm_run(cpm_handle* h, int mcs) {
   }
   h->d_tick_stale = true;
   count_attempts(h, mcs);
-  return CPM_OK;
+  return persist_after_run(h);
 }
 
 int cpm_run_graph(cpm_handle* h, int mcs) {
@@ -1087,7 +1247,7 @@ int cpm_run_graph(cpm_handle* h, int mcs) {
   h->launches += 1;
   h->tick += (uint64_t)mcs;
   count_attempts(h, mcs);
-  return CPM_OK;
+  return persist_after_run(h);  // a launch of its own: its slot changes per run
 }
 
 int cpm_autotune(cpm_handle* h, int probe_mcs, int* chosen, float* ms_per_mcs) {
@@ -1196,9 +1356,9 @@ int cpm_run_scores(cpm_handle* h, int mcs, float* d_scores, uint64_t score_base,
       return h->fail(CPM_ERR_INVALID, "cpm_run_scores: score types must be < %d", kScoreTypes);
   if (mcs == 0) return CPM_OK;
   if (int rc = upload_params(h)) return rc;
-  if (h->act_active)
-    return h->fail(CPM_ERR_UNSUPPORTED, "cpm_run_scores: scores of runs with the act term "
-                                        "are not supported");
+  if (h->act_active || h->persist_active)
+    return h->fail(CPM_ERR_UNSUPPORTED, "cpm_run_scores: scores of runs with the act or "
+                                        "persistence term are not supported");
   SweepArgs a = sweep_args(h, h->variant, h->dispatch);
   a.scores = d_scores;
   a.score_base = score_base;

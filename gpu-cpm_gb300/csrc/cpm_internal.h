@@ -118,9 +118,15 @@ struct DevParams {
   int chemo_on;         // any chemo != 0
   // act model (src/kernels2d.cu:312-473): lambda and max_act per type
   int act_on;           // any act_lambda != 0
-  int pad[2];
+  // persistence (3D, src/kernels3d.cu:327-343, src/kernels.cu:159-212):
+  // lambda and diffusion per type
+  int persist_on;       // any persist_lambda != 0
+  int pad;
   float act_lambda[kMaxTypes];
   int act_max[kMaxTypes];
+  float persist_lambda[kMaxTypes];
+  float persist_diff[kMaxTypes];
+  int persist_time[kMaxTypes];  // stored for get/set only (not read by any kernel)
 };
 
 struct DevReplica {
@@ -193,6 +199,8 @@ struct SweepArgs {
   // source (other targets of the slot) see the phase's starting state.
   uint32_t* act;
   int act_on;
+  // (3D persistence) preferred direction of each table row, [rows][3]
+  const double* prefdir;
   unsigned long long* pend_site;
   uint32_t* pend_val;
   long long pend_cap;  // entries of one block's pending list
@@ -228,6 +236,19 @@ cudaError_t launch_lr_backward(const float* scores, const float* dl_do,
                                const float* obs, const int* checkpoints, int nrep,
                                int len, int nparam, int ncheck, const float* obs_total,
                                int nrep_total, float* grad, cudaStream_t s);
+// 3D persistence: initial preferred directions, history fill (push), and
+// the update after a run (slot: the history slot that receives this run).
+cudaError_t launch_init_prefdir(double* prefdir, const DevReplica* reps, int nrep,
+                                long long rows, unsigned long long seed, unsigned stream0,
+                                cudaStream_t s);
+cudaError_t launch_persist_fill(double* hist, int H, const unsigned long long* ap,
+                                const long long* cs, const DevReplica* reps, int nrep,
+                                long long rows, cudaStream_t s);
+cudaError_t launch_persist_update(double* prefdir, double* hist, int H, int slot,
+                                  const unsigned long long* ap, const long long* cs,
+                                  const int* ctype, const DevParams* params,
+                                  const DevReplica* reps, int nrep, long long rows,
+                                  cudaStream_t s);
 cudaError_t launch_observe_heterotypic(const uint32_t* lat, const DevReplica* reps,
                                        int nrep, long long total_sites,
                                        unsigned long long* counts, cudaStream_t s);

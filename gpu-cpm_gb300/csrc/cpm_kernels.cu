@@ -180,10 +180,14 @@ __device__ __forceinline__ void source_coords(int kdir, int x, int y, int z, int
   sz = NDIM == 3 ? wrap_coord(z + oz, nz) : 0;
 }
 
+// Unit copy direction (target minus source) of neighbour kdir: the raw
+// difference of the wrapped coordinates in 2D (src/kernels2d.cu:302-309),
+// the nearest image in 3D (src/kernels3d.cu:275-299); FP32, rounded as
+// written (the oracle repeats it).  Also returns the source coordinates.
 template <int NDIM>
-__device__ __forceinline__ float chemo_dot(const float* F, long long sites, int x, int y,
-                                           int z, int kdir, int nx, int ny, int nz) {
-  int sx, sy, sz;
+__device__ __forceinline__ void unit_dir(int kdir, int x, int y, int z, int nx, int ny, int nz,
+                                         float& ux, float& uy, float& uz, int& sx, int& sy,
+                                         int& sz) {
   source_coords<NDIM>(kdir, x, y, z, nx, ny, nz, sx, sy, sz);
   int dx = x - sx, dy = y - sy, dz = z - sz;
   if (NDIM == 3) {
@@ -199,10 +203,21 @@ __device__ __forceinline__ float chemo_dot(const float* F, long long sites, int 
   s2 = __fmaf_rn(fy, fy, s2);
   if (NDIM == 3) s2 = __fmaf_rn(fz, fz, s2);
   const float len = __fsqrt_rn(s2);
+  ux = __fdiv_rn(fx, len);
+  uy = __fdiv_rn(fy, len);
+  uz = NDIM == 3 ? __fdiv_rn(fz, len) : 0.0f;
+}
+
+template <int NDIM>
+__device__ __forceinline__ float chemo_dot(const float* F, long long sites, int x, int y,
+                                           int z, int kdir, int nx, int ny, int nz) {
+  float ux, uy, uz;
+  int sx, sy, sz;
+  unit_dir<NDIM>(kdir, x, y, z, nx, ny, nz, ux, uy, uz, sx, sy, sz);
   const long long site = ((long long)sz * ny + sy) * nx + sx;
-  float c = __fmul_rn(__fdiv_rn(fx, len), __ldg(F + site));
-  c = __fmaf_rn(__fdiv_rn(fy, len), __ldg(F + sites + site), c);
-  if (NDIM == 3) c = __fmaf_rn(__fdiv_rn(fz, len), __ldg(F + 2 * sites + site), c);
+  float c = __fmul_rn(ux, __ldg(F + site));
+  c = __fmaf_rn(uy, __ldg(F + sites + site), c);
+  if (NDIM == 3) c = __fmaf_rn(uz, __ldg(F + 2 * sites + site), c);
   return c;
 }
 
@@ -316,10 +331,11 @@ __device__ __forceinline__ void flush_scores(const SweepArgs& a, float* sc, int 
   for (int k = 0; k < kScoreRegs; ++k) sc[k] = 0.0f;
 }
 
-// ACT: the act-model instantiation (variant 0, no scores): act term, and
-// every accepted copy deferred to the end of its phase.  Kept apart so that
-// the other kernels carry none of its registers.
-template <int NDIM, bool PERIM, int V, bool SCORE, bool ACT = false>
+// EXT: the instantiation (variant 0, no scores) with the act term and 3D
+// persistence; with act (a.act_on) every accepted copy is deferred to the
+// end of its phase.  Kept apart so that the other kernels carry none of its
+// registers.
+template <int NDIM, bool PERIM, int V, bool SCORE, bool EXT = false>
 __global__ void __launch_bounds__(kSweepThreadsMax, 1)
     sweep_kernel(const SweepArgs a) {
   using G = TileGeom<NDIM, V>;
@@ -416,7 +432,8 @@ __global__ void __launch_bounds__(kSweepThreadsMax, 1)
     const unsigned fixed_mask = __ldg(&P->fixed_mask);
     const bool stick_on = __ldg(&P->stick_on) != 0;
     const bool chemo_on = __ldg(&P->chemo_on) != 0;
-    const bool act_rec = ACT && __ldg(&P->act_on) != 0;
+    const bool act_rec = EXT && __ldg(&P->act_on) != 0;
+    const bool persist_rec = EXT && NDIM == 3 && __ldg(&P->persist_on) != 0;
     const int nx = __ldg(&a.reps[r].nx), ny = __ldg(&a.reps[r].ny),
               nz = __ldg(&a.reps[r].nz), ncells = __ldg(&a.reps[r].ncells);
     const long long lat_off = __ldg(&a.reps[r].lat_off);
@@ -599,9 +616,30 @@ __global__ void __launch_bounds__(kSweepThreadsMax, 1)
                                                           z, kdir, nx, ny, nz));
               }
             }
+            // persistence next (3D): lambda of the source type (target type for
+            // a medium source), preferred direction of the source cell (of the
+            // target cell for a medium source), src/kernels3d.cu:327-343
+            if (EXT && NDIM == 3 && persist_rec) {  // uniform over the tile
+              const float lam = __ldg(&P->persist_lambda[ts ? ts : tt]);
+              if (lam != 0.0f) {
+                const int qx = q % G::CX, qy = (q / G::CX) % G::CY,
+                          qz = q / (G::CX * G::CY);
+                const int x = class_coord(nx, cx, i0 + qx);
+                const int y = class_coord(ny, cy, j0 + qy);
+                const int z = NDIM == 3 ? class_coord(nz, cz, l0 + qz) : 0;
+                float ux, uy, uz;
+                int sx, sy, sz;
+                unit_dir<NDIM>(kdir, x, y, z, nx, ny, nz, ux, uy, uz, sx, sy, sz);
+                const double* pd = a.prefdir + 3 * (is ? rs : rt);
+                float c = __fmul_rn(ux, (float)__ldg(pd));
+                c = __fmaf_rn(uy, (float)__ldg(pd + 1), c);
+                c = __fmaf_rn(uz, (float)__ldg(pd + 2), c);
+                chemo = __fadd_rn(chemo, __fmul_rn(-lam, c));
+              }
+            }
             // act next: lambda and max of the target type, of the source type
             // for a medium target
-            if (ACT && act_rec) {  // uniform over the tile
+            if (EXT && act_rec) {  // uniform over the tile
               const int ta = tt ? tt : ts;
               const float lam = __ldg(&P->act_lambda[ta]);
               const int amax_a = __ldg(&P->act_max[ta]);
@@ -714,7 +752,7 @@ __global__ void __launch_bounds__(kSweepThreadsMax, 1)
             const int y = class_coord(ny, cy, j0 + qy);
             const int z = NDIM == 3 ? class_coord(nz, cz, l0 + qz) : 0;
             const long long site = ((long long)z * ny + y) * nx + x;
-            if (ACT) {  // written after the phase
+            if (EXT && a.act_on) {  // written after the phase
               const unsigned j = atomicAdd(&s_pend, 1u);
               if ((long long)j < a.pend_cap) {
                 const long long e = (long long)blockIdx.x * a.pend_cap + j;
@@ -797,7 +835,7 @@ __global__ void __launch_bounds__(kSweepThreadsMax, 1)
         __syncthreads();
         if (tid == 0) s_cnt[prv] = 0;
         if (!grid_barrier(a.ctl, ++episode, &s_ok)) return;
-        if (ACT) {  // the slot's copies land before the next slot reads
+        if (EXT && a.act_on) {  // the slot's copies land before the next slot reads
           apply_pending(tick);
           __syncthreads();
           if (tid == 0) s_pend = 0;
@@ -837,7 +875,7 @@ __global__ void __launch_bounds__(kSweepThreadsMax, 1)
             run_tile(pt, r, local, cx, cy, cz, tick, phase);
           __syncthreads();
           if (tid == 0) s_cnt[prv] = 0;
-          if (ACT) {
+          if (EXT && a.act_on) {
             apply_pending(tick);
             __syncthreads();
             if (tid == 0) s_pend = 0;
@@ -1041,6 +1079,127 @@ __global__ void lr_backward_kernel(const float* __restrict__ scores,
   }
 }
 
+// ---- 3D persistence ----------------------------------------------------------
+__device__ __forceinline__ int find_row_replica(const DevReplica* reps, int nrep, long long row) {
+  int lo = 0, hi = nrep - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(&reps[mid].cell_off) <= row)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+// Initial preferred directions: uniform on the sphere, by rejection from the
+// cube [-1, 1)^3 with Philox draws of counter (cell, 0xFFFFFFF0 - try,
+// stream, 0xFFFFFFFF) (outside the sweep's phases), normalised in double.
+// The reference draws normalised Gaussians from std::random_device
+// (src/cpm.cu:226-248).
+__global__ void init_prefdir_kernel(double* prefdir, const DevReplica* __restrict__ reps,
+                                    int nrep, long long rows, unsigned long long seed,
+                                    unsigned stream0) {
+  const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < rows;
+       row += (long long)gridDim.x * blockDim.x) {
+    const int r = find_row_replica(reps, nrep, row);
+    const uint32_t cell = (uint32_t)(row - __ldg(&reps[r].cell_off));
+    double d[3] = {1.0, 0.0, 0.0};
+    for (uint32_t tr = 0; tr < 64; ++tr) {
+      uint32_t c0 = cell, c1 = 0xFFFFFFF0u - tr, c2 = stream0 + (uint32_t)r, c3 = 0xFFFFFFFFu;
+      philox4x32_10(c0, c1, c2, c3, k0, k1);
+      const double x = (double)(c0 >> 8) * 0x1p-23 - 1.0;
+      const double y = (double)(c1 >> 8) * 0x1p-23 - 1.0;
+      const double z = (double)(c2 >> 8) * 0x1p-23 - 1.0;
+      const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
+      if (r2 > 0.0 && r2 <= 1.0) {
+        const double l = __dsqrt_rn(r2);
+        d[0] = __ddiv_rn(x, l);
+        d[1] = __ddiv_rn(y, l);
+        d[2] = __ddiv_rn(z, l);
+        break;
+      }
+    }
+    prefdir[3 * row + 0] = d[0];
+    prefdir[3 * row + 1] = d[1];
+    prefdir[3 * row + 2] = d[2];
+  }
+}
+
+// Mean coordinate of a cell on one axis, in [0, n): exact sum / area.
+__device__ __forceinline__ double mean_coord(long long sum, long long area, int n) {
+  double m = __ddiv_rn((double)sum, (double)area);
+  m = __dsub_rn(m, __dmul_rn((double)n, floor(__ddiv_rn(m, (double)n))));
+  return m;
+}
+
+// hist slots [H][rows][3] all set to the cells' current mean coordinates
+// (the reference fills its history at every push, src/cpm.cu:578-583).
+__global__ void persist_fill_kernel(double* hist, int H, const unsigned long long* __restrict__ ap,
+                                    const long long* __restrict__ cs,
+                                    const DevReplica* __restrict__ reps, int nrep, long long rows) {
+  for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < rows;
+       row += (long long)gridDim.x * blockDim.x) {
+    const int r = find_row_replica(reps, nrep, row);
+    const long long area = unpack_area(__ldg(ap + row));
+    const int dims[3] = {__ldg(&reps[r].nx), __ldg(&reps[r].ny), __ldg(&reps[r].nz)};
+    for (int k = 0; k < 3; ++k) {
+      const double m = area > 0 ? mean_coord(__ldg(cs + 3 * row + k), area, dims[k]) : 0.0;
+      for (int h = 0; h < H; ++h) hist[((long long)h * rows + row) * 3 + k] = m;
+    }
+  }
+}
+
+// After a run: the current mean goes into history slot `slot`; the mean of
+// slot (slot + 1) % H (H runs ago, the oldest) gives the displacement d.
+// As src/kernels.cu:159-212: d is divided by its length taken before the
+// per-axis wrap into (-n/2, n/2], then the preferred direction becomes
+// normalize(d (1 - p) + pref p) with p the cell type's diffusion; cells with
+// no displacement (or no sites) keep theirs.  Double precision throughout.
+__global__ void persist_update_kernel(double* prefdir, double* hist, int H, int slot,
+                                      const unsigned long long* __restrict__ ap,
+                                      const long long* __restrict__ cs,
+                                      const int* __restrict__ ctype,
+                                      const DevParams* __restrict__ params,
+                                      const DevReplica* __restrict__ reps, int nrep,
+                                      long long rows) {
+  for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < rows;
+       row += (long long)gridDim.x * blockDim.x) {
+    const int r = find_row_replica(reps, nrep, row);
+    const long long cell = row - __ldg(&reps[r].cell_off);
+    const long long area = unpack_area(__ldg(ap + row));
+    const int dims[3] = {__ldg(&reps[r].nx), __ldg(&reps[r].ny), __ldg(&reps[r].nz)};
+    double cur[3], d[3];
+    for (int k = 0; k < 3; ++k) {
+      cur[k] = area > 0 ? mean_coord(__ldg(cs + 3 * row + k), area, dims[k]) : 0.0;
+      hist[((long long)slot * rows + row) * 3 + k] = cur[k];
+    }
+    const int prev_slot = (slot + 1) % H;
+    for (int k = 0; k < 3; ++k)
+      d[k] = __dsub_rn(cur[k], hist[((long long)prev_slot * rows + row) * 3 + k]);
+    if (cell == 0 || area <= 0) continue;
+    const double len = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(d[0], d[0]), __dmul_rn(d[1], d[1])),
+                                            __dmul_rn(d[2], d[2])));
+    if (len == 0.0) continue;
+    const int ty = __ldg(ctype + row);
+    if (ty < 0 || ty >= kMaxTypes) continue;
+    const double p = (double)__ldg(&params[__ldg(&reps[r].pset)].persist_diff[ty]);
+    double np[3];
+    for (int k = 0; k < 3; ++k) {
+      double v = d[k];
+      if (v > (double)(dims[k] / 2)) v = __dsub_rn(v, (double)dims[k]);
+      if (v < (double)(-(dims[k] / 2))) v = __dadd_rn(v, (double)dims[k]);
+      v = __ddiv_rn(v, len);
+      np[k] = __dadd_rn(__dmul_rn(v, __dsub_rn(1.0, p)), __dmul_rn(prefdir[3 * row + k], p));
+    }
+    const double l2 = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(np[0], np[0]), __dmul_rn(np[1], np[1])),
+                                           __dmul_rn(np[2], np[2])));
+    if (l2 == 0.0) continue;
+    for (int k = 0; k < 3; ++k) prefdir[3 * row + k] = __ddiv_rn(np[k], l2);
+  }
+}
+
 // ---- sorting order parameter -------------------------------------------------
 // Per replica: number of Moore neighbour pairs (each pair once) of two
 // different non-medium cells, and how many of them join cells of different
@@ -1099,6 +1258,40 @@ cudaError_t launch_lr_backward(const float* scores, const float* dl_do,
   return cudaGetLastError();
 }
 
+namespace {
+int rows_grid(long long rows) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long want = (rows + 255) / 256;
+  return (int)std::max(1LL, std::min<long long>(want, (long long)sms * 8));
+}
+}  // namespace
+
+cudaError_t launch_init_prefdir(double* prefdir, const DevReplica* reps, int nrep,
+                                long long rows, unsigned long long seed, unsigned stream0,
+                                cudaStream_t s) {
+  init_prefdir_kernel<<<rows_grid(rows), 256, 0, s>>>(prefdir, reps, nrep, rows, seed, stream0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_persist_fill(double* hist, int H, const unsigned long long* ap,
+                                const long long* cs, const DevReplica* reps, int nrep,
+                                long long rows, cudaStream_t s) {
+  persist_fill_kernel<<<rows_grid(rows), 256, 0, s>>>(hist, H, ap, cs, reps, nrep, rows);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_persist_update(double* prefdir, double* hist, int H, int slot,
+                                  const unsigned long long* ap, const long long* cs,
+                                  const int* ctype, const DevParams* params,
+                                  const DevReplica* reps, int nrep, long long rows,
+                                  cudaStream_t s) {
+  persist_update_kernel<<<rows_grid(rows), 256, 0, s>>>(prefdir, hist, H, slot, ap, cs, ctype,
+                                                        params, reps, nrep, rows);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_observe_heterotypic(const uint32_t* lat, const DevReplica* reps,
                                        int nrep, long long total_sites,
                                        unsigned long long* counts, cudaStream_t s) {
@@ -1141,10 +1334,11 @@ int sweep_max_blocks_per_sm(int ndim, bool perim, int variant, bool scores) {
 
 cudaError_t launch_sweep(int ndim, bool perim, int variant, const SweepArgs& a,
                          int grid, cudaStream_t s, bool scores) {
-  if (a.act_on) variant = 0;  // the act kernels are built for variant 0
+  const bool ext = a.act_on || a.prefdir;
+  if (ext) variant = 0;  // the extended-term kernels are built for variant 0
   const SweepShape sh = sweep_shape(ndim, variant);
-  const void* fn = sweep_fn(ndim, perim, variant, scores && !a.act_on, a.act_on != 0);
-  if (scores || a.act_on) {  // these kernels get their shared-memory attribute on first use
+  const void* fn = sweep_fn(ndim, perim, variant, scores && !ext, ext);
+  if (scores || ext) {  // these kernels get their shared-memory attribute on first use
     const cudaError_t e = cudaFuncSetAttribute(
         fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem);
     if (e != cudaSuccess) return e;

@@ -149,6 +149,11 @@ extern "C" int cpm_sweep_static(int dimensionality, int nx, int ny, int nz,
   if (!lattice || !area || !perimeter || !centroid_sums || !params)
     return fail(CPM_ERR_INVALID, "cpm_sweep_static: NULL buffer or params");
   if (mcs < 0) return fail(CPM_ERR_INVALID, "cpm_sweep_static: mcs must be >= 0");
+  for (int k = 0; k < kMaxTypes; ++k)
+    if (params->chemotaxis[k] != 0.0f || params->act_lambda[k] != 0.0f ||
+        params->persistence_lambda[k] != 0.0f)
+      return fail(CPM_ERR_UNSUPPORTED,
+                  "cpm_sweep_static: chemotaxis, act and persistence need a handle engine");
   const long long rows = (long long)number_of_cells + 1;
   cudaStream_t s = (cudaStream_t)stream;
 

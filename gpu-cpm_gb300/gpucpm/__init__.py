@@ -29,8 +29,12 @@ Differences from the reference, all deliberate:
   * the act model's geometric means use this library's own FP32 log2 /
     exp2 (the reference uses the fast __powf), and copies of runs with an
     act lambda are written at the end of their phase (see cpm_set_act).
-The persistence term is not part of this engine: setting it raises
-CpmError.
+  * persistence (3D only, as in the reference) draws the initial preferred
+    directions from (seed, stream) instead of std::random_device, and its
+    energy is summed in FP32 like chemotaxis.  Cpm.run makes one engine run
+    per inner_iterations chunk when persistence is on, because the
+    preferred directions are updated once per engine run (the reference
+    updates them once per launch of its run loop).
 """
 import ctypes
 import os
@@ -102,7 +106,13 @@ class StaticParams(ctypes.Structure):
                 ("target_perimeter", ctypes.c_int * MAX_TYPES),
                 ("temperature", ctypes.c_float),
                 ("stickiness", ctypes.c_float * (MAX_TYPES * MAX_TYPES)),
-                ("fixed", ctypes.c_int * MAX_TYPES)]
+                ("fixed", ctypes.c_int * MAX_TYPES),
+                ("chemotaxis", ctypes.c_float * MAX_TYPES),
+                ("act_lambda", ctypes.c_float * MAX_TYPES),
+                ("act_max", ctypes.c_int * MAX_TYPES),
+                ("persistence_lambda", ctypes.c_float * MAX_TYPES),
+                ("persistence_diffusion", ctypes.c_float * MAX_TYPES),
+                ("persistence_time", ctypes.c_int * MAX_TYPES)]
 
 
 class _DeviceArray:
@@ -157,6 +167,13 @@ def library():
                            ctypes.POINTER(ctypes.c_int64)],
         "cpm_has_act": [H, ctypes.POINTER(ctypes.c_int)],
         "cpm_set_chemotaxis_r": [H, ctypes.c_int, ctypes.c_int, ctypes.c_float],
+        "cpm_set_persistence": [H, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float],
+        "cpm_set_persistence_r": [H, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                  ctypes.c_float],
+        "cpm_set_history": [H, ctypes.c_int],
+        "cpm_has_persistence": [H, ip, ip],
+        "cpm_get_persistence_r": [H, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p],
+        "cpm_set_persistence_state_r": [H, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p],
         "cpm_host_field_r": [H, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p),
                              ctypes.POINTER(ctypes.c_int64)],
         "cpm_set_fixed_r": [H, ctypes.c_int, ctypes.c_int, ctypes.c_int],
@@ -281,6 +298,51 @@ class _Engine:
         buf = (ctypes.c_int32 * n.value).from_address(ptr.value)
         buf._owner = self
         return np.ctypeslib.as_array(buf).reshape(tuple(self._replica_shape(replica)))
+
+    def set_history(self, history):
+        """Slots of the mean-coordinate ring of the persistence update (the
+        reference's `history` constructor argument), >= 1."""
+        self._call("cpm_set_history", int(history))
+
+    @property
+    def history(self):
+        v = ctypes.c_int()
+        self._call("cpm_has_persistence", None, ctypes.byref(v))
+        return v.value
+
+    @property
+    def persistence_exists(self):
+        """Whether preferred directions exist (a 3D run with persistence)."""
+        v = ctypes.c_int()
+        self._call("cpm_has_persistence", ctypes.byref(v), None)
+        return bool(v.value)
+
+    def persistence_state(self, replica=0):
+        """(prefdir [ncells+1, 3], history [history, ncells+1, 3] oldest
+        first), float64 copies; None while no persistence state exists."""
+        if not self.persistence_exists:
+            return None
+        n1 = self._ncells(replica) + 1
+        pd = np.empty((n1, 3), np.float64)
+        hist = np.empty((self.history, n1, 3), np.float64)
+        self._call("cpm_get_persistence_r", int(replica), pd.ctypes.data, hist.ctypes.data)
+        return pd, hist
+
+    def set_persistence_state(self, replica, prefdir, history=None):
+        """Restore a replica's preferred directions (and optionally its
+        ring, oldest slot first); the engine must be pushed and 3D."""
+        n1 = self._ncells(replica) + 1
+        pd = np.ascontiguousarray(prefdir, np.float64)
+        if pd.shape != (n1, 3):
+            raise CpmError(CPM_ERR_INVALID, f"prefdir must have shape ({n1}, 3)")
+        hp = None
+        if history is not None:
+            hist = np.ascontiguousarray(history, np.float64)
+            if hist.shape != (self.history, n1, 3):
+                raise CpmError(CPM_ERR_INVALID,
+                               f"history must have shape ({self.history}, {n1}, 3)")
+            hp = hist.ctypes.data
+        self._call("cpm_set_persistence_state_r", int(replica), pd.ctypes.data, hp)
 
     @property
     def act_exists(self):
@@ -480,6 +542,8 @@ class Cpm(_Engine):
         self.has_field = bool(has_field)
         self.has_act = bool(has_act)
         self._shape = (self.dimension,) * self.dimensionality
+        self._persistence = False
+        self.set_history(history)
 
     def _ncells(self, replica):
         return self.number_of_cells
@@ -501,13 +565,12 @@ class Cpm(_Engine):
         engine raise CpmError.
         """
         ct = int(cell_type)
-        unsupported = []
         if (lambda_persistence != -1 and persistence_diffusion != -1
                 and persistence_time != -1):
-            unsupported.append("persistence")
-        if unsupported:
-            raise CpmError(CPM_ERR_UNSUPPORTED,
-                           "terms not modelled by this engine: " + ", ".join(unsupported))
+            self._call("cpm_set_persistence", ct, int(persistence_time),
+                       float(persistence_diffusion), float(lambda_persistence))
+            if float(lambda_persistence) != 0.0:
+                self._persistence = True
         if lambda_perimeter != -1 and target_perimeter != -1:
             self._call("cpm_set_perimeter", ct, int(target_perimeter), float(lambda_perimeter))
         if lambda_area != -1 and target_area != -1:
@@ -559,7 +622,10 @@ class Cpm(_Engine):
         if inner <= 0:
             raise CpmError(CPM_ERR_INVALID, "inner_iterations must be positive")
         total = (int(iterations) // inner) * inner
-        if total > 0:
+        if self._persistence and self.dimensionality == 3:
+            for _ in range(total // inner):  # one direction update per chunk
+                self.run_mcs(inner)
+        elif total > 0:
             self.run_mcs(total)
 
     def get_state(self):
@@ -645,6 +711,16 @@ class Batch(_Engine):
             self._call("cpm_set_act", int(cell_type), int(max_act), float(lam))
         else:
             self._call("cpm_set_act_r", int(replica), int(cell_type), int(max_act), float(lam))
+
+    def set_persistence(self, replica, cell_type, time, diffusion, lam):
+        """Persistence of a type (3D): lambda, diffusion and the stored-only
+        time.  Preferred directions change once per run_mcs call."""
+        if replica is None:
+            self._call("cpm_set_persistence", int(cell_type), int(time), float(diffusion),
+                       float(lam))
+        else:
+            self._call("cpm_set_persistence_r", int(replica), int(cell_type), int(time),
+                       float(diffusion), float(lam))
 
     def set_chemotaxis(self, replica, cell_type, lam):
         if replica is None:

@@ -12,6 +12,11 @@ Carlo time).  The file holds:
   params         uint8 [P, sizeof(StaticParams)]: each parameter record once
   param_index    [R]: the record of each replica
   tick, seed, stream_id
+  act            uint32, the act stamps (only when the engine has them)
+  prefdir, history, history_size   the persistence state: preferred
+                 directions [rows, 3] and the mean-coordinate ring
+                 [history_size, rows, 3] oldest slot first, rows of all
+                 replicas concatenated (only when the engine has it)
 
 Area and perimeter are recomputed by the push on load and checked against
 the file; centroid sums are restored as saved (they record which periodic
@@ -25,7 +30,7 @@ import numpy as np
 
 from . import CPM_ERR_INVALID, CpmError, StaticParams
 
-FORMAT = 1
+FORMAT = 2
 
 
 def save(engine, path):
@@ -48,18 +53,27 @@ def save(engine, path):
     params = np.stack([np.frombuffer(bytes(engine.get_params(first[int(u)])), np.uint8)
                        for u in uniq])
     seed, stream_id = engine.seed
+    extra = {}
+    if getattr(engine, "act_exists", False):
+        extra["act"] = np.concatenate([engine.act_lattice(r).view(np.uint32).ravel()
+                                       for r in range(n)])
+    if getattr(engine, "persistence_exists", False):
+        states = [engine.persistence_state(r) for r in range(n)]
+        extra["prefdir"] = np.concatenate([s[0] for s in states])
+        extra["history"] = np.concatenate([s[1] for s in states], axis=1)
+        extra["history_size"] = np.array([engine.history], np.int64)
     np.savez(path, format=np.array([FORMAT]), dimensionality=np.array([engine.dimensionality]),
              shapes=np.array(shapes, np.int64), ncells=np.array(ncells, np.int64),
              lattice=np.concatenate(lats), area=np.concatenate(areas),
              perimeter=np.concatenate(perims), centroid_sums=np.concatenate(css),
              params=params, param_index=inverse.astype(np.int64),
              tick=np.array([engine.tick], np.uint64), seed=np.array([seed], np.uint64),
-             stream_id=np.array([stream_id], np.uint64))
+             stream_id=np.array([stream_id], np.uint64), **extra)
 
 
 def load(engine, path):
     d = np.load(path)
-    if int(d["format"][0]) != FORMAT:
+    if int(d["format"][0]) not in (1, FORMAT):
         raise CpmError(CPM_ERR_INVALID, f"unknown checkpoint format {int(d['format'][0])}")
     n = engine.n_replicas
     shapes, ncells = d["shapes"], d["ncells"]
@@ -74,7 +88,12 @@ def load(engine, path):
     for r in range(n):
         view = engine.host_lattice(r)
         view[...] = lat[off:off + view.size].view(np.int32).reshape(view.shape)
+        if "act" in d.files:  # pushed with the lattice
+            act = engine.act_lattice(r)
+            act[...] = d["act"][off:off + view.size].view(np.int32).reshape(act.shape)
         off += view.size
+    if "history_size" in d.files:
+        engine.set_history(int(d["history_size"][0]))
     params = d["params"]
     index = d["param_index"]
 
@@ -99,6 +118,9 @@ def load(engine, path):
             raise CpmError(CPM_ERR_INVALID, f"replica {r}: the tables of the checkpoint do "
                                             "not describe its lattice")
         engine.set_centroid_sums(r, cs[rows:rows + n1])
+        if "prefdir" in d.files:
+            engine.set_persistence_state(r, d["prefdir"][rows:rows + n1],
+                                         d["history"][:, rows:rows + n1])
         rows += n1
     engine.tick = int(d["tick"][0])
     engine.set_seed(int(d["seed"][0]), int(d["stream_id"][0]))

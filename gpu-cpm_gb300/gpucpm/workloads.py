@@ -46,6 +46,9 @@ class Workload:
     field: np.ndarray = None     # float64 [ndim, (nz,) ny, nx] chemotaxis field, or None
     act_lambda: np.ndarray = None  # float32 [ntypes]: act lambdas, or None
     act_max: np.ndarray = None     # int32 [ntypes]: act maxima, or None
+    persist_lambda: np.ndarray = None  # float32 [ntypes]: persistence lambdas (3D), or None
+    persist_diff: np.ndarray = None    # float32 [ntypes]: persistence diffusion, or None
+    history: int = 1                   # mean-coordinate ring slots (engine-wide)
 
     @property
     def ndim(self):
@@ -78,6 +81,8 @@ class Workload:
         if self.field is not None:
             view = engine.field(0 if replica is None else replica)
             view[...] = self.field
+        if self.persist_lambda is not None and self.history != engine.history:
+            engine.set_history(self.history)
         for a in range(nt):
             if self.act_lambda is not None and self.act_lambda[a] != 0:
                 mx = int(self.act_max[a]) if self.act_max is not None else 0
@@ -90,6 +95,12 @@ class Workload:
                     engine._call("cpm_set_chemotaxis", a, float(self.chemo[a]))
                 else:
                     engine.set_chemotaxis(replica, a, float(self.chemo[a]))
+            if self.persist_lambda is not None and self.persist_lambda[a] != 0:
+                df = float(self.persist_diff[a]) if self.persist_diff is not None else 0.0
+                if replica is None:
+                    engine._call("cpm_set_persistence", a, 0, df, float(self.persist_lambda[a]))
+                else:
+                    engine.set_persistence(replica, a, 0, df, float(self.persist_lambda[a]))
             if self.fixed is not None and self.fixed[a]:
                 if replica is None:
                     engine._call("cpm_set_fixed", a, 1)
@@ -107,7 +118,8 @@ class Workload:
                     lam_perim=self.lam_perim, tgt_perim=self.tgt_perim,
                     temperature=self.temperature, stick=self.stick, fixed=self.fixed,
                     chemo=self.chemo, field=self.field, act_lambda=self.act_lambda,
-                    act_max=self.act_max)
+                    act_max=self.act_max, persist_lambda=self.persist_lambda,
+                    persist_diff=self.persist_diff, history=self.history)
 
 
 def _params(nt, J, lam_area=0.0, tgt_area=0, lam_perim=0.0, tgt_perim=0):

@@ -145,6 +145,40 @@ int cpm_has_act(const cpm_handle* h, int* has);
 int cpm_set_chemotaxis(cpm_handle* h, int type, float lambda);
 int cpm_set_chemotaxis_r(cpm_handle* h, int replica, int type, float lambda);
 
+/* Replaces Cpm::setPersistence (src/cpm.cu:112-116), 3D only as in the
+ * reference (its 2D kernels have no such term).  An attempt adds
+ * -lambda * (d . p) to dH, d the unit copy direction (nearest image) and p
+ * the preferred direction of the source cell (of the target when the source
+ * is the medium); lambda is the source type's (the target's when the source
+ * is the medium), src/kernels3d.cu:327-343.  After every cpm_run /
+ * cpm_run_graph call (one launch of the reference's run loop,
+ * src/cpm.cu:486-510) each cell's mean coordinate goes into a ring of
+ * `history` slots and p <- normalize(d' (1 - diffusion) + p diffusion), d'
+ * the displacement since the oldest slot divided by its length before the
+ * per-axis wrap (src/kernels.cu:159-212).  `time` is stored and read back
+ * only: the reference uses it in a host update that its run loop no longer
+ * calls (src/cpm.cu:599-648).  Preferred directions start uniform on the
+ * sphere, drawn from (seed, stream id) on first use. */
+int cpm_set_persistence(cpm_handle* h, int type, int time, float diffusion, float lambda);
+int cpm_set_persistence_r(cpm_handle* h, int replica, int type, int time, float diffusion,
+                          float lambda);
+
+/* The reference's `history` constructor argument (src/python_wrapper.cpp:
+ * 27-41): slots of the mean-coordinate ring, >= 1 (default 1, with which the
+ * displacement is always zero and p never changes, as in the reference).
+ * Changing it refills the ring from the current tables. */
+int cpm_set_history(cpm_handle* h, int history);
+
+/* Persistence state of replica r for checkpoints: prefdir[(ncells+1)*3] and
+ * the ring history[history][(ncells+1)*3], oldest slot first (double).
+ * Either pointer may be NULL.  The getter fails with CPM_ERR_STATE when the
+ * engine has no persistence state yet (cpm_has_persistence); the setter
+ * creates it on a pushed 3D engine. */
+int cpm_get_persistence_r(cpm_handle* h, int replica, double* prefdir, double* history);
+int cpm_set_persistence_state_r(cpm_handle* h, int replica, const double* prefdir,
+                                const double* history);
+int cpm_has_persistence(const cpm_handle* h, int* has, int* history);
+
 /* Replaces Cpm::setFixed (src/cpm.cu:150-153).  Cells of a fixed type never
  * move: an attempt whose target belongs to one does nothing, and one whose
  * source belongs to one proposes the medium instead (src/kernels2d.cu:
@@ -396,6 +430,13 @@ struct cpm_static_params {
     float temperature;
     float stickiness[CPM_MAX_TYPES * CPM_MAX_TYPES]; /* as cpm_set_stickiness */
     int fixed[CPM_MAX_TYPES];                        /* as cpm_set_fixed */
+    /* handle engines only: cpm_sweep_static refuses non-zero lambdas here */
+    float chemotaxis[CPM_MAX_TYPES];                 /* as cpm_set_chemotaxis */
+    float act_lambda[CPM_MAX_TYPES];                 /* as cpm_set_act */
+    int act_max[CPM_MAX_TYPES];
+    float persistence_lambda[CPM_MAX_TYPES];         /* as cpm_set_persistence */
+    float persistence_diffusion[CPM_MAX_TYPES];
+    int persistence_time[CPM_MAX_TYPES];
 };
 
 /* No counterpart in the reference.  Runs `mcs` Monte Carlo steps of the same

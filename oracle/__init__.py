@@ -34,6 +34,8 @@ class Params(ctypes.Structure):
         ("act_lambda", ctypes.c_float * MAX_TYPES),
         ("act_max", ctypes.c_int * MAX_TYPES),
         ("act", ctypes.c_void_p),
+        ("persist_lambda", ctypes.c_float * MAX_TYPES),
+        ("prefdir", ctypes.c_void_p),
     ]
 
 
@@ -80,6 +82,12 @@ def lib():
                               ctypes.c_int, ctypes.c_void_p]
         l.orc_run_scores.argtypes = l.orc_run.argtypes + [ctypes.c_void_p,
                                                           ctypes.c_void_p]
+        l.orc_init_prefdir.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32,
+                                       ctypes.c_int, ctypes.c_void_p]
+        l.orc_mean_coords.argtypes = [ctypes.POINTER(Params), ctypes.c_void_p,
+                                      ctypes.c_void_p, ctypes.c_void_p]
+        l.orc_persist_update.argtypes = [ctypes.POINTER(Params)] + [ctypes.c_void_p] * 6 + [
+            ctypes.c_int, ctypes.c_int]
         _lib = l
     return _lib
 
@@ -114,13 +122,18 @@ class OracleSim:
     unmovable types, chemo (optional, per type) the chemotaxis lambdas,
     field (optional, [ndim, (nz,) ny, nx]) the chemotaxis field, act_lambda /
     act_max (optional, per type) the act model and act (optional) its
-    starting stamps (kept in self.act).
+    starting stamps (kept in self.act).  persist_lambda / persist_diff
+    (optional, per type, 3D) the persistence term with a ring of `history`
+    mean-coordinate slots: self.prefdir [ncells+1, 3] starts from
+    (seed, stream) and every run() call ends with one update, as every
+    engine run call does.
     """
 
     def __init__(self, lattice, ncells, J, lam_area, tgt_area,
                  lam_perim=None, tgt_perim=None, temperature=1.0, seed=0,
                  stream=0, stick=None, fixed=None, chemo=None, field=None,
-                 act_lambda=None, act_max=None, act=None):
+                 act_lambda=None, act_max=None, act=None, persist_lambda=None,
+                 persist_diff=None, history=1):
         lat = np.ascontiguousarray(lattice, dtype=np.uint32).copy()
         self.ndim = lat.ndim
         self.lattice = lat
@@ -175,6 +188,19 @@ class OracleSim:
             self.act = (np.zeros(lat.shape, np.uint32) if act is None
                         else np.ascontiguousarray(act, dtype=np.uint32).copy())
             p.act = self.act.ctypes.data
+        fill(p.persist_lambda, persist_lambda, np.float32)
+        self.persist_diff = np.zeros(MAX_TYPES, np.float32)
+        if persist_diff is not None:
+            d = np.asarray(persist_diff, np.float32).ravel()
+            self.persist_diff[:d.size] = d
+        self.prefdir = None
+        persist = (self.ndim == 3 and persist_lambda is not None
+                   and np.any(np.asarray(persist_lambda) != 0))
+        if persist:
+            self.prefdir = np.zeros((self.ncells + 1, 3), np.float64)
+            lib().orc_init_prefdir(ctypes.c_uint64(int(seed)), ctypes.c_uint32(int(stream)),
+                                   ctypes.c_uint32(0), self.ncells, self.prefdir.ctypes.data)
+            p.prefdir = self.prefdir.ctypes.data
         self.params = p
         n1 = self.ncells + 1
         self.area = np.zeros(n1, np.int32)
@@ -188,6 +214,22 @@ class OracleSim:
                                     self.csum.ctypes.data)
         if err:
             raise ValueError(f"invalid lattice (oracle error bits {err})")
+        if self.prefdir is not None:
+            # the type of every id (-1 for ids without sites), and every
+            # history slot holding the means at the start
+            self.ctype = np.full(self.ncells + 1, -1, np.int32)
+            self.ctype[self.lattice.ravel() & 0xFFFFFF] = self.lattice.ravel() >> 24
+            self.history = int(history)
+            self.hist = np.empty((self.history, self.ncells + 1, 3), np.float64)
+            self.hist[:] = self.mean_coords()
+            self.hist_slot = 0
+
+    def mean_coords(self):
+        """[ncells+1, 3] mean coordinate of every cell, in [0, n) per axis."""
+        out = np.zeros((self.ncells + 1, 3), np.float64)
+        lib().orc_mean_coords(ctypes.byref(self.params), self.area.ctypes.data,
+                              self.csum.ctypes.data, out.ctypes.data)
+        return out
 
     def run(self, mcs: int, nthreads: int = 0):
         lib().orc_run(ctypes.byref(self.params), self.lattice.ctypes.data,
@@ -195,6 +237,12 @@ class OracleSim:
                       self.csum.ctypes.data, self.tick, int(mcs),
                       int(nthreads), self.counters.ctypes.data)
         self.tick += int(mcs)
+        if self.prefdir is not None and int(mcs) > 0:
+            lib().orc_persist_update(ctypes.byref(self.params), self.area.ctypes.data,
+                                     self.csum.ctypes.data, self.ctype.ctypes.data,
+                                     self.persist_diff.ctypes.data, self.prefdir.ctypes.data,
+                                     self.hist.ctypes.data, self.history, self.hist_slot)
+            self.hist_slot = (self.hist_slot + 1) % self.history
         return self
 
     def run_scores(self, mcs: int, spec, nthreads: int = 0):

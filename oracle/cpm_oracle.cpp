@@ -85,6 +85,10 @@ struct Params {
   float act_lambda[kMaxTypes];
   int act_max[kMaxTypes];
   uint32_t* act;
+  // persistence (3D, src/kernels3d.cu:327-343): lambda per type and the
+  // preferred direction of every cell ([ncells+1][3] doubles, or null)
+  float persist_lambda[kMaxTypes];
+  const double* prefdir;
 };
 
 // log2(v), v >= 1, and 2^y in FP32, the library's own (act model): log2 by
@@ -160,11 +164,12 @@ float act_mean(const Params& p, const uint32_t* lat, int x, int y, int z, uint32
   return exp2_own(sum / (float)count);
 }
 
-// Unit copy direction (target minus source) dotted with the field at the
-// source site: the raw difference of wrapped coordinates in 2D
-// (src/kernels2d.cu:302-309), the nearest image in 3D (src/kernels3d.cu:
-// 275-299); FP32, rounded step by step.
-float chemo_dot(const Params& p, int x, int y, int z, int kdir) {
+// Unit copy direction (target minus source): the raw difference of wrapped
+// coordinates in 2D (src/kernels2d.cu:302-309), the nearest image in 3D
+// (src/kernels3d.cu:275-299); FP32, rounded step by step.  Returns the
+// source site's index.
+int64_t unit_dir(const Params& p, int x, int y, int z, int kdir, float& ux, float& uy,
+                 float& uz) {
   int ox, oy, oz;
   if (p.ndim == 2) {
     const int m = kdir + (kdir >= 4);
@@ -194,11 +199,31 @@ float chemo_dot(const Params& p, int x, int y, int z, int kdir) {
   s2 = std::fma(fy, fy, s2);
   if (p.ndim == 3) s2 = std::fma(fz, fz, s2);
   const float len = std::sqrt(s2);
-  const int64_t sites = (int64_t)nx * ny * nz;
-  const int64_t site = ((int64_t)sz * ny + sy) * nx + sx;
-  float c = (fx / len) * p.field[site];
-  c = std::fma(fy / len, p.field[sites + site], c);
-  if (p.ndim == 3) c = std::fma(fz / len, p.field[2 * sites + site], c);
+  ux = fx / len;
+  uy = fy / len;
+  uz = p.ndim == 3 ? fz / len : 0.0f;
+  return ((int64_t)sz * ny + sy) * nx + sx;
+}
+
+// The unit copy direction dotted with the chemotaxis field at the source.
+float chemo_dot(const Params& p, int x, int y, int z, int kdir) {
+  float ux, uy, uz;
+  const int64_t site = unit_dir(p, x, y, z, kdir, ux, uy, uz);
+  const int64_t sites = (int64_t)p.nx * p.ny * (p.ndim == 3 ? p.nz : 1);
+  float c = ux * p.field[site];
+  c = std::fma(uy, p.field[sites + site], c);
+  if (p.ndim == 3) c = std::fma(uz, p.field[2 * sites + site], c);
+  return c;
+}
+
+// The unit copy direction dotted with a preferred direction, each component
+// rounded to FP32 (persistence, src/kernels3d.cu:327-343).
+float persist_dot(const Params& p, int x, int y, int z, int kdir, const double* pd) {
+  float ux, uy, uz;
+  unit_dir(p, x, y, z, kdir, ux, uy, uz);
+  float c = ux * (float)pd[0];
+  c = std::fma(uy, (float)pd[1], c);
+  c = std::fma(uz, (float)pd[2], c);
   return c;
 }
 
@@ -391,6 +416,12 @@ inline int attempt(const Params& p, uint32_t* lat, const Tables& tb, int x,
     float chemo = 0.0f;
     const float lam = p.chemo[ts ? ts : tt];
     if (lam != 0.0f && p.field) chemo = -lam * chemo_dot(p, x, y, z, kdir);
+    if (p.prefdir && p.ndim == 3) {  // persistence next: the source cell's
+      // direction and type, the target's for a medium source
+      const float lamP = p.persist_lambda[ts ? ts : tt];
+      const uint32_t own = (s & 0xFFFFFFu) ? (s & 0xFFFFFFu) : (t & 0xFFFFFFu);
+      if (lamP != 0.0f) chemo = chemo + -lamP * persist_dot(p, x, y, z, kdir, p.prefdir + 3 * own);
+    }
     if (p.act) {  // act next: of the target type, of the source type for a medium target
       const int ta = tt ? tt : ts;
       const float lamA = p.act_lambda[ta];
@@ -687,6 +718,94 @@ int orc_run_scores(const orc_params* pp, uint32_t* lat, int32_t* area,
                    double* scores) {
   return run_impl(pp, lat, area, perim, csum, tick0, mcs, nthreads, counters,
                   static_cast<const ScoreSpec*>(spec), scores);
+}
+
+// Initial preferred directions of cells 0..ncells of replica `replica`:
+// uniform on the sphere (the reference normalises three normal deviates,
+// src/cpm.cu:224-251; this library draws by rejection in the cube instead).
+// Try k of cell c uses the Philox block (c, 0xFFFFFFF0 - k, stream +
+// replica, 0xFFFFFFFF): x, y, z = (word >> 8) * 2^-23 - 1 from its first
+// three words, kept when 0 < |v|^2 <= 1; (1, 0, 0) after 64 failed tries.
+void orc_init_prefdir(uint64_t seed, uint32_t stream, uint32_t replica, int ncells,
+                      double* prefdir) {
+  for (int c = 0; c <= ncells; ++c) {
+    double d[3] = {1.0, 0.0, 0.0};
+    for (uint32_t k = 0; k < 64; ++k) {
+      uint32_t w[4] = {(uint32_t)c, 0xFFFFFFF0u - k, stream + replica, 0xFFFFFFFFu};
+      philox4x32_10(w, (uint32_t)seed, (uint32_t)(seed >> 32));
+      const double x = (double)(w[0] >> 8) * 0x1p-23 - 1.0;
+      const double y = (double)(w[1] >> 8) * 0x1p-23 - 1.0;
+      const double z = (double)(w[2] >> 8) * 0x1p-23 - 1.0;
+      const double r2 = x * x + y * y + z * z;
+      if (r2 > 0.0 && r2 <= 1.0) {
+        const double l = std::sqrt(r2);
+        d[0] = x / l;
+        d[1] = y / l;
+        d[2] = z / l;
+        break;
+      }
+    }
+    std::memcpy(prefdir + 3 * c, d, sizeof d);
+  }
+}
+
+// Mean coordinate of every cell on every axis, in [0, n): sum / area
+// reduced modulo n (0 for cells without sites).  out[(ncells+1)*3].
+void orc_mean_coords(const orc_params* pp, const int32_t* area, const int64_t* csum,
+                     double* out) {
+  const Params& p = *pp;
+  const int dims[3] = {p.nx, p.ny, p.nz};
+  for (int c = 0; c <= p.ncells; ++c)
+    for (int k = 0; k < 3; ++k) {
+      double m = 0.0;
+      if (area[c] > 0) {
+        m = (double)csum[3 * c + k] / (double)area[c];
+        m = m - (double)dims[k] * std::floor(m / (double)dims[k]);
+      }
+      out[3 * c + k] = m;
+    }
+}
+
+// One preferred-direction update after a run (src/cpm.cu:486-510,
+// src/kernels.cu:159-212): the current means go into history slot `slot`
+// (hist [H][ncells+1][3]); the displacement d from slot (slot + 1) % H is
+// divided by its length taken before the per-axis wrap into (-n/2, n/2],
+// and p <- normalize(d (1 - diff) + p diff), diff of the cell's type
+// (ctype[c], -1 for none).  Cell 0, empty cells and zero displacements keep
+// their direction.
+void orc_persist_update(const orc_params* pp, const int32_t* area, const int64_t* csum,
+                        const int32_t* ctype, const float* diffusion, double* prefdir,
+                        double* hist, int H, int slot) {
+  const Params& p = *pp;
+  const int n1 = p.ncells + 1;
+  const int dims[3] = {p.nx, p.ny, p.nz};
+  std::vector<double> cur((size_t)n1 * 3);
+  orc_mean_coords(pp, area, csum, cur.data());
+  const int prev = (slot + 1) % H;
+  for (int c = 0; c < n1; ++c) {
+    double d[3];
+    for (int k = 0; k < 3; ++k) {
+      hist[((int64_t)slot * n1 + c) * 3 + k] = cur[3 * c + k];
+      d[k] = cur[3 * c + k] - hist[((int64_t)prev * n1 + c) * 3 + k];
+    }
+    if (c == 0 || area[c] <= 0) continue;
+    const double len = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    if (len == 0.0) continue;
+    const int ty = ctype[c];
+    if (ty < 0 || ty >= kMaxTypes) continue;
+    const double q = (double)diffusion[ty];
+    double np[3];
+    for (int k = 0; k < 3; ++k) {
+      double v = d[k];
+      if (v > (double)(dims[k] / 2)) v = v - (double)dims[k];
+      if (v < (double)(-(dims[k] / 2))) v = v + (double)dims[k];
+      v = v / len;
+      np[k] = v * (1.0 - q) + prefdir[3 * c + k] * q;
+    }
+    const double l2 = std::sqrt(np[0] * np[0] + np[1] * np[1] + np[2] * np[2]);
+    if (l2 == 0.0) continue;
+    for (int k = 0; k < 3; ++k) prefdir[3 * c + k] = np[k] / l2;
+  }
 }
 
 }  // extern "C"

@@ -133,12 +133,15 @@ def test_push_rejects_invalid_lattices(engine_lib):
     sim.synchronize()
 
 
-def test_unsupported_terms_and_bad_arguments(engine_lib):
+def test_optional_terms_and_bad_arguments(engine_lib):
     import gpucpm
     sim = gpucpm.Cpm(32, 2, 4, 10, False)
-    with pytest.raises(gpucpm.CpmError, match="persistence"):
-        sim.set_constraints(cell_type=1, lambda_persistence=1.0, persistence_diffusion=0.5,
-                            persistence_time=10)
+    # persistence is accepted in 2D and has no effect there, as in the reference
+    sim.set_constraints(cell_type=1, lambda_persistence=1.0, persistence_diffusion=0.5,
+                        persistence_time=10)
+    assert not sim.persistence_exists
+    with pytest.raises(gpucpm.CpmError):
+        sim.set_history(0)
     # chemotaxis needs the field, which exists (zero) once asked for
     sim.set_constraints(cell_type=1, lambda_chemotaxis=1.0)
     with pytest.raises(gpucpm.CpmError):

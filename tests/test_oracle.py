@@ -1,6 +1,7 @@
 """CPU tests of the oracle: known-answer vectors, exp error bound, table
 recount on hand-computed lattices, hand-computed dH against the reference's
 formula, invariants after sweeps and thread-count independence."""
+import ctypes
 import math
 
 import numpy as np
@@ -478,3 +479,93 @@ def test_act_mcs_matches_restatement():
     np.testing.assert_array_equal(sim.lattice, lat)
     np.testing.assert_array_equal(sim.act, act)
     np.testing.assert_array_equal(sim.area, area)
+
+
+def test_initial_preferred_directions():
+    """Unit vectors, a pure function of (seed, stream + replica), spread
+    over the sphere (the reference draws normalised normal deviates,
+    src/cpm.cu:224-251)."""
+    lib = oracle.lib()
+    n = 3000
+    a = np.zeros((n + 1, 3))
+    b = np.zeros((n + 1, 3))
+    c = np.zeros((n + 1, 3))
+    lib.orc_init_prefdir(7, 3, 0, n, a.ctypes.data)
+    lib.orc_init_prefdir(7, 2, 1, n, b.ctypes.data)
+    lib.orc_init_prefdir(8, 3, 0, n, c.ctypes.data)
+    np.testing.assert_array_equal(a, b)  # stream + replica is one counter word
+    assert not np.array_equal(a, c)
+    np.testing.assert_allclose(np.linalg.norm(a, axis=1), 1.0, rtol=0, atol=1e-15)
+    assert np.linalg.norm(a.mean(axis=0)) < 0.06
+    np.testing.assert_allclose(np.abs(a).mean(axis=0), 0.5, atol=0.03)  # E|x| on the sphere
+
+
+def test_preferred_direction_update_known_answer():
+    """src/kernels.cu:159-212 restated with numpy: displacement from the
+    oldest ring slot, divided by its length taken BEFORE the per-axis wrap
+    into (-n/2, n/2], blended with the old direction by the diffusion and
+    normalised; the medium, empty cells and resting cells keep theirs."""
+    n = (10, 8, 12)
+    p = oracle.Params()
+    p.ndim, p.nx, p.ny, p.nz, p.ncells = 3, n[0], n[1], n[2], 4
+    area = np.array([900, 4, 5, 0, 3], np.int32)
+    rng = np.random.default_rng(4)
+    csum = rng.integers(-50, 200, size=(5, 3)).astype(np.int64)
+    csum[3] = 0
+    ctype = np.array([0, 1, 2, -1, 1], np.int32)
+    diff = np.zeros(32, np.float32)
+    diff[1], diff[2] = 0.75, 0.25
+    pref = rng.normal(size=(5, 3))
+    pref /= np.linalg.norm(pref, axis=1, keepdims=True)
+    H, slot = 3, 1
+    hist = rng.uniform(0, 8, size=(H, 5, 3))
+    cur = np.zeros((5, 3))
+    for c in range(5):
+        if area[c] > 0:
+            m = csum[c] / area[c]
+            cur[c] = m - np.array(n) * np.floor(m / np.array(n))
+    hist[(slot + 1) % H, 4] = cur[4]  # cell 4 has not moved since the oldest slot
+    want = pref.copy()
+    old = hist[(slot + 1) % H].copy()
+    for c in (1, 2):
+        d = cur[c] - old[c]
+        length = np.sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2])
+        w = d.copy()
+        for k in range(3):
+            if w[k] > n[k] // 2:
+                w[k] -= n[k]
+            if w[k] < -(n[k] // 2):
+                w[k] += n[k]
+        q = float(diff[ctype[c]])
+        v = (w / length) * (1 - q) + pref[c] * q
+        want[c] = v / np.sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2])
+    got, h2 = pref.copy(), hist.copy()
+    oracle.lib().orc_persist_update(ctypes.byref(p), area.ctypes.data, csum.ctypes.data,
+                                    ctype.ctypes.data, diff.ctypes.data, got.ctypes.data,
+                                    h2.ctypes.data, H, slot)
+    np.testing.assert_array_equal(got, want)
+    np.testing.assert_array_equal(h2[slot], cur)
+
+
+def test_persistence_steers_a_single_cell():
+    """A lone cell with a strong persistence term keeps going: its net
+    displacement over several direction updates is several times that of
+    the same cell without the term."""
+    nn = 20
+    z, y, x = np.mgrid[:nn, :nn, :nn]
+    lat = np.zeros((nn, nn, nn), np.uint32)
+    ball = (x - 10) ** 2 + (y - 10) ** 2 + (z - 10) ** 2 <= 9
+    lat[ball] = 1 | (1 << 24)
+    J = np.zeros((2, 2), np.float32)
+    J[0, 1] = J[1, 0] = 8.0
+    out = []
+    for lam in (0.0, 30.0):
+        s = oracle.OracleSim(lat, 1, J, [0, 2.0], [0, int(ball.sum())], temperature=8.0,
+                             persist_lambda=[0, lam], persist_diff=[0, 0.8], history=3,
+                             seed=1)
+        start = np.array([10.0, 10.0, 10.0])
+        for _ in range(10):
+            s.run(8)
+        m = s.csum[1] / s.area[1]
+        out.append(np.linalg.norm((m - start + nn / 2) % nn - nn / 2))
+    assert out[1] > 3 * max(out[0], 1.0), out
