@@ -1405,6 +1405,137 @@ int cpm_observe_heterotypic(cpm_handle* h, float* out_host) {
   return CPM_OK;
 }
 
+int cpm_seed_voronoi_r(cpm_handle* h, int r, int npoints, const double* points,
+                       const uint32_t* values) {
+  if (int rc = check_replica(h, r)) return rc;
+  CPM_BIND(h);
+  if (npoints < 1 || !points || !values)
+    return h->fail(CPM_ERR_INVALID, "cpm_seed_voronoi_r: need npoints >= 1, points, values");
+  const DevReplica& R = h->reps[r];
+  const int nd = h->ndim;
+  const int n[3] = {R.nx, R.ny, R.nz};
+  for (int k = 0; k < npoints; ++k) {
+    for (int a = 0; a < nd; ++a) {
+      const double p = points[(size_t)k * nd + a];
+      if (!(p >= 0.0 && p < (double)n[a]))
+        return h->fail(CPM_ERR_INVALID, "cpm_seed_voronoi_r: point %d lies outside [0, n)", k);
+    }
+    const uint32_t v = values[k], id = v & 0xFFFFFFu, ty = v >> 24;
+    if ((int)id > R.ncells || ty >= (uint32_t)kMaxTypes || (id == 0 && ty != 0))
+      return h->fail(CPM_ERR_INVALID,
+                     "cpm_seed_voronoi_r: value %d is not id <= ncells | type < 32 << 24 "
+                     "(id 0 with type 0)", k);
+  }
+  // Bucket grid with about two points per bucket.
+  VoronoiGrid vg;
+  vg.ndim = nd;
+  const double sites = (double)n[0] * n[1] * n[2];
+  const double side = std::pow(2.0 * sites / npoints, 1.0 / nd);
+  long long G = 1;
+  double wmin = 1e300;
+  vg.rmax = 0;
+  for (int a = 0; a < 3; ++a) {
+    vg.n[a] = n[a];
+    int g = a < nd ? (int)std::lround((double)n[a] / side) : 1;
+    g = std::max(1, std::min(g, n[a]));
+    vg.g[a] = g;
+    vg.w[a] = (double)n[a] / g;
+    if (a < nd) wmin = std::min(wmin, vg.w[a]);
+    vg.rmax = std::max(vg.rmax, g / 2 + 1);
+    G *= g;
+  }
+  vg.lb_scale = wmin;
+  // Counting sort of the points by bucket (host; O(npoints)).
+  std::vector<int> bucket_of(npoints), start(G + 1, 0);
+  for (int k = 0; k < npoints; ++k) {
+    long long b = 0;
+    for (int a = nd - 1; a >= 0; --a) {
+      int ba = (int)std::floor(points[(size_t)k * nd + a] / vg.w[a]);
+      ba = std::max(0, std::min(ba, vg.g[a] - 1));
+      b = b * vg.g[a] + ba;
+    }
+    bucket_of[k] = (int)b;
+    ++start[b + 1];
+  }
+  for (long long b = 0; b < G; ++b) start[b + 1] += start[b];
+  std::vector<double> pts((size_t)npoints * 3, 0.0);
+  std::vector<int> idx(npoints), fill(start.begin(), start.end() - 1);
+  for (int k = 0; k < npoints; ++k) {
+    const int slot = fill[bucket_of[k]]++;
+    for (int a = 0; a < nd; ++a) pts[(size_t)slot * 3 + a] = points[(size_t)k * nd + a];
+    idx[slot] = k;
+  }
+  double* d_pts = nullptr;
+  int *d_idx = nullptr, *d_start = nullptr;
+  uint32_t* d_val = nullptr;
+  cudaError_t e = cudaMallocAsync((void**)&d_pts, sizeof(double) * pts.size(), h->stream);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&d_idx, sizeof(int) * npoints, h->stream);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&d_val, sizeof(uint32_t) * npoints, h->stream);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&d_start, sizeof(int) * (G + 1), h->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_pts, pts.data(), sizeof(double) * pts.size(), cudaMemcpyHostToDevice,
+                        h->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_idx, idx.data(), sizeof(int) * npoints, cudaMemcpyHostToDevice,
+                        h->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_val, values, sizeof(uint32_t) * npoints, cudaMemcpyHostToDevice,
+                        h->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_start, start.data(), sizeof(int) * (G + 1), cudaMemcpyHostToDevice,
+                        h->stream);
+  if (e == cudaSuccess)
+    e = launch_voronoi(h->d_lat + R.lat_off, vg, d_pts, d_idx, d_val, d_start, h->stream);
+  h->launches += 1;
+  cudaFreeAsync(d_pts, h->stream);
+  cudaFreeAsync(d_idx, h->stream);
+  cudaFreeAsync(d_val, h->stream);
+  cudaFreeAsync(d_start, h->stream);
+  // the host vectors are read by the copies: wait before they go
+  const cudaError_t e2 = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return h->cuda_fail(e, "cpm_seed_voronoi_r");
+  if (e2 != cudaSuccess) return h->cuda_fail(e2, "cpm_seed_voronoi_r");
+  h->pushed = false;  // the tables no longer describe the lattice
+  return CPM_OK;
+}
+
+int cpm_observe_boundaries(cpm_handle* h, int ntypes, uint64_t* out_host) {
+  CPM_BIND(h);
+  if (ntypes < 1 || ntypes > kMaxTypes)
+    return h->fail(CPM_ERR_INVALID, "ntypes must be in [1, %d]", kMaxTypes);
+  if (!out_host) return h->fail(CPM_ERR_INVALID, "out_host is NULL");
+  std::vector<long long> tile_start(h->nrep + 1, 0);
+  for (int r = 0; r < h->nrep; ++r) {
+    const DevReplica& R = h->reps[r];
+    const long long sites = (long long)R.nx * R.ny * R.nz;
+    tile_start[r + 1] = tile_start[r] + (sites + kBoundaryTile - 1) / kBoundaryTile;
+  }
+  const long long ntiles = tile_start[h->nrep];
+  const size_t nc = (size_t)h->nrep * ntypes * ntypes;
+  unsigned long long* counts = nullptr;
+  long long* d_ts = nullptr;
+  cudaError_t e = cudaMallocAsync((void**)&counts, sizeof(unsigned long long) * nc, h->stream);
+  if (e == cudaSuccess)
+    e = cudaMallocAsync((void**)&d_ts, sizeof(long long) * (h->nrep + 1), h->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(counts, 0, sizeof(unsigned long long) * nc, h->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_ts, tile_start.data(), sizeof(long long) * (h->nrep + 1),
+                        cudaMemcpyHostToDevice, h->stream);
+  if (e == cudaSuccess)
+    e = launch_observe_boundaries(h->ndim, h->d_lat, h->d_reps, h->nrep, d_ts, ntiles, ntypes,
+                                  counts, h->stream);
+  h->launches += 1;
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(out_host, counts, sizeof(unsigned long long) * nc,
+                        cudaMemcpyDeviceToHost, h->stream);
+  cudaFreeAsync(counts, h->stream);
+  cudaFreeAsync(d_ts, h->stream);
+  const cudaError_t e2 = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return h->cuda_fail(e, "cpm_observe_boundaries");
+  if (e2 != cudaSuccess) return h->cuda_fail(e2, "cpm_observe_boundaries");
+  return CPM_OK;
+}
+
 int cpm_lr_backward(const float* scores, const float* dl_do, const float* obs,
                     const int* checkpoints, int nrep, int len, int nparam, int ncheck,
                     const float* obs_total, int nrep_total, float* grad, void* stream) {

@@ -252,6 +252,31 @@ cudaError_t launch_persist_update(double* prefdir, double* hist, int H, int slot
 cudaError_t launch_observe_heterotypic(const uint32_t* lat, const DevReplica* reps,
                                        int nrep, long long total_sites,
                                        unsigned long long* counts, cudaStream_t s);
+// Periodic Voronoi seeding of one lattice region (nx*ny*nz sites at `lat`):
+// every site takes values[k] of its nearest point (min-image Euclidean
+// distance in double, ties to the lowest k).  Points are binned in a
+// g[0]*g[1]*g[2] bucket grid of widths w[] (bucket-major order: pts[k*3+a],
+// idx[k] their original index, start[b]..start[b+1] bucket b's points).
+struct VoronoiGrid {
+  int n[3];         // lattice sides (n[2] = 1 in 2D)
+  int g[3];         // buckets per axis
+  double w[3];      // bucket widths n / g
+  double lb_scale;  // min(w): ring r bounds unscanned points at r * min(w)
+  int ndim;
+  int rmax;         // rings to scan at most (covers every bucket)
+};
+cudaError_t launch_voronoi(uint32_t* lat, const VoronoiGrid& vg, const double* pts,
+                           const int* idx, const uint32_t* values, const int* start,
+                           cudaStream_t s);
+// Boundary counts per replica and unordered type pair: Moore pairs (each
+// once) of sites with different values, counts[r*T*T + a*T + b] for a <= b
+// (types >= T are skipped).  tile_start: per replica the first of its tiles
+// of kBoundaryTile sites (nrep+1 entries).
+constexpr int kBoundaryTile = 4096;
+cudaError_t launch_observe_boundaries(int ndim, const uint32_t* lat, const DevReplica* reps,
+                                      int nrep, const long long* tile_start,
+                                      long long ntiles, int T, unsigned long long* counts,
+                                      cudaStream_t s);
 cudaError_t launch_barrier_probe(uint32_t* ctl, unsigned long long timeout_ns,
                                  cudaStream_t s);
 cudaError_t launch_init(int ndim, const uint32_t* lat, const DevReplica* reps,

@@ -1238,7 +1238,157 @@ __global__ void observe_heterotypic_kernel(const uint32_t* __restrict__ lat,
   }
 }
 
+// ---- periodic Voronoi seeding -------------------------------------------------
+// One thread per site.  Buckets are scanned ring by ring (Chebyshev distance
+// r in bucket units, wrapped; a bucket met twice through the wrap changes
+// nothing) until the best squared distance is below the squared lower bound
+// r * min(w) of every bucket not yet scanned, so the answer is the exact
+// brute-force nearest point with ties to the lowest index.
+__device__ __forceinline__ double min_image(double a, double b, int n) {
+  double d = fabs(__dsub_rn(a, b));
+  const double e = __dsub_rn((double)n, d);
+  return e < d ? e : d;
+}
+
+__global__ void voronoi_kernel(uint32_t* lat, VoronoiGrid vg, const double* __restrict__ pts,
+                               const int* __restrict__ idx, const uint32_t* __restrict__ values,
+                               const int* __restrict__ start) {
+  const long long sites = (long long)vg.n[0] * vg.n[1] * vg.n[2];
+  for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < sites;
+       s += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(s % vg.n[0]), y = (int)((s / vg.n[0]) % vg.n[1]),
+              z = (int)(s / ((long long)vg.n[0] * vg.n[1]));
+    const double c[3] = {(double)x, (double)y, (double)z};
+    int b[3];
+    for (int a = 0; a < 3; ++a) {
+      b[a] = (int)floor(__ddiv_rn(c[a], vg.w[a]));
+      b[a] = b[a] < 0 ? 0 : (b[a] >= vg.g[a] ? vg.g[a] - 1 : b[a]);
+    }
+    double best = 1e300;
+    int best_k = 0x7FFFFFFF;
+    uint32_t best_v = 0;
+    const int rz_max = vg.ndim == 3 ? 1 : 0;
+    for (int r = 0; r <= vg.rmax; ++r) {
+      for (int dz = -r * rz_max; dz <= r * rz_max; ++dz)
+        for (int dy = -r; dy <= r; ++dy)
+          for (int dx = -r; dx <= r; ++dx) {
+            const int ax = dx < 0 ? -dx : dx, ay = dy < 0 ? -dy : dy, az = dz < 0 ? -dz : dz;
+            const int cheb = ax > ay ? (ax > az ? ax : az) : (ay > az ? ay : az);
+            if (cheb != r) continue;  // the shell of ring r only
+            int bx = (b[0] + dx) % vg.g[0], by = (b[1] + dy) % vg.g[1],
+                bz = (b[2] + dz) % vg.g[2];
+            bx += bx < 0 ? vg.g[0] : 0;
+            by += by < 0 ? vg.g[1] : 0;
+            bz += bz < 0 ? vg.g[2] : 0;
+            const int bucket = (bz * vg.g[1] + by) * vg.g[0] + bx;
+            const int k1 = __ldg(start + bucket + 1);
+            for (int k = __ldg(start + bucket); k < k1; ++k) {
+              const double ddx = min_image(c[0], __ldg(pts + 3 * k), vg.n[0]);
+              const double ddy = min_image(c[1], __ldg(pts + 3 * k + 1), vg.n[1]);
+              double d2 = __dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy));
+              if (vg.ndim == 3) {
+                const double ddz = min_image(c[2], __ldg(pts + 3 * k + 2), vg.n[2]);
+                d2 = __dadd_rn(d2, __dmul_rn(ddz, ddz));
+              }
+              const int kk = __ldg(idx + k);
+              if (d2 < best || (d2 == best && kk < best_k)) {
+                best = d2;
+                best_k = kk;
+              }
+            }
+          }
+      // every bucket not scanned yet lies at periodic Chebyshev distance
+      // >= r + 1, so its points are at least r * min(w) away; the margin
+      // covers the rounding of the bucket indices
+      const double lb = __dsub_rn(__dmul_rn((double)r, vg.lb_scale), 1e-6);
+      if (best_k != 0x7FFFFFFF && lb > 0.0 && best < __dmul_rn(lb, lb)) break;
+    }
+    if (best_k != 0x7FFFFFFF) best_v = __ldg(values + best_k);
+    lat[s] = best_v;
+  }
+}
+
+// ---- boundary counts per type pair ------------------------------------------
+// A block takes tiles of kBoundaryTile sites of one replica, histograms the
+// pairs in shared memory and adds the non-zero bins to global memory.
+template <int NDIM>
+__global__ void observe_boundaries_kernel(const uint32_t* __restrict__ lat,
+                                          const DevReplica* __restrict__ reps, int nrep,
+                                          const long long* __restrict__ tile_start,
+                                          long long ntiles, int T,
+                                          unsigned long long* counts) {
+  extern __shared__ unsigned int hist[];  // T * T
+  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    int lo = 0, hi = nrep - 1;  // the replica owning tile t
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(tile_start + mid) <= t) lo = mid; else hi = mid - 1;
+    }
+    const int r = lo;
+    const DevReplica R = reps[r];
+    const long long sites = (long long)R.nx * R.ny * R.nz;
+    const long long first = (t - __ldg(tile_start + r)) * kBoundaryTile;
+    for (int i = threadIdx.x; i < T * T; i += blockDim.x) hist[i] = 0;
+    __syncthreads();
+    for (long long local = first + threadIdx.x;
+         local < sites && local < first + kBoundaryTile; local += blockDim.x) {
+      const int x = (int)(local % R.nx), y = (int)((local / R.nx) % R.ny),
+                z = (int)(local / ((long long)R.nx * R.ny));
+      const uint32_t v = lat[R.lat_off + local];
+      const int tv = (int)(v >> 24);
+      // forward half of the neighbourhood: offsets after (0,0,0) in
+      // (dz, dy, dx) row-major order
+      for (int m = (NDIM == 3 ? 14 : 5); m < (NDIM == 3 ? 27 : 9); ++m) {
+        const int ox = m % 3 - 1, oy = (m / 3) % 3 - 1, oz = NDIM == 3 ? m / 9 - 1 : 0;
+        int xx = x + ox, yy = y + oy, zz = z + oz;
+        xx = xx < 0 ? xx + R.nx : (xx >= R.nx ? xx - R.nx : xx);
+        yy = yy < 0 ? yy + R.ny : (yy >= R.ny ? yy - R.ny : yy);
+        zz = zz < 0 ? zz + R.nz : (zz >= R.nz ? zz - R.nz : zz);
+        const uint32_t w = lat[R.lat_off + ((long long)zz * R.ny + yy) * R.nx + xx];
+        if (w == v) continue;
+        const int tw = (int)(w >> 24);
+        if (tv >= T || tw >= T) continue;
+        const int a = tv < tw ? tv : tw, bb = tv < tw ? tw : tv;
+        atomicAdd(&hist[a * T + bb], 1u);
+      }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < T * T; i += blockDim.x)
+      if (hist[i]) atomicAdd(&counts[(long long)r * T * T + i], (unsigned long long)hist[i]);
+    __syncthreads();
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_voronoi(uint32_t* lat, const VoronoiGrid& vg, const double* pts,
+                           const int* idx, const uint32_t* values, const int* start,
+                           cudaStream_t s) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long sites = (long long)vg.n[0] * vg.n[1] * vg.n[2];
+  const int grid = (int)std::max(1LL, std::min<long long>((sites + 255) / 256, (long long)sms * 16));
+  voronoi_kernel<<<grid, 256, 0, s>>>(lat, vg, pts, idx, values, start);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_observe_boundaries(int ndim, const uint32_t* lat, const DevReplica* reps,
+                                      int nrep, const long long* tile_start, long long ntiles,
+                                      int T, unsigned long long* counts, cudaStream_t s) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int grid = (int)std::max(1LL, std::min<long long>(ntiles, (long long)sms * 8));
+  const size_t shm = sizeof(unsigned int) * T * T;
+  if (ndim == 2)
+    observe_boundaries_kernel<2><<<grid, 256, shm, s>>>(lat, reps, nrep, tile_start, ntiles, T,
+                                                        counts);
+  else
+    observe_boundaries_kernel<3><<<grid, 256, shm, s>>>(lat, reps, nrep, tile_start, ntiles, T,
+                                                        counts);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_lr_backward(const float* scores, const float* dl_do,
                                const float* obs, const int* checkpoints, int nrep,

@@ -216,6 +216,8 @@ def library():
         "cpm_run_scores": [H, ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int,
                            ctypes.POINTER(ScoreSpec)],
         "cpm_observe_heterotypic": [H, ctypes.c_void_p],
+        "cpm_observe_boundaries": [H, ctypes.c_int, ctypes.c_void_p],
+        "cpm_seed_voronoi_r": [H, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -508,6 +510,27 @@ class _Engine:
         out = np.empty(self.n_replicas, np.float32)
         self._call("cpm_observe_heterotypic", out.ctypes.data)
         return out
+
+    def boundary_counts(self, ntypes):
+        """uint64 [n_replicas, ntypes, ntypes]: Moore neighbour pairs (each
+        once) of sites with different values, by unordered type pair (a <= b)
+        — the boundary lengths between types, medium (type 0) included.
+        Read from the device lattices.  Synchronous."""
+        out = np.empty((self.n_replicas, int(ntypes), int(ntypes)), np.uint64)
+        self._call("cpm_observe_boundaries", int(ntypes), out.ctypes.data)
+        return out
+
+    def seed_voronoi(self, replica, points, values):
+        """Fill a replica's device lattice with the periodic Voronoi tiling of
+        `points` ([npoints, ndim] in [0, n), x first): each site takes
+        values[k] (id | type << 24) of its nearest point, ties to the lowest
+        k.  The tables are stale until recount() (or pull + push)."""
+        pts = np.ascontiguousarray(points, np.float64)
+        vals = np.ascontiguousarray(values, np.uint32)
+        if pts.ndim != 2 or pts.shape[1] != self.dimensionality or len(vals) != len(pts):
+            raise CpmError(CPM_ERR_INVALID, "points must be [npoints, ndim] with one value each")
+        self._call("cpm_seed_voronoi_r", int(replica), len(vals), pts.ctypes.data,
+                   vals.ctypes.data)
 
     def sweep_config(self):
         """dict(variant, tile, warps_per_block, grid, dispatch) of the launch

@@ -196,8 +196,9 @@ def sorting_grid(n=256, ncells=2600, size=5, seed=0, mcs=500, temperature=10.0):
                     {"n": n})
 
 
-def voronoi_labels(shape, npoints, rng):
-    """Periodic Voronoi labels 0..npoints-1 of every site of `shape`."""
+def voronoi_labels(shape, npoints, rng, return_points=False):
+    """Periodic Voronoi labels 0..npoints-1 of every site of `shape` (and the
+    points, [npoints, ndim] x first, when asked)."""
     from scipy.spatial import cKDTree
     dims = np.array(shape[::-1], np.float64)  # (nx, ny[, nz])
     pts = rng.random((npoints, len(shape))) * dims
@@ -209,7 +210,8 @@ def voronoi_labels(shape, npoints, rng):
     # meshgrid with indexing="ij" over (x, y[, z]) puts x slowest; bring the
     # labels back to row-major [z, y, x].
     lab = idx.reshape(tuple(int(d) for d in dims)).transpose()
-    return np.ascontiguousarray(lab).astype(np.int64)
+    lab = np.ascontiguousarray(lab).astype(np.int64)
+    return (lab, pts) if return_points else lab
 
 
 def _sym_uniform(nt, lo, hi, rng):
@@ -220,30 +222,32 @@ def _sym_uniform(nt, lo, hi, rng):
 def tissue_2d(n=4096, area=100, ntypes=3, seed=1, mcs=500):
     rng = _rng(seed)
     ncells = (n * n) // area
-    lab = voronoi_labels((n, n), ncells, rng)
+    lab, pts = voronoi_labels((n, n), ncells, rng, return_points=True)
     types = rng.integers(1, ntypes + 1, ncells)
-    lat = ((lab + 1) | (types[lab] << 24)).astype(np.uint32)
+    values = ((np.arange(ncells) + 1) | (types << 24)).astype(np.uint32)
+    lat = values[lab]
     J, la, ta, lp, tp = _params(ntypes + 1, _sym_uniform(ntypes + 1, 2.0, 20.0, rng),
                                 1.0, area, 0.5, 40)
     return Workload("tissue_2d", lat, ncells, J, la, ta, lp, tp, 20.0, mcs,
-                    {"n": n, "area": area})
+                    {"n": n, "area": area, "points": pts, "values": values})
 
 
 def tissue_3d(n=256, volume=500, fill=0.8, ntypes=2, seed=2, mcs=200):
     rng = _rng(seed)
     nreg = (n ** 3) // volume
-    lab = voronoi_labels((n, n, n), nreg, rng)
+    lab, pts = voronoi_labels((n, n, n), nreg, rng, return_points=True)
     is_cell = rng.random(nreg) < fill
     ids = np.zeros(nreg, np.int64)
     ncells = int(is_cell.sum())
     ids[is_cell] = np.arange(1, ncells + 1)
     types = np.zeros(nreg, np.int64)
     types[is_cell] = rng.integers(1, ntypes + 1, ncells)
-    lat = (ids[lab] | (types[lab] << 24)).astype(np.uint32)
+    values = (ids | (types << 24)).astype(np.uint32)
+    lat = values[lab]
     J, la, ta, lp, tp = _params(ntypes + 1, _sym_uniform(ntypes + 1, 4.0, 16.0, rng),
                                 1.0, volume, 0.2, 350)
     return Workload("tissue_3d", lat, ncells, J, la, ta, lp, tp, 20.0, mcs,
-                    {"n": n, "volume": volume})
+                    {"n": n, "volume": volume, "points": pts, "values": values})
 
 
 def ensemble_2d(nrep=256, lo=64, hi=1024, sites_per_cell=50, seed=3, mcs=500):

@@ -394,6 +394,28 @@ int cpm_run_scores(cpm_handle* h, int mcs, float* d_scores, uint64_t score_base,
  * Synchronous. */
 int cpm_observe_heterotypic(cpm_handle* h, float* out_host);
 
+/* No counterpart in the reference (its examples draw cell boundaries with
+ * skimage on the host).  Boundary lengths of every replica's device lattice
+ * by unordered type pair: out_host[r*ntypes*ntypes + a*ntypes + b], a <= b,
+ * counts the Moore neighbour pairs (each pair once; 8 neighbours in 2D, 26
+ * in 3D) whose two sites hold different values and have types a and b
+ * (pairs with a type >= ntypes are skipped; entries with a > b stay 0).
+ * The sum over 1 <= a <= b is the number of cell-cell contacts, over
+ * 1 <= a < b the heterotypic ones (cpm_observe_heterotypic's ratio). */
+int cpm_observe_boundaries(cpm_handle* h, int ntypes, uint64_t* out_host);
+
+/* No counterpart in the reference (its examples paint squares on the host).
+ * Fills replica r's DEVICE lattice with a periodic Voronoi tiling of
+ * `npoints` points (host arrays): points[k*dimensionality + a] in [0, n_a)
+ * (x first), values[k] = id | type << 24 given to the sites whose nearest
+ * point (min-image Euclidean distance in double) is k, ties to the lowest
+ * k, so the result is the brute-force answer bit for bit.  Points are
+ * bucketed on the host and searched ring by ring on the device.  The tables
+ * are stale afterwards: cpm_recount (or cpm_pull, edit, cpm_push) must
+ * come before the next run. */
+int cpm_seed_voronoi_r(cpm_handle* h, int replica, int npoints, const double* points,
+                       const uint32_t* values);
+
 /* Backward of the likelihood-ratio estimator, on the GPU:
  *   grad[k] = sum_r sum_c dl_do[r][c] (obs[r][c] - b[r][c])
  *                     * sum_{t < checkpoints[c]} scores[r][t][k]

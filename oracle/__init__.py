@@ -82,6 +82,9 @@ def lib():
                               ctypes.c_int, ctypes.c_void_p]
         l.orc_run_scores.argtypes = l.orc_run.argtypes + [ctypes.c_void_p,
                                                           ctypes.c_void_p]
+        l.orc_voronoi.argtypes = [ctypes.c_int] * 5 + [ctypes.c_void_p] * 3
+        l.orc_boundaries.argtypes = [ctypes.c_int] * 4 + [ctypes.c_void_p, ctypes.c_int,
+                                                           ctypes.c_void_p]
         l.orc_init_prefdir.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32,
                                        ctypes.c_int, ctypes.c_void_p]
         l.orc_mean_coords.argtypes = [ctypes.POINTER(Params), ctypes.c_void_p,
@@ -270,3 +273,31 @@ class OracleSim:
         if err:
             raise ValueError(f"invalid lattice (oracle error bits {err})")
         return area, perim, csum
+
+
+def voronoi(shape, points, values):
+    """Brute-force periodic Voronoi lattice (uint32, shape [(nz,) ny, nx]):
+    each site takes values[k] of its nearest point (min-image distance in
+    double, ties to the lowest k); points [npoints, ndim], x first."""
+    shape = tuple(int(v) for v in shape)
+    ndim = len(shape)
+    nx, ny = shape[-1], shape[-2]
+    nz = shape[0] if ndim == 3 else 1
+    pts = np.ascontiguousarray(points, np.float64)
+    vals = np.ascontiguousarray(values, np.uint32)
+    out = np.zeros(shape, np.uint32)
+    lib().orc_voronoi(ndim, nx, ny, nz, len(vals), pts.ctypes.data, vals.ctypes.data,
+                      out.ctypes.data)
+    return out
+
+
+def boundaries(lattice, ntypes):
+    """[ntypes, ntypes] uint64 boundary counts by unordered type pair (a <= b)
+    of one lattice: Moore pairs, each once, of sites with different values."""
+    lat = np.ascontiguousarray(lattice, np.uint32)
+    ndim = lat.ndim
+    nx, ny = lat.shape[-1], lat.shape[-2]
+    nz = lat.shape[0] if ndim == 3 else 1
+    out = np.zeros((ntypes, ntypes), np.uint64)
+    lib().orc_boundaries(ndim, nx, ny, nz, lat.ctypes.data, int(ntypes), out.ctypes.data)
+    return out

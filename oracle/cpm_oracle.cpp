@@ -720,6 +720,62 @@ int orc_run_scores(const orc_params* pp, uint32_t* lat, int32_t* area,
                   static_cast<const ScoreSpec*>(spec), scores);
 }
 
+// Periodic Voronoi labels by brute force: site (x, y, z) takes values[k] of
+// the point with the smallest min-image squared distance, summed x, y, z in
+// double; ties go to the lowest k.  points[k*ndim + a], x first.
+void orc_voronoi(int ndim, int nx, int ny, int nz, int npoints, const double* points,
+                 const uint32_t* values, uint32_t* out) {
+  if (ndim == 2) nz = 1;
+  const int n[3] = {nx, ny, nz};
+  const int64_t sites = (int64_t)nx * ny * nz;
+  auto min_image = [](double a, double b, int len) {
+    const double d = std::fabs(a - b);
+    const double e = (double)len - d;
+    return e < d ? e : d;
+  };
+#pragma omp parallel for schedule(static)
+  for (int64_t s = 0; s < sites; ++s) {
+    const double c[3] = {(double)(s % nx), (double)((s / nx) % ny), (double)(s / ((int64_t)nx * ny))};
+    double best = 1e300;
+    int bk = -1;
+    for (int k = 0; k < npoints; ++k) {
+      double d2 = 0.0;
+      for (int a = 0; a < ndim; ++a) {
+        const double d = min_image(c[a], points[(int64_t)k * ndim + a], n[a]);
+        d2 = a == 0 ? d * d : d2 + d * d;
+      }
+      if (d2 < best) {
+        best = d2;
+        bk = k;
+      }
+    }
+    out[s] = bk >= 0 ? values[bk] : 0u;
+  }
+}
+
+// Boundary counts by unordered type pair: every Moore pair (each once: the
+// forward half of the neighbourhood of every site) of sites with different
+// values and types a, b < T adds 1 to out[min*T + max].
+void orc_boundaries(int ndim, int nx, int ny, int nz, const uint32_t* lat, int T,
+                    uint64_t* out) {
+  if (ndim == 2) nz = 1;
+  std::memset(out, 0, sizeof(uint64_t) * T * T);
+  for (int z = 0; z < nz; ++z)
+    for (int y = 0; y < ny; ++y)
+      for (int x = 0; x < nx; ++x) {
+        const uint32_t v = lat[((int64_t)z * ny + y) * nx + x];
+        for (int m = ndim == 3 ? 14 : 5; m < (ndim == 3 ? 27 : 9); ++m) {
+          const int ox = m % 3 - 1, oy = (m / 3) % 3 - 1, oz = ndim == 3 ? m / 9 - 1 : 0;
+          const int xx = (x + ox + nx) % nx, yy = (y + oy + ny) % ny, zz = (z + oz + nz) % nz;
+          const uint32_t w = lat[((int64_t)zz * ny + yy) * nx + xx];
+          if (w == v) continue;
+          const int a = (int)(v >> 24), b = (int)(w >> 24);
+          if (a >= T || b >= T) continue;
+          ++out[(a < b ? a : b) * T + (a < b ? b : a)];
+        }
+      }
+}
+
 // Initial preferred directions of cells 0..ncells of replica `replica`:
 // uniform on the sphere (the reference normalises three normal deviates,
 // src/cpm.cu:224-251; this library draws by rejection in the cube instead).

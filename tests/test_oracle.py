@@ -569,3 +569,41 @@ def test_persistence_steers_a_single_cell():
         m = s.csum[1] / s.area[1]
         out.append(np.linalg.norm((m - start + nn / 2) % nn - nn / 2))
     assert out[1] > 3 * max(out[0], 1.0), out
+
+
+@pytest.mark.parametrize("shape", [(40, 52), (12, 10, 14)])
+def test_oracle_voronoi_matches_kdtree_and_breaks_ties_low(shape):
+    """The brute-force labelling equals scipy's periodic k-d tree (the
+    workloads' seeding) on random points; with every point duplicated the
+    lower index of each pair wins."""
+    from scipy.spatial import cKDTree
+    rng = np.random.default_rng(len(shape))
+    dims = np.array(shape[::-1], np.float64)
+    pts = rng.random((90, len(shape))) * dims
+    vals = np.arange(1, 91, dtype=np.uint32)
+    lab = oracle.voronoi(shape, pts, vals)
+    grids = np.meshgrid(*[np.arange(d, dtype=np.float64) for d in shape[::-1]], indexing="ij")
+    coords = np.stack([g.ravel() for g in grids], axis=1)
+    _, idx = cKDTree(pts, boxsize=dims).query(coords, k=1)
+    kd = np.ascontiguousarray(idx.reshape(tuple(int(d) for d in dims)).transpose()) + 1
+    np.testing.assert_array_equal(lab, kd)
+    dup = np.concatenate([pts, pts])
+    lab2 = oracle.voronoi(shape, dup, np.arange(1, 181, dtype=np.uint32))
+    np.testing.assert_array_equal(lab2, lab)
+
+
+@pytest.mark.parametrize("shape", [(30, 26), (9, 11, 10)])
+def test_oracle_boundaries_match_numpy(shape):
+    w = W.random_small(shape, 20, ntypes=3, seed=7)
+    lat = w.lattice
+    T = 4
+    want = np.zeros((T, T), np.uint64)
+    offs = ([(0, 1), (1, -1), (1, 0), (1, 1)] if lat.ndim == 2 else
+            [(dz, dy, dx) for dz in (-1, 0, 1) for dy in (-1, 0, 1) for dx in (-1, 0, 1)
+             if (dz, dy, dx) > (0, 0, 0)])
+    for off in offs:
+        nb = np.roll(lat, tuple(-o for o in off), axis=tuple(range(lat.ndim)))
+        diff = nb != lat
+        a, b = (lat >> 24)[diff], (nb >> 24)[diff]
+        np.add.at(want, (np.minimum(a, b), np.maximum(a, b)), 1)
+    np.testing.assert_array_equal(oracle.boundaries(lat, T), want)
