@@ -1294,10 +1294,13 @@ int cpm_autotune(cpm_handle* h, int probe_mcs, int* chosen, float* ms_per_mcs) {
   float best = -1.0f;
   int best_v = h->variant, best_d = h->dispatch;
   const bool any_perim = any_perimeter(h);
-  // Every (tile variant, dispatch) pair; replica dispatch only for batches.
+  // Every (tile variant, dispatch) pair, replica dispatch only for batches,
+  // timed in three rounds (the fastest run counts): a variant's first launch
+  // also loads its module, and clocks may still be rising.
   const int ndispatch = h->nrep > 1 ? 2 : 1;
-  for (int i = 0; i < kTileVariants * ndispatch && e == cudaSuccess; ++i) {
-    const int v = i % kTileVariants, d = i / kTileVariants;
+  const int npairs = kTileVariants * ndispatch;
+  for (int i = 0; i < 3 * npairs && e == cudaSuccess; ++i) {
+    const int v = (i % npairs) % kTileVariants, d = (i % npairs) / kTileVariants;
     SweepArgs a = sweep_args(h, v, d);
     a.tick0 = tick;
     a.mcs = probe_mcs;

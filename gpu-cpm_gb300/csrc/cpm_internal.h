@@ -32,8 +32,14 @@
 namespace gpucpm {
 
 constexpr int kMaxTypes = 32;
-constexpr int kMaxSweepWarps = 24;  // warps per sweep block (one block per SM)
-constexpr int kSweepThreadsMax = 32 * kMaxSweepWarps;
+// Warps per sweep block (one block per SM): 24 at 80 registers in 2D; 20 at
+// 96 registers in 3D, whose 26-neighbour attempt would spill at 80.
+constexpr int kMaxSweepWarps = 24;
+constexpr int kMaxSweepWarps3d = 20;
+template <int NDIM>
+constexpr int max_sweep_warps() {
+  return NDIM == 3 ? kMaxSweepWarps3d : kMaxSweepWarps;
+}
 constexpr int kSweepSmemMax = 227 * 1024;  // usable shared memory per block
 constexpr int kInitThreads = 256;
 

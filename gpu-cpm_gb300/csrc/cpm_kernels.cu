@@ -128,11 +128,11 @@ struct WarpSmem {
 };
 
 // Warps per block of a variant: as many warp tiles as fit in shared memory,
-// at most kMaxSweepWarps (the register file's limit at 80 registers).
+// at most max_sweep_warps (the register file's limit).
 template <int NDIM, int V>
 constexpr int variant_warps() {
   const size_t w = kSweepSmemMax / sizeof(WarpSmem<NDIM, V>);
-  return w < (size_t)kMaxSweepWarps ? (int)w : kMaxSweepWarps;
+  return w < (size_t)max_sweep_warps<NDIM>() ? (int)w : max_sweep_warps<NDIM>();
 }
 
 template <int NDIM, int V>
@@ -336,7 +336,7 @@ __device__ __forceinline__ void flush_scores(const SweepArgs& a, float* sc, int 
 // end of its phase.  Kept apart so that the other kernels carry none of its
 // registers.
 template <int NDIM, bool PERIM, int V, bool SCORE, bool EXT = false>
-__global__ void __launch_bounds__(kSweepThreadsMax, 1)
+__global__ void __launch_bounds__(32 * max_sweep_warps<NDIM>(), 1)
     sweep_kernel(const SweepArgs a) {
   using G = TileGeom<NDIM, V>;
   using S = Stage<NDIM, V>;
@@ -353,8 +353,6 @@ __global__ void __launch_bounds__(kSweepThreadsMax, 1)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int wpb = blockDim.x >> 5;  // warps (tiles in flight) per block
   WarpSmem<NDIM, V>& ws = reinterpret_cast<WarpSmem<NDIM, V>*>(smem_raw)[warp];
-  const int gwarp = blockIdx.x * wpb + warp;
-  const int nwarps = gridDim.x * wpb;
   const uint32_t k0 = (uint32_t)a.seed, k1 = (uint32_t)(a.seed >> 32);
   int* err = reinterpret_cast<int*>(&a.ctl[kCtlErr]);
   // (kernel-parameter arrays are selected with ?: rather than indexed with
@@ -826,9 +824,23 @@ __global__ void __launch_bounds__(kSweepThreadsMax, 1)
         const unsigned long long phase = tick * NSLOTS + (unsigned long long)slot;
         const int* pre = a.task_prefix + slot * (a.nrep + 1);
         const int ntiles = __ldg(pre + a.nrep);
-        for (int task = gwarp; task < ntiles; task += nwarps) {
-          const int r = find_task_replica(pre, a.nrep, task);
-          run_tile(pt, r, task - __ldg(pre + r), cx, cy, cz, tick, phase);
+        // One lattice: each block takes one contiguous run of the slot's
+        // tiles (rows of tiles in raster order), the same band in every
+        // phase, so the band's lines and most of its halo stay with this
+        // SM's side of L2.  Batches: tiles dealt round-robin over all warps
+        // (the light edge tiles of ragged replicas would unbalance bands).
+        if (a.nrep == 1) {
+          const int per_b = ntiles / (int)gridDim.x, extra = ntiles % (int)gridDim.x;
+          const int tb0 = (int)blockIdx.x * per_b + min((int)blockIdx.x, extra);
+          const int tb1 = tb0 + per_b + ((int)blockIdx.x < extra ? 1 : 0);
+          for (int task = tb0 + warp; task < tb1; task += wpb)
+            run_tile(pt, 0, task, cx, cy, cz, tick, phase);
+        } else {
+          for (int task = (int)blockIdx.x * wpb + warp; task < ntiles;
+               task += (int)gridDim.x * wpb) {
+            const int r = find_task_replica(pre, a.nrep, task);
+            run_tile(pt, r, task - __ldg(pre + r), cx, cy, cz, tick, phase);
+          }
         }
         // The replayed list is consumed; every attempt of the slot is done
         // once all blocks pass the barrier.

@@ -295,6 +295,8 @@ int cpm_run_graph(cpm_handle* h, int mcs);
 
 /* Project autotuner: times `probe_mcs` MCS of every compiled tile variant
  * (warp tile shape and warps per block), under both dispatches for a batch,
+ * three times each (the fastest run counts: a first launch also loads its
+ * module; a GPU coming out of idle should be warmed up first),
  * on a saved copy of the current state, restores the state, and makes the
  * fastest pair the one later runs use.  The sweep's result does not depend
  * on either choice.  *chosen (may be NULL) receives the variant,
