@@ -348,6 +348,7 @@ __global__ void __launch_bounds__(32 * max_sweep_warps<NDIM>(), 1)
   __shared__ unsigned s_cnt[2];
   __shared__ unsigned long long s_tick0;
   __shared__ int s_claim;
+  __shared__ unsigned s_next[2];  // next unclaimed tile of the phase (parity of claim_phase)
   __shared__ unsigned s_pend;  // (act runs) entries on this block's pending list
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -368,6 +369,7 @@ __global__ void __launch_bounds__(32 * max_sweep_warps<NDIM>(), 1)
   int sc_rep = -1;
   unsigned long long sc_tick = 0;
   if (tid < 2) s_cnt[tid] = 0;
+  if (NDIM == 3 && tid < 2) s_next[tid] = 0;
   if (tid == 0) s_pend = 0;
   // Every block reads *tick_ptr before its first barrier arrival, and block
   // 0 advances it only after its last barrier, so all blocks see one value.
@@ -809,6 +811,26 @@ __global__ void __launch_bounds__(32 * max_sweep_warps<NDIM>(), 1)
     __syncwarp();  // the tile buffers are rewritten by the next tile
   };
 
+  // The block's tiles of one phase.  3D: warp w starts with tile w, then
+  // claims the next unclaimed one from a shared counter, so the phase ends
+  // within one tile on every warp (a 256^3 slot gives a block ~54 tiles of
+  // 20 warps: 2.7 rounds).  Counter claim_phase % 2 serves this phase; the
+  // other one was last used before the previous barrier and is cleared for
+  // the next phase.  2D: warp-strided (2D blocks hold a whole number of
+  // rounds on the large lattices, and the claim costs the 2D kernel a spill).
+  unsigned claim_phase = 0;
+  auto claimed_tiles = [&](int count, auto&& body) {
+    unsigned* ctr = &s_next[claim_phase & 1u];
+    if (tid == 0) s_next[(claim_phase + 1u) & 1u] = 0u;
+    ++claim_phase;
+    for (int k = warp; k < count;) {
+      body(k);
+      unsigned v = 0;
+      if (lane == 0) v = atomicAdd(ctr, 1u);
+      k = wpb + (int)__shfl_sync(kFull, v, 0);
+    }
+  };
+
   if (!a.block_local) {
     // Grid dispatch: the tiles of a slot, over all replicas, are dealt out
     // to every warp of the grid; one grid barrier ends each phase.
@@ -833,8 +855,13 @@ __global__ void __launch_bounds__(32 * max_sweep_warps<NDIM>(), 1)
           const int per_b = ntiles / (int)gridDim.x, extra = ntiles % (int)gridDim.x;
           const int tb0 = (int)blockIdx.x * per_b + min((int)blockIdx.x, extra);
           const int tb1 = tb0 + per_b + ((int)blockIdx.x < extra ? 1 : 0);
-          for (int task = tb0 + warp; task < tb1; task += wpb)
-            run_tile(pt, 0, task, cx, cy, cz, tick, phase);
+          if constexpr (NDIM == 3) {
+            claimed_tiles(tb1 - tb0,
+                          [&](int k) { run_tile(pt, 0, tb0 + k, cx, cy, cz, tick, phase); });
+          } else {
+            for (int task = tb0 + warp; task < tb1; task += wpb)
+              run_tile(pt, 0, task, cx, cy, cz, tick, phase);
+          }
         } else {
           for (int task = (int)blockIdx.x * wpb + warp; task < ntiles;
                task += (int)gridDim.x * wpb) {
@@ -883,8 +910,12 @@ __global__ void __launch_bounds__(32 * max_sweep_warps<NDIM>(), 1)
           const unsigned long long phase = tick * NSLOTS + (unsigned long long)slot;
           const int* pre = a.task_prefix + slot * (a.nrep + 1);
           const int ntiles = __ldg(pre + r + 1) - __ldg(pre + r);
-          for (int local = warp; local < ntiles; local += wpb)
-            run_tile(pt, r, local, cx, cy, cz, tick, phase);
+          if constexpr (NDIM == 3) {
+            claimed_tiles(ntiles, [&](int k) { run_tile(pt, r, k, cx, cy, cz, tick, phase); });
+          } else {
+            for (int local = warp; local < ntiles; local += wpb)
+              run_tile(pt, r, local, cx, cy, cz, tick, phase);
+          }
           __syncthreads();
           if (tid == 0) s_cnt[prv] = 0;
           if (EXT && a.act_on) {
