@@ -177,8 +177,10 @@ __device__ __forceinline__ bool grid_barrier(
             break;
           }
         }
-        __nanosleep(nap);
-        if (nap < 256) nap <<= 1;
+        if (spins > 64) {  // (polls are L2 round trips: most waits end before)
+          __nanosleep(nap);
+          if (nap < 128) nap <<= 1;
+        }
       }
     }
     __threadfence();
