@@ -130,3 +130,24 @@ def test_boundaries_3d(engine_lib):
     c = e.boundary_counts(4)[0]
     e.pull_from_gpu()
     np.testing.assert_array_equal(c, oracle.boundaries(e.lattice(0).view(np.uint32), 4))
+
+
+def test_voronoi_seeds_one_replica_of_a_batch(engine_lib):
+    """Seeding replica 1 writes only its own lattice region."""
+    import gpucpm
+    shapes = [(20, 24), (31, 26), (17, 17)]
+    b = gpucpm.Batch(2, [s[::-1] for s in shapes], [30, 40, 10])
+    for r in range(3):
+        b.lattice(r)[...] = 0
+    b.push_to_gpu()
+    rng = np.random.default_rng(9)
+    pts = rng.random((40, 2)) * np.array(shapes[1][::-1], np.float64)
+    vals = ((np.arange(40) + 1) | (2 << 24)).astype(np.uint32)
+    b.seed_voronoi(1, pts, vals)
+    b.recount()
+    b.synchronize()
+    b.pull_from_gpu()
+    np.testing.assert_array_equal(b.lattice(1).view(np.uint32), oracle.voronoi(shapes[1], pts, vals))
+    assert not b.lattice(0).any() and not b.lattice(2).any()
+    area, _, _ = b.tables(1)
+    assert area[1:].sum() == shapes[1][0] * shapes[1][1]

@@ -264,3 +264,71 @@ def test_set_constraints_act_and_get_act_state(engine_lib):
                            act_lambda=[0, 40], act_max=[0, 20]).run(30)
     np.testing.assert_array_equal(sim.get_state().view(np.uint32), ref.lattice)
     np.testing.assert_array_equal(st.view(np.uint32), ref.act)
+
+
+def _all_terms(w, seed):
+    """Every Hamiltonian term at once: fixed type 3, stickiness, chemotaxis,
+    act, persistence (3D) on top of adhesion, area and perimeter."""
+    nt = w.J.shape[0]
+    _with_terms(w, 3 if nt > 3 else None, [(1, 2), (2, 1), (1, 0)], seed)
+    w.chemo = np.array([0.0, 3.0, -2.0, 1.0][:nt], np.float32)
+    w.field = _smooth_field(w.lattice.shape, seed=seed)
+    _with_act(w, [0.0, 25.0, 0.0, 10.0][:nt], [0, 14, 0, 6][:nt])
+    if w.ndim == 3:
+        w.persist_lambda = np.array([0.0, 6.0, -4.0, 0.0][:nt], np.float32)
+        w.persist_diff = np.array([0.0, 0.5, 0.2, 0.0][:nt], np.float32)
+        w.history = 2
+    return w
+
+
+@pytest.mark.parametrize("shape", [(46, 40), (13, 12, 14)])
+def test_all_terms_together_match_oracle(engine_lib, shape):
+    w = _all_terms(W.random_small(shape, 26 if len(shape) == 2 else 18, ntypes=3,
+                                  seed=190 + len(shape), temperature=9.0), seed=5)
+    e = make_engine(w, seed=12, stream=4)
+    sim = oracle.OracleSim(w.lattice, w.ncells, **w.oracle_kwargs(), seed=12, stream=4)
+    for k in (3, 2, 4):
+        e.run_mcs(k)
+        sim.run(k)
+    finish(e)
+    assert_same(e, sim)
+    np.testing.assert_array_equal(e.act_lattice(0).view(np.uint32), sim.act)
+    if len(shape) == 3:
+        pd, hist = e.persistence_state(0)
+        np.testing.assert_array_equal(pd, sim.prefdir)
+        np.testing.assert_array_equal(hist, np.roll(sim.hist, -sim.hist_slot, axis=0))
+
+
+@pytest.mark.parametrize("dims,dispatch", [(2, "grid"), (2, "replica"), (3, "grid"),
+                                           (3, "replica")])
+def test_all_terms_batch_matches_oracle(engine_lib, dims, dispatch):
+    """Replicas with diverging records (one without act, one without
+    chemotaxis) under both dispatches."""
+    import gpucpm
+    shapes = [(40, 36), (33, 45), (30, 30)] if dims == 2 else [(12, 11, 13), (14, 10, 12)]
+    ws = [_all_terms(W.random_small(s, 18, ntypes=3, seed=200 + i, temperature=8.0 + i),
+                     seed=i) for i, s in enumerate(shapes)]
+    ws[0].act_lambda = None
+    ws[1].chemo = None
+    b = gpucpm.Batch(dims, [w.lattice.shape[::-1] for w in ws], [w.ncells for w in ws])
+    for r, w in enumerate(ws):
+        b.lattice(r)[...] = w.lattice.view(np.int32)
+        w.apply(b, replica=r)
+    b.set_seed(3, 9)
+    b.set_dispatch(gpucpm.DISPATCH_GRID if dispatch == "grid" else gpucpm.DISPATCH_REPLICA)
+    b.push_to_gpu()
+    sims = [oracle.OracleSim(w.lattice, w.ncells, **w.oracle_kwargs(), seed=3, stream=9 + r)
+            for r, w in enumerate(ws)]
+    for k in (2, 3):
+        b.run_mcs(k)
+        for s in sims:
+            s.run(k)
+    finish(b)
+    for r, s in enumerate(sims):
+        np.testing.assert_array_equal(b.lattice(r).view(np.uint32), s.lattice)
+        area, perim, cs = b.tables(r)
+        np.testing.assert_array_equal(area, s.area)
+        np.testing.assert_array_equal(perim, s.perim)
+        np.testing.assert_array_equal(cs, s.csum)
+        if s.act is not None:
+            np.testing.assert_array_equal(b.act_lattice(r).view(np.uint32), s.act)
