@@ -1448,6 +1448,8 @@ int cpm_seed_voronoi_r(cpm_handle* h, int r, int npoints, const double* points,
     G *= g;
   }
   vg.lb_scale = wmin;
+  if (G > (1LL << 30))
+    return h->fail(CPM_ERR_INVALID, "cpm_seed_voronoi_r: too many buckets");
   // Counting sort of the points by bucket (host; O(npoints)).
   std::vector<int> bucket_of(npoints), start(G + 1, 0);
   for (int k = 0; k < npoints; ++k) {
@@ -1461,6 +1463,52 @@ int cpm_seed_voronoi_r(cpm_handle* h, int r, int npoints, const double* points,
     ++start[b + 1];
   }
   for (long long b = 0; b < G; ++b) start[b + 1] += start[b];
+  // Work bound.  A site's search ends within about (d + 1) sqrt(ndim)
+  // max(w) / min(w) + 1 rings, d the Chebyshev distance (in buckets, wrapped)
+  // from its bucket to the nearest occupied one; d comes from a breadth-first
+  // search over the bucket grid.  Point sets clustered so much that the
+  // search would run for seconds are refused instead of launched.
+  {
+    std::vector<int> dist(G, -1), frontier, next;
+    for (long long b = 0; b < G; ++b)
+      if (start[b + 1] > start[b]) {
+        dist[b] = 0;
+        frontier.push_back((int)b);
+      }
+    for (int d = 1; !frontier.empty(); ++d) {
+      next.clear();
+      for (int b : frontier) {
+        const int bx = b % vg.g[0], by = (b / vg.g[0]) % vg.g[1], bz = b / (vg.g[0] * vg.g[1]);
+        for (int dz = (nd == 3 ? -1 : 0); dz <= (nd == 3 ? 1 : 0); ++dz)
+          for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+              const int x2 = (bx + dx + vg.g[0]) % vg.g[0], y2 = (by + dy + vg.g[1]) % vg.g[1],
+                        z2 = (bz + dz + vg.g[2]) % vg.g[2];
+              const int b2 = (z2 * vg.g[1] + y2) * vg.g[0] + x2;
+              if (dist[b2] < 0) {
+                dist[b2] = d;
+                next.push_back(b2);
+              }
+            }
+      }
+      frontier.swap(next);
+    }
+    double wmax = 0.0;
+    for (int a = 0; a < nd; ++a) wmax = std::max(wmax, vg.w[a]);
+    const double per_bucket_sites = sites / (double)G;
+    const double per_bucket_points = (double)npoints / (double)G;
+    double work = 0.0;  // estimated distance evaluations
+    for (long long b = 0; b < G; ++b) {
+      const double rings =
+          std::min((double)vg.rmax, (dist[b] + 1) * std::sqrt((double)nd) * wmax / wmin + 1.0);
+      work += per_bucket_sites * std::pow(2.0 * rings + 1.0, nd) * std::max(1.0, per_bucket_points);
+    }
+    if (work > 5e11)
+      return h->fail(CPM_ERR_INVALID,
+                     "cpm_seed_voronoi_r: the points are too unevenly spread for the bucketed "
+                     "search (about %.3g distance evaluations); spread them more evenly or "
+                     "label the lattice on the host", work);
+  }
   std::vector<double> pts((size_t)npoints * 3, 0.0);
   std::vector<int> idx(npoints), fill(start.begin(), start.end() - 1);
   for (int k = 0; k < npoints; ++k) {

@@ -412,7 +412,9 @@ int cpm_observe_boundaries(cpm_handle* h, int ntypes, uint64_t* out_host);
  * (x first), values[k] = id | type << 24 given to the sites whose nearest
  * point (min-image Euclidean distance in double) is k, ties to the lowest
  * k, so the result is the brute-force answer bit for bit.  Points are
- * bucketed on the host and searched ring by ring on the device.  The tables
+ * bucketed on the host and searched ring by ring on the device; point sets
+ * clustered so much that the search would run for seconds are refused
+ * (CPM_ERR_INVALID) before anything is launched.  The tables
  * are stale afterwards: cpm_recount (or cpm_pull, edit, cpm_push) must
  * come before the next run. */
 int cpm_seed_voronoi_r(cpm_handle* h, int replica, int npoints, const double* points,

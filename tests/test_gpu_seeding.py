@@ -151,3 +151,20 @@ def test_voronoi_seeds_one_replica_of_a_batch(engine_lib):
     assert not b.lattice(0).any() and not b.lattice(2).any()
     area, _, _ = b.tables(1)
     assert area[1:].sum() == shapes[1][0] * shapes[1][1]
+
+
+def test_voronoi_refuses_clustered_points_before_launch(engine_lib):
+    """2M points crowded into one corner of a 4096^2 lattice would make the
+    ring search scan ~10^13 buckets; the host bound refuses the call before
+    any kernel runs, and the engine stays usable."""
+    import gpucpm
+    e = _engine_for((4096, 4096), 2_000_000)
+    rng = np.random.default_rng(1)
+    pts = rng.random((2_000_000, 2)) * 2.0
+    vals = (np.arange(2_000_000, dtype=np.uint32) + 1) | (1 << 24)
+    with pytest.raises(gpucpm.CpmError, match="unevenly"):
+        e.seed_voronoi(0, pts, vals)
+    ok = rng.random((1000, 2)) * 4096.0
+    e.seed_voronoi(0, ok, (np.arange(1000, dtype=np.uint32) + 1) | (1 << 24))
+    e.recount()
+    e.synchronize()
