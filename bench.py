@@ -66,7 +66,7 @@ def parse_args():
     p.add_argument("--variant", type=int, default=None,
                    help="tile variant instead of the autotuner's choice (profiling runs: "
                         "timing under a profiler can change the tuner's pick)")
-    p.add_argument("--dispatch", choices=["grid", "replica"], default=None,
+    p.add_argument("--dispatch", choices=["grid", "replica", "hybrid"], default=None,
                    help="batches: dispatch instead of the autotuner's choice")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-reference-gpu", action="store_true",
@@ -507,8 +507,9 @@ def run_ensemble(args, world, rank, local):
     if args.variant is not None:
         b.set_variant(args.variant)
     if args.dispatch is not None:
-        b.set_dispatch(gpucpm.DISPATCH_REPLICA if args.dispatch == "replica"
-                       else gpucpm.DISPATCH_GRID)
+        b.set_dispatch({"replica": gpucpm.DISPATCH_REPLICA,
+                        "hybrid": gpucpm.DISPATCH_HYBRID}.get(args.dispatch,
+                                                              gpucpm.DISPATCH_GRID))
     for _ in range(args.warmup):
         b.run_graph(mcs)
     b.synchronize()

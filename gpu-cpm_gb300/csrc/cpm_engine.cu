@@ -88,6 +88,7 @@ struct cpm_handle {
   DevReplica* d_reps = nullptr;
   DevParams* d_params = nullptr;
   int* d_task_prefix = nullptr;
+  int* d_hyb_prefix = nullptr;  // [variant][27][nrep + 1] (hybrid grid part)
   int* d_rep_order = nullptr;  // replicas by decreasing site count
 
   cudaStream_t stream = nullptr;      // stream work is enqueued on
@@ -102,6 +103,11 @@ struct cpm_handle {
     long long list_cap_local = 0;
     std::vector<int> task_prefix;  // [27][nrep + 1] warp tiles per slot
     std::vector<int> active_slots;
+    // hybrid dispatch: the first hyb_ng replicas of rep_order run in grid
+    // dispatch (hyb_prefix: [27][hyb_ng + 1], in rep_order), the rest in
+    // replica dispatch, a whole number of rounds
+    int hyb_ng = 0;
+    std::vector<int> hyb_prefix;
   } cfg[kTileVariants];
   int variant = 0;
   int dispatch = CPM_DISPATCH_GRID;  // CPM_DISPATCH_*
@@ -113,6 +119,7 @@ struct cpm_handle {
   bool d_tick_stale = true;
   cudaGraphExec_t graph_exec = nullptr;
   int graph_mcs = 0, graph_variant = -1, graph_dispatch = -1;
+  int graph_launches = 1;  // sweep kernels per replay (2 for hybrid)
   cudaStream_t graph_stream = nullptr;
 
   uint64_t seed = 0;
@@ -183,6 +190,7 @@ void free_all(cpm_handle* h) {
   cudaFree(h->d_reps);
   cudaFree(h->d_params);
   cudaFree(h->d_task_prefix);
+  cudaFree(h->d_hyb_prefix);
   cudaFree(h->d_rep_order);
   cudaFree(h->d_tick);
   if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
@@ -286,6 +294,7 @@ int build_engine(int n, int ndim, const int* nx, const int* ny, const int* nz,
   al((void**)&h->d_params, sizeof(DevParams));
   h->params_cap = 1;
   al((void**)&h->d_task_prefix, sizeof(int) * kTileVariants * 27 * (n + 1));
+  al((void**)&h->d_hyb_prefix, sizeof(int) * kTileVariants * 27 * (n + 1));
   al((void**)&h->d_rep_order, sizeof(int) * n);
   al((void**)&h->d_tick, sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMallocHost((void**)&h->h_lat, sizeof(uint32_t) * (sites ? sites : 1));
@@ -369,6 +378,20 @@ int build_engine(int n, int ndim, const int* nx, const int* ny, const int* nz,
     c.grid_local = std::min(per_sm * sms, n);
     c.list_cap_local = n > 1 ? 2LL * nt * max_rep_tiles : 0;  // batches only
     dlist_entries = std::max(dlist_entries, c.list_cap_local * 2 * c.grid_local);
+    // Hybrid split: replica dispatch gets whole rounds of the smallest
+    // replicas, grid dispatch the rest.
+    c.hyb_ng = n - (n / c.grid_local) * c.grid_local;
+    const int ng = c.hyb_ng;
+    c.hyb_prefix.assign(27 * (ng + 1), 0);
+    for (int slot = 0; slot < 27; ++slot) {
+      int acc = 0;
+      for (int i = 0; i < ng; ++i) {
+        c.hyb_prefix[slot * (ng + 1) + i] = acc;
+        const int r = order[i];
+        acc += c.task_prefix[slot * (n + 1) + r + 1] - c.task_prefix[slot * (n + 1) + r];
+      }
+      c.hyb_prefix[slot * (ng + 1) + ng] = acc;
+    }
   }
   // act runs defer one copy per attempt at most: half a dirty list's entries
   h->pend_entries = dlist_entries / 4 + 1;
@@ -381,21 +404,28 @@ int build_engine(int n, int ndim, const int* nx, const int* ny, const int* nz,
   }
 
   // Replica dispatch by default when there are replicas for every block and
-  // no replica is much larger than a block's fair share of the sites (the
-  // autotuner can change the choice).
+  // no replica is much larger than a block's fair share of the sites, hybrid
+  // when those replicas do not fill whole rounds (the autotuner can change
+  // the choice).
   h->dispatch = (n >= h->cfg[0].grid_local && n >= sms &&
                  max_sites * (long long)h->cfg[0].grid_local <= 2 * sites)
-                    ? CPM_DISPATCH_REPLICA
+                    ? (h->cfg[0].hyb_ng > 0 ? CPM_DISPATCH_HYBRID : CPM_DISPATCH_REPLICA)
                     : CPM_DISPATCH_GRID;
   e = cudaMemcpyAsync(h->d_reps, h->reps.data(), sizeof(DevReplica) * n,
                       cudaMemcpyHostToDevice, h->stream);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(h->d_rep_order, order.data(), sizeof(int) * n,
                         cudaMemcpyHostToDevice, h->stream);
-  for (int v = 0; v < kTileVariants && e == cudaSuccess; ++v)
+  for (int v = 0; v < kTileVariants && e == cudaSuccess; ++v) {
     e = cudaMemcpyAsync(h->d_task_prefix + (size_t)v * 27 * (n + 1),
                         h->cfg[v].task_prefix.data(), sizeof(int) * 27 * (n + 1),
                         cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(h->d_hyb_prefix + (size_t)v * 27 * (n + 1),
+                          h->cfg[v].hyb_prefix.data(),
+                          sizeof(int) * h->cfg[v].hyb_prefix.size(), cudaMemcpyHostToDevice,
+                          h->stream);
+  }
   if (e == cudaSuccess) e = cudaMemsetAsync(h->d_ctl, 0, sizeof(uint32_t) * kCtlWords, h->stream);
   if (e == cudaSuccess)
     e = cudaMemsetAsync(h->d_counters, 0, sizeof(unsigned long long) * 2 * n, h->stream);
@@ -676,6 +706,9 @@ SweepArgs sweep_args(const cpm_handle* h, int v, int d) {
   a.pend_cap = (d == CPM_DISPATCH_REPLICA ? c.list_cap_local : c.list_cap) / 2;
   a.list_cap = a.block_local ? c.list_cap_local : c.list_cap;
   a.rep_order = h->d_rep_order;
+  a.queue_len = h->nrep;
+  a.rep_map = nullptr;
+  a.tick_advance = 1;
   a.ctl = h->d_ctl;
   a.counters = h->d_counters;
   a.reps = h->d_reps;
@@ -692,6 +725,47 @@ SweepArgs sweep_args(const cpm_handle* h, int v, int d) {
 int grid_of(const cpm_handle* h, int v, int d) {
   if (h->act_active || h->persist_active) v = 0;
   return d == CPM_DISPATCH_REPLICA ? h->cfg[v].grid_local : h->cfg[v].grid;
+}
+
+// The launches of one sweep run (`a` from sweep_args with dispatch `d`,
+// times filled in): one launch for GRID and REPLICA, two for HYBRID (grid
+// dispatch over the first hyb_ng replicas of rep_order, then replica
+// dispatch over the rest).  Each launch starts with its barrier words
+// cleared.  Returns the number of launches through *nlaunch.
+cudaError_t enqueue_sweep(const cpm_handle* h, int v, int d, const SweepArgs& a, bool perim,
+                          bool scores, int* nlaunch) {
+  if (h->act_active || h->persist_active) v = 0;
+  const cpm_handle::Config& c = h->cfg[v];
+  *nlaunch = 0;
+  auto one = [&](const SweepArgs& x, int grid) {
+    cudaError_t e = cudaMemsetAsync(h->d_ctl, 0, sizeof(uint32_t) * kCtlErr, h->stream);
+    if (e == cudaSuccess) e = launch_sweep(h->ndim, perim, v, x, grid, h->stream, scores);
+    if (e == cudaSuccess) ++*nlaunch;
+    return e;
+  };
+  if (d != CPM_DISPATCH_HYBRID) return one(a, grid_of(h, v, d));
+  const int ng = c.hyb_ng;
+  if (ng > 0) {  // grid dispatch over the largest replicas
+    SweepArgs g = a;
+    g.block_local = 0;
+    g.list_cap = c.list_cap;
+    g.pend_cap = c.list_cap / 2;
+    g.nrep = ng;
+    g.task_prefix = h->d_hyb_prefix + (size_t)v * 27 * (h->nrep + 1);
+    g.rep_map = h->d_rep_order;
+    g.tick_advance = ng < h->nrep ? 0 : 1;
+    if (cudaError_t e = one(g, c.grid)) return e;
+  }
+  if (ng < h->nrep) {  // replica dispatch over the rest, whole rounds
+    SweepArgs q = a;
+    q.block_local = 1;
+    q.list_cap = c.list_cap_local;
+    q.pend_cap = c.list_cap_local / 2;
+    q.rep_order = h->d_rep_order + ng;
+    q.queue_len = h->nrep - ng;
+    if (cudaError_t e = one(q, c.grid_local)) return e;
+  }
+  return cudaSuccess;
 }
 
 void count_attempts(cpm_handle* h, int mcs) {
@@ -1188,10 +1262,9 @@ int cpm_run(cpm_handle* h, int mcs) {
     a.mcs = chunk;
     // Barrier counter and release flag start at zero in every launch; the
     // sticky error word is left alone until cpm_synchronize reads it.
-    CPM_CUDA(h, cudaMemsetAsync(h->d_ctl, 0, sizeof(uint32_t) * kCtlErr, h->stream));
-    CPM_CUDA(h, launch_sweep(h->ndim, any_perim, h->variant, a,
-                             grid_of(h, h->variant, h->dispatch), h->stream));
-    h->launches += 1;
+    int nl = 0;
+    CPM_CUDA(h, enqueue_sweep(h, h->variant, h->dispatch, a, any_perim, false, &nl));
+    h->launches += nl;
     h->tick += (uint64_t)chunk;
     left -= chunk;
   }
@@ -1221,11 +1294,8 @@ int cpm_run_graph(cpm_handle* h, int mcs) {
     a.mcs = mcs;
     cudaGraph_t g = nullptr;
     CPM_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    cudaError_t e1 = cudaMemsetAsync(h->d_ctl, 0, sizeof(uint32_t) * kCtlErr, h->stream);
-    cudaError_t e2 = e1 == cudaSuccess
-                         ? launch_sweep(h->ndim, any_perimeter(h), h->variant, a,
-                                        grid_of(h, h->variant, h->dispatch), h->stream)
-                         : e1;
+    int nl = 0;
+    cudaError_t e2 = enqueue_sweep(h, h->variant, h->dispatch, a, any_perimeter(h), false, &nl);
     cudaError_t e3 = cudaStreamEndCapture(h->stream, &g);
     if (e2 != cudaSuccess) return h->cuda_fail(e2, "capture of the sweep launch");
     if (e3 != cudaSuccess) return h->cuda_fail(e3, "cudaStreamEndCapture");
@@ -1233,6 +1303,7 @@ int cpm_run_graph(cpm_handle* h, int mcs) {
     cudaGraphDestroy(g);
     if (e4 != cudaSuccess) return h->cuda_fail(e4, "cudaGraphInstantiate");
     h->graph_mcs = mcs;
+    h->graph_launches = nl;
     h->graph_variant = h->variant;
     h->graph_dispatch = h->dispatch;
     h->graph_stream = h->stream;
@@ -1244,7 +1315,7 @@ int cpm_run_graph(cpm_handle* h, int mcs) {
     h->d_tick_stale = false;
   }
   CPM_CUDA(h, cudaGraphLaunch(h->graph_exec, h->stream));
-  h->launches += 1;
+  h->launches += h->graph_launches;
   h->tick += (uint64_t)mcs;
   count_attempts(h, mcs);
   return persist_after_run(h);  // a launch of its own: its slot changes per run
@@ -1297,23 +1368,27 @@ int cpm_autotune(cpm_handle* h, int probe_mcs, int* chosen, float* ms_per_mcs) {
   // Every (tile variant, dispatch) pair, replica dispatch only for batches,
   // timed in three rounds (the fastest run counts): a variant's first launch
   // also loads its module, and clocks may still be rising.
-  const int ndispatch = h->nrep > 1 ? 2 : 1;
-  const int npairs = kTileVariants * ndispatch;
+  // (hybrid only where it splits the batch into two non-empty parts)
+  std::vector<std::pair<int, int>> pairs;
+  for (int d = 0; d < (h->nrep > 1 ? 3 : 1); ++d)
+    for (int v = 0; v < kTileVariants; ++v)
+      if (d != CPM_DISPATCH_HYBRID || (h->cfg[v].hyb_ng > 0 && h->cfg[v].hyb_ng < h->nrep))
+        pairs.emplace_back(v, d);
+  const int npairs = (int)pairs.size();
   for (int i = 0; i < 3 * npairs && e == cudaSuccess; ++i) {
-    const int v = (i % npairs) % kTileVariants, d = (i % npairs) / kTileVariants;
+    const int v = pairs[i % npairs].first, d = pairs[i % npairs].second;
     SweepArgs a = sweep_args(h, v, d);
     a.tick0 = tick;
     a.mcs = probe_mcs;
     e = copy(false);
-    if (e == cudaSuccess) e = cudaMemsetAsync(h->d_ctl, 0, sizeof(uint32_t) * kCtlErr, h->stream);
     if (e == cudaSuccess) e = cudaEventRecord(ev[0], h->stream);
-    if (e == cudaSuccess)
-      e = launch_sweep(h->ndim, any_perim, v, a, grid_of(h, v, d), h->stream);
+    int nl = 0;
+    if (e == cudaSuccess) e = enqueue_sweep(h, v, d, a, any_perim, false, &nl);
     if (e == cudaSuccess) e = cudaEventRecord(ev[1], h->stream);
     if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
     float ms = 0.0f;
     if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ev[0], ev[1]);
-    h->launches += 1;
+    h->launches += nl;
     if (e == cudaSuccess && (best < 0.0f || ms < best)) {
       best = ms;
       best_v = v;
@@ -1372,10 +1447,9 @@ int cpm_run_scores(cpm_handle* h, int mcs, float* d_scores, uint64_t score_base,
     const int chunk = std::min(left, kMaxMcsPerLaunch);
     a.tick0 = h->tick;
     a.mcs = chunk;
-    CPM_CUDA(h, cudaMemsetAsync(h->d_ctl, 0, sizeof(uint32_t) * kCtlErr, h->stream));
-    CPM_CUDA(h, launch_sweep(h->ndim, any_perimeter(h), h->variant, a,
-                             grid_of(h, h->variant, h->dispatch), h->stream, true));
-    h->launches += 1;
+    int nl = 0;
+    CPM_CUDA(h, enqueue_sweep(h, h->variant, h->dispatch, a, any_perimeter(h), true, &nl));
+    h->launches += nl;
     h->tick += (uint64_t)chunk;
     left -= chunk;
   }
@@ -1616,10 +1690,13 @@ int cpm_set_variant(cpm_handle* h, int variant) {
 
 int cpm_set_dispatch(cpm_handle* h, int dispatch) {
   if (!h) return CPM_ERR_INVALID;
-  if (dispatch != CPM_DISPATCH_GRID && dispatch != CPM_DISPATCH_REPLICA)
-    return h->fail(CPM_ERR_INVALID, "dispatch %d is neither grid (0) nor replica (1)", dispatch);
-  if (dispatch == CPM_DISPATCH_REPLICA && h->nrep < 2)
-    return h->fail(CPM_ERR_UNSUPPORTED, "replica dispatch needs a batch of two or more replicas");
+  if (dispatch != CPM_DISPATCH_GRID && dispatch != CPM_DISPATCH_REPLICA &&
+      dispatch != CPM_DISPATCH_HYBRID)
+    return h->fail(CPM_ERR_INVALID, "dispatch %d is not grid (0), replica (1) or hybrid (2)",
+                   dispatch);
+  if (dispatch != CPM_DISPATCH_GRID && h->nrep < 2)
+    return h->fail(CPM_ERR_UNSUPPORTED, "replica and hybrid dispatch need a batch of two or "
+                                        "more replicas");
   h->dispatch = dispatch;
   return CPM_OK;
 }

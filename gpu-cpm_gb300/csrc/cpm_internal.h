@@ -194,7 +194,13 @@ struct SweepArgs {
   // of the grid, one grid barrier per phase; 1 = each block claims whole
   // replicas in rep_order and runs all their phases with block barriers.
   int block_local;
-  const int* rep_order;  // [nrep] replicas by decreasing site count
+  const int* rep_order;  // replicas by decreasing site count (replica dispatch:
+                         // the queue, queue_len entries)
+  int queue_len;         // replica dispatch: replicas to claim
+  // Grid dispatch over a subset of the replicas (hybrid runs): task_prefix
+  // and nrep describe the subset, and rep_map[i] is subset member i's
+  // replica (null: the subset is every replica, in order).
+  const int* rep_map;
   // chemotaxis field, float: replica r's component k of site i at
   // field[ndim * lat_off + k * sites_r + i] (null when no field exists)
   const float* field;
@@ -214,6 +220,7 @@ struct SweepArgs {
   // set (graph replays); in the latter case block 0 advances *tick_ptr by
   // mcs when the launch ends.
   unsigned long long* tick_ptr;
+  int tick_advance;  // 0: leave *tick_ptr to a later launch of the same run
   unsigned long long tick0;
   // Score output (score launches only): scores[(r * score_len + tick -
   // score_base) * kScoreMax + k] receives replica r's summed score of

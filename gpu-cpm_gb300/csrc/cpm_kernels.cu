@@ -851,7 +851,7 @@ __global__ void __launch_bounds__(32 * max_sweep_warps<NDIM>(), 1)
         // phase, so the band's lines and most of its halo stay with this
         // SM's side of L2.  Batches: tiles dealt round-robin over all warps
         // (the light edge tiles of ragged replicas would unbalance bands).
-        if (a.nrep == 1) {
+        if (a.nrep == 1 && a.rep_map == nullptr) {
           const int per_b = ntiles / (int)gridDim.x, extra = ntiles % (int)gridDim.x;
           const int tb0 = (int)blockIdx.x * per_b + min((int)blockIdx.x, extra);
           const int tb1 = tb0 + per_b + ((int)blockIdx.x < extra ? 1 : 0);
@@ -865,8 +865,9 @@ __global__ void __launch_bounds__(32 * max_sweep_warps<NDIM>(), 1)
         } else {
           for (int task = (int)blockIdx.x * wpb + warp; task < ntiles;
                task += (int)gridDim.x * wpb) {
-            const int r = find_task_replica(pre, a.nrep, task);
-            run_tile(pt, r, task - __ldg(pre + r), cx, cy, cz, tick, phase);
+            const int i = find_task_replica(pre, a.nrep, task);
+            const int r = a.rep_map ? __ldg(a.rep_map + i) : i;
+            run_tile(pt, r, task - __ldg(pre + i), cx, cy, cz, tick, phase);
           }
         }
         // The replayed list is consumed; every attempt of the slot is done
@@ -896,7 +897,7 @@ __global__ void __launch_bounds__(32 * max_sweep_warps<NDIM>(), 1)
       if (tid == 0) s_claim = (int)atomicAdd(&a.ctl[kCtlQueue], 1u);
       __syncthreads();
       const int qi = s_claim;
-      if (qi >= a.nrep) break;  // block-uniform
+      if (qi >= a.queue_len) break;  // block-uniform
       const int r = __ldg(a.rep_order + qi);
       int step = 0;
       for (int m = 0; m < a.mcs; ++m) {
@@ -938,7 +939,7 @@ __global__ void __launch_bounds__(32 * max_sweep_warps<NDIM>(), 1)
     if (n_acc) atomicAdd(&a.counters[2 * cnt_rep + 1], n_acc);
   }
   if (SCORE) flush_scores(a, sc, sc_rep, sc_tick);
-  if (a.tick_ptr && blockIdx.x == 0 && tid == 0 && a.mcs > 0)
+  if (a.tick_ptr && a.tick_advance && blockIdx.x == 0 && tid == 0 && a.mcs > 0)
     *a.tick_ptr = s_tick0 + (unsigned long long)a.mcs;
 }
 

@@ -57,6 +57,7 @@ CPM_FLAG_FIELD = 1
 CPM_FLAG_ACT = 2
 DISPATCH_GRID = 0
 DISPATCH_REPLICA = 1
+DISPATCH_HYBRID = 2
 
 
 class CpmError(RuntimeError):
@@ -494,8 +495,10 @@ class _Engine:
         self._call("cpm_set_variant", int(variant))
 
     def set_dispatch(self, dispatch):
-        """DISPATCH_GRID (all warps on every slot of all replicas) or
-        DISPATCH_REPLICA (a block runs whole replicas); same results."""
+        """DISPATCH_GRID (all warps on every slot of all replicas),
+        DISPATCH_REPLICA (a block runs whole replicas) or DISPATCH_HYBRID
+        (grid over the largest replicas, then replica dispatch over whole
+        rounds of the rest); same results."""
         self._call("cpm_set_dispatch", int(dispatch))
 
     def run_scores(self, mcs, scores_ptr, score_base, score_len, spec):
@@ -539,7 +542,8 @@ class _Engine:
         self._call("cpm_sweep_config", *[ctypes.byref(v) for v in vals])
         v, tx, ty, tz, w, g, d = (x.value for x in vals)
         return {"variant": v, "tile": (tx, ty, tz), "warps_per_block": w, "grid": g,
-                "dispatch": "replica" if d == DISPATCH_REPLICA else "grid"}
+                "dispatch": {DISPATCH_REPLICA: "replica",
+                             DISPATCH_HYBRID: "hybrid"}.get(d, "grid")}
 
 
 class Cpm(_Engine):

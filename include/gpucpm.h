@@ -287,11 +287,19 @@ int cpm_run_graph(cpm_handle* h, int mcs);
  *                         and runs all their phases with block barriers, so
  *                         a replica's lattice and tables stay near one SM
  *                         (many small replicas).
+ *   CPM_DISPATCH_HYBRID   two launches per run: GRID over the largest
+ *                         replicas, then REPLICA over the others, as many
+ *                         as make whole rounds of one replica per block
+ *                         (512 equal replicas on 152 SMs: GRID over 56,
+ *                         REPLICA over 456, instead of a last REPLICA round
+ *                         that leaves 96 blocks idle).
  * Results do not depend on the dispatch.  A batch starts with REPLICA when
  * it has a replica for every block and none is much larger than a block's
- * share of the sites, else GRID. */
+ * share of the sites (HYBRID when they do not fill whole rounds), else
+ * GRID. */
 #define CPM_DISPATCH_GRID 0
 #define CPM_DISPATCH_REPLICA 1
+#define CPM_DISPATCH_HYBRID 2
 
 /* Project autotuner: times `probe_mcs` MCS of every compiled tile variant
  * (warp tile shape and warps per block), under both dispatches for a batch,

@@ -199,3 +199,52 @@ def test_replica_dispatch_scores_and_autotune(engine_lib):
         sim = oracle.OracleSim(w.lattice, w.ncells, **w.oracle_kwargs(), seed=4,
                                stream=r).run(5)
         np.testing.assert_array_equal(fin[r][0].view(np.uint32), sim.lattice)
+
+
+@pytest.mark.parametrize("dims", [2, 3])
+def test_hybrid_dispatch_matches_oracle(engine_lib, dims):
+    """More replicas than blocks: hybrid dispatch runs the largest ones in
+    grid dispatch and whole rounds of the rest in replica dispatch (two
+    launches per run, the device tick advanced once).  Lattices, tables and
+    counters equal the oracle's for every replica, for plain and graph runs;
+    score launches equal grid dispatch's."""
+    import torch
+
+    import gpucpm
+    n = 160 if dims == 2 else 156
+    g = np.random.default_rng(5)
+    shapes = [tuple(int(v) for v in g.integers(10, 26, dims)) for _ in range(n)]
+    ws = [W.random_small(s, 6, seed=400 + i, temperature=7.0) for i, s in enumerate(shapes)]
+    b = _batch(ws, seed=21, stream0=3)
+    b.set_dispatch(gpucpm.DISPATCH_HYBRID)
+    assert b.sweep_config()["dispatch"] == "hybrid"
+    l0 = b.kernel_launches()
+    b.run_mcs(3)
+    b.run_graph(2)
+    b.run_graph(2)
+    assert b.tick == 7
+    st = _batch_state(b, n)
+    assert b.kernel_launches() - l0 >= 6  # two sweep launches per run
+    for r, w in enumerate(ws):
+        sim = oracle.OracleSim(w.lattice, w.ncells, **w.oracle_kwargs(), seed=21,
+                               stream=3 + r).run(7)
+        lat, a, p, c, cnt = st[r]
+        np.testing.assert_array_equal(lat.view(np.uint32), sim.lattice)
+        np.testing.assert_array_equal(a, sim.area)
+        np.testing.assert_array_equal(c, sim.csum)
+        assert cnt["accepted"] == int(sim.counters[2])
+    if dims == 2:
+        spec = gpucpm.ScoreSpec.make(((1, 1), (1, 2)))
+        res = {}
+        for d in (gpucpm.DISPATCH_GRID, gpucpm.DISPATCH_HYBRID):
+            bb = _batch(ws, seed=21, stream0=3)
+            bb.set_dispatch(d)
+            sc = torch.zeros((n, 4, gpucpm.SCORE_MAX), device="cuda")
+            torch.cuda.synchronize()
+            bb.run_scores(4, sc.data_ptr(), 0, 4, spec)
+            res[d] = (_batch_state(bb, n), sc.cpu().numpy())
+        (sg, scg), (sh, sch) = res[gpucpm.DISPATCH_GRID], res[gpucpm.DISPATCH_HYBRID]
+        for r in range(n):
+            np.testing.assert_array_equal(sg[r][0], sh[r][0])
+        scale = np.abs(scg).max(axis=(0, 1)) + 1e-6
+        assert (np.abs(scg - sch) / scale).max() < 1e-4
