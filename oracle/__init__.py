@@ -2,9 +2,10 @@
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
 CPU-baseline leg of bench.py, never by the product.  See cpm_oracle.cpp for
-the algorithm, its reference citations and its parity status (bit-level
-parity with the reference is unpinned by golden vectors; the reference has
-none and is nondeterministic).
+the algorithm, its reference citations and its parity status: the reference
+ships no golden vectors and its parallel runs are nondeterministic, so the
+pin is the reference's own deterministic one-thread runs and table recounts,
+kept in tests/golden/.
 """
 import ctypes
 

@@ -4,12 +4,16 @@
 // it is loaded by tests/, by __graft_entry__.smoke() and by bench.py's CPU
 // baseline, as the checker the CUDA engine is compared against bit for bit.
 //
-// Parity status: bit-level parity with the reference is unpinned by golden
-// vectors — the reference (shabaz/gpu-cpm) ships no tests or fixtures and is
-// nondeterministic (std::random_device seed per run, src/cpm.cu:347-350; racy
-// area reads, src/kernels2d.cu:297-298).  This file restates the reference's
-// per-attempt algorithm on a deterministic schedule; the restatement is
-// checked against the reference's own CUDA build statistically on the GPU.
+// Parity status: the reference (shabaz/gpu-cpm) ships no tests or fixtures,
+// and its production runs are nondeterministic (std::random_device seed per
+// run, src/cpm.cu:347-350; racy area reads, src/kernels2d.cu:297-298).  Its
+// one-thread runs are deterministic: tests/golden/ holds five of them and
+// three table recounts, made by the reference's own CUDA build, and the CPU
+// tests check this file's table recount against them and, through
+// tests/refmodel.py, its dH, test and bookkeeping.  This file restates the
+// reference's per-attempt algorithm on a deterministic schedule; the
+// restatement is checked against the reference's parallel runs
+// statistically on the GPU.
 //
 // What follows the reference, function by function:
 //   * site pick / neighbour pick:  src/kernels2d.cu:199-243 (target and a
