@@ -551,8 +551,9 @@ class Cpm(_Engine):
 
     Cpm(dimension, dimensionality, number_of_cells, temperature, has_field,
         history=1, has_act=1) — the argument order of PyCpm_init
-    (src/python_wrapper.cpp:27-41).  has_field / has_act select lattices of
-    terms this engine does not model; their getters return zeros.
+    (src/python_wrapper.cpp:27-41).  has_field allocates the chemotaxis
+    field and has_act the act stamps up front (both also appear on first
+    use); history sets the ring of the 3D persistence update.
     """
 
     def __init__(self, dimension, dimensionality, number_of_cells, temperature,
