@@ -149,3 +149,110 @@ def heterotypic_fraction(lat):
         total += int(both.sum())
         hetero += int((both & ((lat >> 24) != (nb >> 24))).sum())
     return hetero / max(total, 1)
+
+
+def reference_dh_nb(t, s, nb_vals, area, perim, J, lam_a, tgt_a, lam_p, tgt_p,
+                    perimeter_on=True, stick=None):
+    """dH of copying value s into a target holding t, from the values of the
+    target's neighbours (8 in 2D, 26 in 3D), as src/kernels3d.cu:355-541
+    (and src/kernels2d.cu:346-519) sum it: integer adhesion (stickiness added
+    to the old configuration's), double lambda terms, rounded to float once
+    at the end (every term here is an integer or half-integer, exact in
+    float either way).  Returns (dH, source perimeter change, target
+    perimeter change)."""
+    ts, tt = s >> 24, t >> 24
+    e_old = e_new = 0
+    ops = nps = opt = npt = 0
+    for v in nb_vals:
+        tv = v >> 24
+        if t != v:
+            e_old += J[tt][tv] + (int(stick[tt][tv]) if stick is not None else 0)
+        if s != v:
+            e_new += J[ts][tv]
+        ops += v == s
+        nps += v != s
+        opt += v != t
+        npt += v == t
+    e = float(e_new - e_old)
+    if perimeter_on:
+        if s:
+            P = int(perim[s & 0xFFFFFF])
+            Pn = P - ops + nps
+            e += lam_p[ts] * ((Pn - tgt_p[ts]) ** 2 - (P - tgt_p[ts]) ** 2)
+        if t:
+            P = int(perim[t & 0xFFFFFF])
+            Pn = P - opt + npt
+            e += lam_p[tt] * ((Pn - tgt_p[tt]) ** 2 - (P - tgt_p[tt]) ** 2)
+    if s:
+        e += lam_a[ts] * (1 + 2 * int(area[s & 0xFFFFFF]) - 2 * tgt_a[ts])
+    if t:
+        e += lam_a[tt] * (1 - 2 * int(area[t & 0xFFFFFF]) + 2 * tgt_a[tt])
+    return e, (nps - ops), (npt - opt)
+
+
+def sequential_run_3d(lat, area, perim, J, lam_a, tgt_a, lam_p, tgt_p, T, seed, mcs,
+                      perimeter_on=True, stick=None, fixed=None):
+    """The reference's one-thread 3D run (src/kernels3d.cu:51-594 with one
+    thread, positions_per_thread = positions_per_checkerboard = D,
+    non-shared branch), in place; returns the accept count.  lat is
+    [z, y, x] with a power-of-two side D.
+      seed mixing       :85 (calculateIndex(0, 0, 0) + seed)
+      source site       :159-164, 196-199 (three draws, a, b, c = r % D)
+      target neighbour  :202-212 (dx = r % 3 - 1 per axis, wrap with
+                        & (D - 1), src/random.cu:18-26), redrawn while
+                        nx == x && ny == y && nz == y: the reference compares
+                        nz with y (:208), so a zero displacement with
+                        z != y is kept (and is a no-op) while some true
+                        neighbours are redrawn
+      fixed types       :251-261
+      dH                :355-541 via reference_dh_nb()
+      Metropolis test   :544-546 (r = seed / (2^31 - 1))
+      commit + tables   :549-582"""
+    D = lat.shape[0]
+    seed = next_random(0 + seed)
+    accepted = 0
+    for _ in range(mcs):
+        for _ in range(D * D * D):
+            seed = next_random(seed)
+            x = seed % D
+            seed = next_random(seed)
+            y = seed % D
+            seed = next_random(seed)
+            z = seed % D
+            while True:
+                seed = next_random(seed)
+                nx = (x + seed % 3 - 1) & (D - 1)
+                seed = next_random(seed)
+                ny = (y + seed % 3 - 1) & (D - 1)
+                seed = next_random(seed)
+                nz = (z + seed % 3 - 1) & (D - 1)
+                if not (nx == x and ny == y and nz == y):
+                    break
+            s, t = int(lat[z, y, x]), int(lat[nz, ny, nx])
+            if s == t:
+                continue
+            if fixed is not None:
+                if fixed[t >> 24]:
+                    continue
+                if fixed[s >> 24]:
+                    s = 0
+            nb = [int(lat[(nz + k) % D, (ny + j) % D, (nx + i) % D])
+                  for k in (-1, 0, 1) for j in (-1, 0, 1) for i in (-1, 0, 1)
+                  if (i, j, k) != (0, 0, 0)]
+            dH, dps, dpt = reference_dh_nb(t, s, nb, area, perim, J, lam_a, tgt_a, lam_p,
+                                           tgt_p, perimeter_on, stick)
+            e = np.float32(dH)
+            seed = next_random(seed)
+            r = np.float32(seed / M)
+            if e < 0 or (T > 0 and r < np.float32(math.exp(-float(e) / T))):
+                lat[nz, ny, nx] = s
+                accepted += 1
+                if s:
+                    area[s & 0xFFFFFF] += 1
+                    if perimeter_on:
+                        perim[s & 0xFFFFFF] += dps
+                if t:
+                    area[t & 0xFFFFFF] -= 1
+                    if perimeter_on:
+                        perim[t & 0xFFFFFF] += dpt
+    return accepted

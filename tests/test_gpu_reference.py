@@ -117,6 +117,57 @@ def test_one_thread_reference_run_equals_restatement(engine_lib, D, perimeter, s
         np.testing.assert_array_equal(rp.astype(np.int64), perim)
 
 
+def one_thread_case_3d(D, perimeter, seed, terms):
+    """Inputs of a one-thread 3D reference run (shared with the golden
+    fixture generator)."""
+    nt = 3 if terms == "fixed_sticky" else 2
+    w = W.random_small((D, D, D), D ** 3 // 40, ntypes=nt, seed=D + seed % 89,
+                       temperature=6.0, perim=perimeter)
+    J = np.rint(w.J).astype(int)
+    lam_a = [0.0] + [1.0] * nt
+    tgt_a = [0] + [40] * nt
+    lam_p = ([0.0] + [0.5] * nt) if perimeter else [0.0] * (nt + 1)
+    tgt_p = [0] + [90] * nt
+    stick = fixed = None
+    if terms == "fixed_sticky":
+        stick = np.zeros((nt + 1, nt + 1), np.float32)
+        stick[1, 2], stick[2, 1], stick[1, 0], stick[0, 2] = 3, 2, 4, 1
+        fixed = np.array([False, False, False, True])
+    wi = W.Workload("one_thread_3d", w.lattice, w.ncells, J.astype(np.float32),
+                    np.array(lam_a, np.float32), np.array(tgt_a, np.int32),
+                    np.array(lam_p, np.float32), np.array(tgt_p, np.int32), 6.0, 0,
+                    stick=stick, fixed=fixed)
+    return wi, J, lam_a, tgt_a, lam_p, tgt_p
+
+
+@pytest.mark.parametrize("D,perimeter,seed,terms", [(8, False, 999, None),
+                                                    (16, True, 555, None),
+                                                    (16, True, 8080, "fixed_sticky")])
+def test_one_thread_reference_run_3d_equals_restatement(engine_lib, D, perimeter, seed, terms):
+    """The reference's 3D sweep (src/kernels3d.cu:51-594, non-shared
+    branch, with its neighbour redraw test that compares nz with y, :208)
+    run by one thread equals tests/refmodel.py's sequential_run_3d."""
+    wi, J, lam_a, tgt_a, lam_p, tgt_p = one_thread_case_3d(D, perimeter, seed, terms)
+    ref = _ref(wi)
+    a0, p0 = ref.tables()
+    mcs = 2
+    ref.run(mcs, threads_per_block=1, positions_per_thread=D, positions_per_checkerboard=D,
+            seed=seed)
+    ref.synchronize()
+    got = ref.pull()
+    ra, rp = ref.tables()
+    lat = wi.lattice.copy()
+    area, perim = a0.astype(np.int64), p0.astype(np.int64)
+    acc = refmodel.sequential_run_3d(lat, area, perim, J, lam_a, tgt_a, lam_p, tgt_p, 6.0,
+                                     seed, mcs, perimeter_on=perimeter, stick=wi.stick,
+                                     fixed=wi.fixed)
+    assert acc > 10
+    np.testing.assert_array_equal(got, lat)
+    np.testing.assert_array_equal(ra.astype(np.int64), area)
+    if perimeter:
+        np.testing.assert_array_equal(rp.astype(np.int64), perim)
+
+
 def _observables(lat, prev):
     ids = (lat & 0xFFFFFF).astype(np.int64)
     areas = np.bincount(ids.ravel())[1:]

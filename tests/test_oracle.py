@@ -607,3 +607,75 @@ def test_oracle_boundaries_match_numpy(shape):
         a, b = (lat >> 24)[diff], (nb >> 24)[diff]
         np.add.at(want, (np.minimum(a, b), np.maximum(a, b)), 1)
     np.testing.assert_array_equal(oracle.boundaries(lat, T), want)
+
+
+@pytest.mark.parametrize("case", ["plain", "fixed_sticky"])
+def test_first_mcs_3d_matches_reference_dh_formula(case):
+    """3D: replay one MCS of the oracle's schedule (8 slots of an even box,
+    26-neighbour source pick from the same Philox draws) with the
+    reference's 3D dH (tests/refmodel.py reference_dh_nb, restating
+    src/kernels3d.cu:355-541), copies landing after their slot."""
+    import refmodel
+    n = 8
+    w = W.random_small((n, n, n), 12, ntypes=3, seed=21, temperature=6.0)
+    J = np.rint(w.J).astype(int)
+    lam_a, lam_p = [1.0] * 4, [0.5] * 4
+    tgt_a, tgt_p = [0, 40, 40, 40], [0, 90, 90, 90]
+    T = 6.0
+    stick = fixed = None
+    if case == "fixed_sticky":
+        stick = np.zeros((4, 4), int)
+        stick[1, 2], stick[2, 1], stick[1, 0], stick[2, 3] = 3, 5, 2, 4
+        fixed = [False, False, False, True]
+    sim = oracle.OracleSim(w.lattice, w.ncells, J.astype(np.float32), lam_a, tgt_a,
+                           lam_p, tgt_p, temperature=T, seed=9, stick=stick, fixed=fixed)
+    lat = w.lattice.copy()
+    area, perim = sim.area.copy(), sim.perim.copy()
+    offs = [(m % 3 - 1, (m // 3) % 3 - 1, m // 9 - 1) for m in range(27) if m != 13]
+    accepted = 0
+    for cz in (0, 1):
+        for cy in (0, 1):
+            for cx in (0, 1):
+                slot = cz * 9 + cy * 3 + cx
+                changes = []
+                for z in range(cz, n, 2):
+                    for y in range(cy, n, 2):
+                        for x in range(cx, n, 2):
+                            t = int(lat[z, y, x])
+                            nbs = [((x + i) % n, (y + j) % n, (z + k) % n) for i, j, k in offs]
+                            vals = [int(lat[c, b, a]) for a, b, c in nbs]
+                            if all(v == t for v in vals):
+                                continue
+                            r = oracle.philox4x32_10([(z * n + y) * n + x, slot, 0, 0], [9, 0])
+                            kd = (r[0] * 26) >> 32
+                            if vals[kd] == t:
+                                continue
+                            s = vals[kd]
+                            if fixed is not None:
+                                if fixed[t >> 24]:
+                                    continue
+                                if fixed[s >> 24]:
+                                    s = 0
+                                    if s == t:
+                                        continue
+                            dH, dps, dpt = refmodel.reference_dh_nb(
+                                t, s, vals, area, perim, J, lam_a, tgt_a, lam_p, tgt_p,
+                                True, stick)
+                            u = ((r[1] >> 8) | 1) * 2.0 ** -24
+                            if dH < 0 or u < math.exp(-dH / T):
+                                changes.append((x, y, z, s, t, dps, dpt))
+                for x, y, z, s, t, dps, dpt in changes:
+                    lat[z, y, x] = s
+                    accepted += 1
+                    if s:
+                        area[s & 0xFFFFFF] += 1
+                        perim[s & 0xFFFFFF] += dps
+                    if t:
+                        area[t & 0xFFFFFF] -= 1
+                        perim[t & 0xFFFFFF] += dpt
+    sim.run(1)
+    assert accepted > 5
+    assert int(sim.counters[2]) == accepted
+    np.testing.assert_array_equal(sim.lattice, lat)
+    np.testing.assert_array_equal(sim.area, area)
+    np.testing.assert_array_equal(sim.perim, perim)
