@@ -951,6 +951,7 @@ __global__ void __launch_bounds__(kInitThreads)
                const DevReplica* __restrict__ reps, int nrep, long long total,
                unsigned long long* first, int* ctype, uint32_t* ctl) {
   int* err = reinterpret_cast<int*>(&ctl[kCtlErr]);
+  const int lane = threadIdx.x & 31;
   for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
        g < total; g += (long long)gridDim.x * blockDim.x) {
     const int r = find_site_replica(reps, nrep, g);
@@ -958,16 +959,25 @@ __global__ void __launch_bounds__(kInitThreads)
     const uint32_t v = lat[g];
     const uint32_t id = v & 0xFFFFFFu;
     const int ty = (int)(v >> 24);
-    if (id > (uint32_t)__ldg(&reps[r].ncells)) {
-      atomicOr(err, kErrBadId);
-      continue;
-    }
+    const bool bad = id > (uint32_t)__ldg(&reps[r].ncells);
+    if (bad) atomicOr(err, kErrBadId);
     if (ty >= kMaxTypes) atomicOr(err, kErrBadType);
     if (id == 0 && ty != 0) atomicOr(err, kErrMediumType);
-    const long long row = __ldg(&reps[r].cell_off) + id;
-    const int old = atomicCAS(&ctype[row], -1, ty);
-    if (old != -1 && old != ty) atomicOr(err, kErrTypeConflict);
-    atomicMin(&first[row], (unsigned long long)local);
+    const long long row = bad ? -1 : __ldg(&reps[r].cell_off) + id;
+    // Lanes of one cell (neighbouring sites usually share one) check their
+    // types against the lowest such lane, which holds the lowest site index
+    // and alone updates the row: one CAS and one min per cell and warp.
+    const unsigned mask = __activemask();
+    const unsigned peers = __match_any_sync(mask, (unsigned long long)row);
+    const int leader = __ffs(peers) - 1;
+    const int lty = __shfl_sync(mask, ty, leader);
+    if (bad) continue;
+    if (ty != lty) atomicOr(err, kErrTypeConflict);
+    if (lane == leader) {
+      const int old = atomicCAS(&ctype[row], -1, ty);
+      if (old != -1 && old != ty) atomicOr(err, kErrTypeConflict);
+      atomicMin(&first[row], (unsigned long long)local);
+    }
   }
 }
 
