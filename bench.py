@@ -333,6 +333,31 @@ def traffic_per_attempt(workload):
         return None
 
 
+def warp_inst_per_attempt(workload):
+    """Warp instructions per attempt of the sweep from the committed ncu summary."""
+    f = ROOT / "profiles" / "traffic.json"
+    try:
+        return float(json.loads(f.read_text())[workload]["warp_inst_per_attempt"])
+    except Exception:
+        return None
+
+
+def issue_roofline(workload, attempts_per_s, clocks, torch, local):
+    """The bound the sweep actually meets: warp-instruction issue.  Peak =
+    4 schedulers x SMs x the SM clock sampled during the timed steps; achieved
+    = attempts/s x the warp instructions per attempt that ncu counted."""
+    ipa = warp_inst_per_attempt(workload)
+    if ipa is None or not clocks or not clocks.get("sm_mhz"):
+        return None
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    peak = 4 * sms * clocks["sm_mhz"] * 1e6
+    achieved = attempts_per_s * ipa
+    return {"bound": "issue", "achieved": achieved, "peak": peak,
+            "unit": "warp instructions/s", "frac": achieved / peak,
+            "warp_inst_per_attempt": ipa,
+            "peak_source": f"4 x {sms} SMs x {clocks['sm_mhz']:.0f} MHz (sampled)"}
+
+
 def warm_gpu(seconds=0.3):
     """Keep the GPU busy for a moment so that its clocks have left idle
     before the autotuner times anything (an idle GB300 ramps up over the
@@ -448,7 +473,10 @@ def run_ours(args, world, rank, local):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "u32+f32", "data": "synthetic (seeded Voronoi tissue)",
             "config": dict(describe(w, mcs), tile=sim.sweep_config()["tile"]),
-            "roofline": roofline, "e2e": e2e,
+            "roofline": roofline,
+            "issue_roofline": issue_roofline(args.workload, value / world, clocks, torch,
+                                             local),
+            "e2e": e2e,
             "autotune": {"variant": variant, "probe_ms_per_mcs": tuned_ms,
                          "dispatch": sim.sweep_config()["dispatch"]},
             "gpu_launches": int(launches), "clocks": clocks,
