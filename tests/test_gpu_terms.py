@@ -332,3 +332,38 @@ def test_all_terms_batch_matches_oracle(engine_lib, dims, dispatch):
         np.testing.assert_array_equal(cs, s.csum)
         if s.act is not None:
             np.testing.assert_array_equal(b.act_lattice(r).view(np.uint32), s.act)
+
+
+@pytest.mark.parametrize("dims", [2, 3])
+def test_all_terms_hybrid_dispatch_matches_oracle(engine_lib, dims):
+    """Hybrid dispatch (grid over the largest replicas, replica dispatch over
+    whole rounds of the rest) with every term on, act's deferred copies and
+    3D persistence included; more replicas than blocks."""
+    import gpucpm
+    n = 158 if dims == 2 else 154
+    g = np.random.default_rng(11)
+    shapes = [tuple(int(v) for v in g.integers(10, 18, dims)) for _ in range(n)]
+    ws = [_all_terms(W.random_small(s, 6, ntypes=3, seed=600 + i, temperature=8.0), seed=i)
+          for i, s in enumerate(shapes)]
+    b = gpucpm.Batch(dims, [w.lattice.shape[::-1] for w in ws], [w.ncells for w in ws])
+    for r, w in enumerate(ws):
+        b.lattice(r)[...] = w.lattice.view(np.int32)
+        w.apply(b, replica=r)
+    b.set_seed(2, 40)
+    b.set_dispatch(gpucpm.DISPATCH_HYBRID)
+    b.push_to_gpu()
+    b.run_mcs(2)
+    b.run_graph(2)
+    finish(b)
+    for r, w in enumerate(ws):
+        s = oracle.OracleSim(w.lattice, w.ncells, **w.oracle_kwargs(), seed=2, stream=40 + r)
+        s.run(2)
+        s.run(2)
+        np.testing.assert_array_equal(b.lattice(r).view(np.uint32), s.lattice)
+        area, perim, cs = b.tables(r)
+        np.testing.assert_array_equal(area, s.area)
+        np.testing.assert_array_equal(cs, s.csum)
+        np.testing.assert_array_equal(b.act_lattice(r).view(np.uint32), s.act)
+        if dims == 3:
+            pd, hist = b.persistence_state(r)
+            np.testing.assert_array_equal(pd, s.prefdir)
