@@ -367,6 +367,11 @@ int build_engine(int n, int ndim, const int* nx, const int* ny, const int* nz,
     const long long warps = (long long)c.grid * c.shape.warps;
     const long long nt = (long long)c.shape.cx * c.shape.cy * c.shape.cz;
     c.list_cap = 2LL * nt * c.shape.warps * ((max_tasks + warps - 1) / warps);
+    if (ndim == 2) {  // score launches run fewer warps per block (more tiles each)
+      const int sw = sweep_shape(ndim, v, true).warps;
+      const long long swarps = (long long)c.grid * sw;
+      c.list_cap = std::max(c.list_cap, 2LL * nt * sw * ((max_tasks + swarps - 1) / swarps));
+    }
     dlist_entries = std::max(dlist_entries, c.list_cap * 2 * c.grid);
     // Replica dispatch: one block per replica at a time; its dirty list takes
     // up to two rows per attempt of the replica's largest slot.

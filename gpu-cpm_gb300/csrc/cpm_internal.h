@@ -33,12 +33,12 @@ namespace gpucpm {
 
 constexpr int kMaxTypes = 32;
 // Warps per sweep block (one block per SM): 24 at 80 registers in 2D; 20 at
-// 96 registers in 3D, whose 26-neighbour attempt would spill at 80.
+// 96 registers in 3D and in score launches, whose attempts would spill at 80.
 constexpr int kMaxSweepWarps = 24;
 constexpr int kMaxSweepWarps3d = 20;
-template <int NDIM>
+template <int NDIM, bool SCORE = false>
 constexpr int max_sweep_warps() {
-  return NDIM == 3 ? kMaxSweepWarps3d : kMaxSweepWarps;
+  return (NDIM == 3 || SCORE) ? kMaxSweepWarps3d : kMaxSweepWarps;
 }
 constexpr int kSweepSmemMax = 227 * 1024;  // usable shared memory per block
 constexpr int kInitThreads = 256;
@@ -84,7 +84,7 @@ struct SweepShape {
   int warps;        // warps per block (tiles in flight per block)
   size_t smem;      // dynamic shared memory per block
 };
-SweepShape sweep_shape(int ndim, int variant);
+SweepShape sweep_shape(int ndim, int variant, bool scores = false);
 
 // ctl[] word indices (the barrier counter and its release flag sit in
 // different 128-byte lines so that waiting blocks do not slow down arriving

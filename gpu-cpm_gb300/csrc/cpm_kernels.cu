@@ -129,13 +129,13 @@ struct WarpSmem {
 
 // Warps per block of a variant: as many warp tiles as fit in shared memory,
 // at most max_sweep_warps (the register file's limit).
-template <int NDIM, int V>
+template <int NDIM, int V, bool SCORE = false>
 constexpr int variant_warps() {
   const size_t w = kSweepSmemMax / sizeof(WarpSmem<NDIM, V>);
-  return w < (size_t)max_sweep_warps<NDIM>() ? (int)w : max_sweep_warps<NDIM>();
+  return w < (size_t)max_sweep_warps<NDIM, SCORE>() ? (int)w : max_sweep_warps<NDIM, SCORE>();
 }
 
-template <int NDIM, int V>
+template <int NDIM, int V, bool SCORE = false>
 SweepShape shape_of() {
   using G = TileGeom<NDIM, V>;
   SweepShape s;
@@ -143,7 +143,7 @@ SweepShape shape_of() {
   s.cx = G::CX;
   s.cy = G::CY;
   s.cz = G::CZ;
-  s.warps = variant_warps<NDIM, V>();
+  s.warps = variant_warps<NDIM, V, SCORE>();
   s.smem = sizeof(WarpSmem<NDIM, V>) * (size_t)s.warps;
   return s;
 }
@@ -336,7 +336,7 @@ __device__ __forceinline__ void flush_scores(const SweepArgs& a, float* sc, int 
 // end of its phase.  Kept apart so that the other kernels carry none of its
 // registers.
 template <int NDIM, bool PERIM, int V, bool SCORE, bool EXT = false>
-__global__ void __launch_bounds__(32 * max_sweep_warps<NDIM>(), 1)
+__global__ void __launch_bounds__(32 * max_sweep_warps<NDIM, SCORE>(), 1)
     sweep_kernel(const SweepArgs a) {
   using G = TileGeom<NDIM, V>;
   using S = Stage<NDIM, V>;
@@ -1508,7 +1508,14 @@ cudaError_t launch_observe_heterotypic(const uint32_t* lat, const DevReplica* re
   return cudaGetLastError();
 }
 
-SweepShape sweep_shape(int ndim, int variant) {
+SweepShape sweep_shape(int ndim, int variant, bool scores) {
+  if (ndim == 2 && scores) {
+    switch (variant) {
+      case 1: return shape_of<2, 1, true>();
+      case 2: return shape_of<2, 2, true>();
+      default: return shape_of<2, 0, true>();
+    }
+  }
   if (ndim == 2) {
     switch (variant) {
       case 1: return shape_of<2, 1>();
@@ -1524,7 +1531,7 @@ SweepShape sweep_shape(int ndim, int variant) {
 }
 
 int sweep_max_blocks_per_sm(int ndim, bool perim, int variant, bool scores) {
-  const SweepShape sh = sweep_shape(ndim, variant);
+  const SweepShape sh = sweep_shape(ndim, variant, scores);
   const void* fn = sweep_fn(ndim, perim, variant, scores, false);
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)sh.smem) != cudaSuccess)
@@ -1540,7 +1547,7 @@ cudaError_t launch_sweep(int ndim, bool perim, int variant, const SweepArgs& a,
                          int grid, cudaStream_t s, bool scores) {
   const bool ext = a.act_on || a.prefdir;
   if (ext) variant = 0;  // the extended-term kernels are built for variant 0
-  const SweepShape sh = sweep_shape(ndim, variant);
+  const SweepShape sh = sweep_shape(ndim, variant, scores && !ext);
   const void* fn = sweep_fn(ndim, perim, variant, scores && !ext, ext);
   if (scores || ext) {  // these kernels get their shared-memory attribute on first use
     const cudaError_t e = cudaFuncSetAttribute(
