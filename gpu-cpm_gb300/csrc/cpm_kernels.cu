@@ -9,6 +9,15 @@
 //                              (area, perimeter, centroid sums).  Replaces
 //                              calculateAreasAndCircumferences{,3d}
 //                              (src/kernels2d.cu:5-41, src/kernels3d.cu:3-47).
+//   init_prefdir_kernel, persist_fill_kernel, persist_update_kernel
+//                              3D persistence: initial preferred directions,
+//                              the mean-coordinate ring and the per-run
+//                              direction update (src/kernels.cu:159-212).
+//   lr_backward_kernel         likelihood-ratio gradient from score sums.
+//   voronoi_kernel             periodic Voronoi seeding (bucketed, exact).
+//   observe_heterotypic_kernel, observe_boundaries_kernel
+//                              sorting order parameter and boundary lengths
+//                              by type pair.
 //
 // Sweep schedule.  Sites are coloured by their class on every axis (even /
 // odd / last coordinate of an odd axis); one phase ("slot") is one colour,
@@ -20,8 +29,9 @@
 // result is independent of thread, block and replica order, which is what
 // makes the CPU oracle (oracle/cpm_oracle.cpp) reproduce it bit for bit.
 //
-// Work decomposition.  One block of up to 24 warps per SM, one grid
-// barrier per slot.  The unit of work is a warp tile: CX x CY (x CZ)
+// Work decomposition.  One block per SM (24 warps at 80 registers in 2D; at
+// most 20 at 96 registers in 3D and in score launches), one grid barrier
+// per slot.  The unit of work is a warp tile: CX x CY (x CZ)
 // targets of one slot of one replica, staged with a one-site halo in the
 // warp's own shared memory (periodic wrap resolved while loading; even and
 // odd lattice columns kept in separate halves so that 32 consecutive
@@ -33,10 +43,14 @@
 //      source id equals the target's are dropped, the rest are queued with
 //      their direction and uniform;
 //   3. dH, Metropolis test, lattice write and table deltas.
-// A warp never waits for another warp inside a slot, so the 24 warps of an
-// SM hide each other's load latencies.  Tiles of a slot are flattened over
-// replicas (prefix table per slot) and dealt out warp-strided over the
-// grid, which balances ragged batches by work.
+// A warp never waits for another warp inside a slot, so the warps of an SM
+// hide each other's load latencies.  Tiles of a slot are flattened over
+// replicas (prefix table per slot).  A single lattice gives each block one
+// contiguous band of tile rows, the same in every slot (3D warps claim the
+// band's tiles from a shared counter); a batch deals its tiles warp-strided
+// over the grid, which balances ragged replicas by work.  Replica dispatch
+// instead lets each block run whole replicas with block barriers, and
+// hybrid runs (two launches, cpm_engine.cu) combine the two.
 //
 // Memory.  Mutable data (lattice, tables, deltas, dirty lists) is read with
 // ld.global.cg so that no SM serves a stale L1 line after a barrier; the
