@@ -8,10 +8,10 @@
 //   * one CUDA stream per handle instead of the legacy default stream;
 //   * one cooperative persistent launch per run() covers every MCS, slot and
 //     replica (the reference relaunches per inner_iterations and grid-syncs
-//     per attempt);
-//   * parameters live in per-replica device blocks uploaded once per run
-//     when changed (the reference re-uploads its __constant__ struct in every
-//     setter, src/kernels.cu:50-53);
+//     per attempt); hybrid-dispatch batches make two;
+//   * parameters live in device records shared by replicas (copy on write)
+//     and uploaded once per run when changed (the reference re-uploads its
+//     __constant__ struct in every setter, src/kernels.cu:50-53);
 //   * every call returns a status and keeps a message (the reference prints
 //     CUDA errors and carries on, src/cpm.cu:52-56).
 #include <algorithm>

@@ -16,12 +16,15 @@
 //                                        rows changed in a phase (a row may
 //                                        appear more than once)
 //   ctl    : uint32 [64]                 barrier counter / release flag,
-//                                        sticky error bits
+//                                        replica queue, sticky error bits
+//   (optional) field (chemotaxis, float), act stamps (uint32 per site),
+//   prefdir [rows][3] and the persistence ring [history][rows][3] (double)
 // Table double buffering: phase k reads copy k % 2 and adds its deltas both
 // into the other copy and into dap/dcs[k % 2]; phase k + 1 replays those
 // deltas into copy k % 2, which missed them (each delta is taken with an
 // exchange, so a row listed twice is replayed once).  So every phase reads
-// tables as they stood when it began, with one grid barrier per phase.  The tables are
+// tables as they stood when it began, with one grid barrier per phase.  The
+// tables are
 // small next to the lattice (4096^2 at 100 sites per cell: 67 MB of lattice,
 // 4 MB per table copy) and stay L2-resident through a run.
 #pragma once
