@@ -348,8 +348,10 @@ __device__ __forceinline__ void flush_scores(const SweepArgs& a, float* sc, int 
 // EXT: the instantiation (variant 0, no scores) with the act term and 3D
 // persistence; with act (a.act_on) every accepted copy is deferred to the
 // end of its phase.  Kept apart so that the other kernels carry none of its
-// registers.
-template <int NDIM, bool PERIM, int V, bool SCORE, bool EXT = false>
+// registers.  ONE: the instantiation of single-lattice grid launches (tile
+// bands per block, the replica index a constant), apart from the batch one
+// so that neither carries the other's loop.
+template <int NDIM, bool PERIM, int V, bool SCORE, bool EXT = false, bool ONE = false>
 __global__ void __launch_bounds__(32 * max_sweep_warps<NDIM, SCORE>(), 1)
     sweep_kernel(const SweepArgs a) {
   using G = TileGeom<NDIM, V>;
@@ -865,7 +867,7 @@ __global__ void __launch_bounds__(32 * max_sweep_warps<NDIM, SCORE>(), 1)
         // phase, so the band's lines and most of its halo stay with this
         // SM's side of L2.  Batches: tiles dealt round-robin over all warps
         // (the light edge tiles of ragged replicas would unbalance bands).
-        if (a.nrep == 1 && a.rep_map == nullptr) {
+        if constexpr (ONE) {
           const int per_b = ntiles / (int)gridDim.x, extra = ntiles % (int)gridDim.x;
           const int tb0 = (int)blockIdx.x * per_b + min((int)blockIdx.x, extra);
           const int tb1 = tb0 + per_b + ((int)blockIdx.x < extra ? 1 : 0);
@@ -900,7 +902,7 @@ __global__ void __launch_bounds__(32 * max_sweep_warps<NDIM, SCORE>(), 1)
     // Final replay: the last phase's deltas into the copy it read, so that
     // both copies agree when the kernel ends.
     if (step > 0) replay_phase((step - 1) & 1);
-  } else {
+  } else if constexpr (!ONE) {
     // Replica dispatch: a block claims whole replicas (largest first) and
     // runs all their MCS with block barriers between phases; a replica's
     // lattice and tables then stay in this SM's share of L2.  The one grid
@@ -1053,7 +1055,10 @@ __global__ void barrier_probe(uint32_t* ctl, unsigned long long timeout_ns) {
 }
 
 template <int NDIM, int V>
-const void* sweep_fn_v(bool perim, bool scores, bool act) {
+const void* sweep_fn_v(bool perim, bool scores, bool act, bool one = false) {
+  if (one && !scores && !act)
+    return perim ? (const void*)sweep_kernel<NDIM, true, V, false, false, true>
+                 : (const void*)sweep_kernel<NDIM, false, V, false, false, true>;
   if constexpr (V == 0) {
     if (act)
       return perim ? (const void*)sweep_kernel<NDIM, true, 0, false, true>
@@ -1070,19 +1075,19 @@ const void* sweep_fn_v(bool perim, bool scores, bool act) {
 
 // Score launches exist for 2D lattices (the differentiable ensembles), act
 // launches for variant 0 without scores (the engine sees to both).
-const void* sweep_fn(int ndim, bool perim, int variant, bool scores, bool act) {
+const void* sweep_fn(int ndim, bool perim, int variant, bool scores, bool act, bool one = false) {
   if (act) variant = 0;
   if (ndim == 2) {
     switch (variant) {
-      case 1: return sweep_fn_v<2, 1>(perim, scores, false);
-      case 2: return sweep_fn_v<2, 2>(perim, scores, false);
-      default: return sweep_fn_v<2, 0>(perim, act ? false : scores, act);
+      case 1: return sweep_fn_v<2, 1>(perim, scores, false, one);
+      case 2: return sweep_fn_v<2, 2>(perim, scores, false, one);
+      default: return sweep_fn_v<2, 0>(perim, act ? false : scores, act, one);
     }
   }
   switch (variant) {
-    case 1: return sweep_fn_v<3, 1>(perim, false, false);
-    case 2: return sweep_fn_v<3, 2>(perim, false, false);
-    default: return sweep_fn_v<3, 0>(perim, false, act);
+    case 1: return sweep_fn_v<3, 1>(perim, false, false, one);
+    case 2: return sweep_fn_v<3, 2>(perim, false, false, one);
+    default: return sweep_fn_v<3, 0>(perim, false, act, one);
   }
 }
 
@@ -1562,8 +1567,11 @@ cudaError_t launch_sweep(int ndim, bool perim, int variant, const SweepArgs& a,
   const bool ext = a.act_on || a.prefdir;
   if (ext) variant = 0;  // the extended-term kernels are built for variant 0
   const SweepShape sh = sweep_shape(ndim, variant, scores && !ext);
-  const void* fn = sweep_fn(ndim, perim, variant, scores && !ext, ext);
-  if (scores || ext) {  // these kernels get their shared-memory attribute on first use
+  // single-lattice grid launches have kernels of their own (tile bands, the
+  // replica index a constant)
+  const bool one = a.nrep == 1 && a.rep_map == nullptr && !a.block_local && !scores && !ext;
+  const void* fn = sweep_fn(ndim, perim, variant, scores && !ext, ext, one);
+  if (scores || ext || one) {  // these kernels get their shared-memory attribute on first use
     const cudaError_t e = cudaFuncSetAttribute(
         fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem);
     if (e != cudaSuccess) return e;
