@@ -428,9 +428,12 @@ __global__ void __launch_bounds__(32 * max_sweep_warps<NDIM, SCORE>(), 1)
 
   // One warp tile of replica r (its `local`-th tile of the slot): stage the
   // tile, then boundary test, source pick and dH / test / commit.
-  auto run_tile = [&](const PhaseTables<NDIM>& pt, const int r, const int local,
-                      const int cx, const int cy, const int cz,
-                      const unsigned long long tick, const unsigned long long phase) {
+  // A tile by its coordinates in the replica's tile grid of the slot (tz is
+  // the third coordinate in 3D; in 2D the grid has one layer).
+  auto run_tile_at = [&](const PhaseTables<NDIM>& pt, const int r, const int tx,
+                         const int ty, const int tz, const int cx, const int cy,
+                         const int cz, const unsigned long long tick,
+                         const unsigned long long phase) {
     if (r != cnt_rep) {
       if (lane == 0 && cnt_rep >= 0) {
         if (n_eval) atomicAdd(&a.counters[2 * cnt_rep], n_eval);
@@ -456,10 +459,6 @@ __global__ void __launch_bounds__(32 * max_sweep_warps<NDIM, SCORE>(), 1)
     const long long cell_off = __ldg(&a.reps[r].cell_off);
     const int ncx = class_count(nx, cx), ncy = class_count(ny, cy),
               ncz = class_count(nz, cz);
-    const int tnx = (ncx + G::CX - 1) / G::CX;
-    const int tny = (ncy + G::CY - 1) / G::CY;
-    const int tx = local % tnx, rest = local / tnx;
-    const int ty = rest % tny, tz = rest / tny;
     const int i0 = tx * G::CX, j0 = ty * G::CY, l0 = tz * G::CZ;
     const int cntx = min(G::CX, ncx - i0), cnty = min(G::CY, ncy - j0),
               cntz = min(G::CZ, ncz - l0);
@@ -827,6 +826,22 @@ __global__ void __launch_bounds__(32 * max_sweep_warps<NDIM, SCORE>(), 1)
     __syncwarp();  // the tile buffers are rewritten by the next tile
   };
 
+  // Tiles per row and per layer of replica r's slot (cx, cy).
+  auto tile_grid = [&](const int r, const int cx, const int cy, int& tnx, int& tny) {
+    tnx = (class_count(__ldg(&a.reps[r].nx), cx) + G::CX - 1) / G::CX;
+    tny = (class_count(__ldg(&a.reps[r].ny), cy) + G::CY - 1) / G::CY;
+  };
+  // A tile by its index within the replica's slot.
+  auto run_tile = [&](const PhaseTables<NDIM>& pt, const int r, const int local,
+                      const int cx, const int cy, const int cz,
+                      const unsigned long long tick, const unsigned long long phase) {
+    int tnx, tny;
+    tile_grid(r, cx, cy, tnx, tny);
+    const int tx = local % tnx, rest = local / tnx;
+    const int ty = rest % tny, tz = rest / tny;
+    run_tile_at(pt, r, tx, ty, tz, cx, cy, cz, tick, phase);
+  };
+
   // The block's tiles of one phase.  3D: warp w starts with tile w, then
   // claims the next unclaimed one from a shared counter, so the phase ends
   // within one tile on every warp (a 256^3 slot gives a block ~54 tiles of
@@ -875,8 +890,20 @@ __global__ void __launch_bounds__(32 * max_sweep_warps<NDIM, SCORE>(), 1)
             claimed_tiles(tb1 - tb0,
                           [&](int k) { run_tile(pt, 0, tb0 + k, cx, cy, cz, tick, phase); });
           } else {
-            for (int task = tb0 + warp; task < tb1; task += wpb)
-              run_tile(pt, 0, task, cx, cy, cz, tick, phase);
+            // tile coordinates stepped by the warp stride, not divided out
+            // per tile
+            int tnx, tny;
+            tile_grid(0, cx, cy, tnx, tny);
+            int task = tb0 + warp;
+            int tx = task % tnx, ty = (task / tnx) % tny;
+            for (; task < tb1; task += wpb) {
+              run_tile_at(pt, 0, tx, ty, 0, cx, cy, cz, tick, phase);
+              tx += wpb;
+              while (tx >= tnx) {
+                tx -= tnx;
+                ++ty;
+              }
+            }
           }
         } else {
           for (int task = (int)blockIdx.x * wpb + warp; task < ntiles;
