@@ -43,3 +43,28 @@ def test_invalid_arguments_rejected_before_touching_cuda(engine_lib):
     assert b"dimensionality" in engine_lib.cpm_last_error(None)
     assert engine_lib.cpm_create(64, 2, 10, 10.0, 4, ctypes.byref(h)) == 6  # unknown flag
     assert engine_lib.cpm_create(2, 2, 10, 10.0, 0, ctypes.byref(h)) == 1
+
+
+def test_static_sweep_refuses_handle_only_terms_before_touching_cuda(engine_lib):
+    """cpm_sweep_static models adhesion, area, perimeter, stickiness and fixed
+    types; a record with a chemotaxis, act or persistence lambda is refused
+    (CPM_ERR_UNSUPPORTED) before any CUDA call, and bad sizes are refused
+    with CPM_ERR_INVALID."""
+    import sys
+    sys.path.insert(0, str(ROOT / "gpu-cpm_gb300"))
+    from gpucpm import StaticParams
+    f = engine_lib.cpm_sweep_static
+    f.argtypes = [ctypes.c_int] * 5 + [ctypes.c_void_p] * 4 + [
+        ctypes.c_int, ctypes.POINTER(StaticParams), ctypes.c_uint64, ctypes.c_uint32,
+        ctypes.c_uint64, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    buf = (ctypes.c_uint32 * 64)()  # never dereferenced: the calls fail first
+    ptr = ctypes.addressof(buf)
+    for field in ("chemotaxis", "act_lambda", "persistence_lambda"):
+        p = StaticParams()
+        getattr(p, field)[1] = 1.0
+        rc = f(2, 8, 8, 1, 4, ptr, ptr, ptr, ptr, 0, ctypes.byref(p), 0, 0, 0, 1, None, None)
+        assert rc == 6, field  # CPM_ERR_UNSUPPORTED
+        assert b"handle engine" in engine_lib.cpm_last_error(None)
+    p = StaticParams()
+    assert f(2, 2, 8, 1, 4, ptr, ptr, ptr, ptr, 0, ctypes.byref(p), 0, 0, 0, 1, None,
+             None) == 1  # a side below 3
