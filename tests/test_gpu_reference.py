@@ -15,6 +15,7 @@ reference sources by oracle/ref_gpu/build.py and driven by ref_driver.cpp).
    within the tolerances below.
 """
 import json
+import os
 import pathlib
 
 import numpy as np
@@ -30,7 +31,8 @@ if not ref_gpu.available():
     pytest.skip("reference cubin not built (needs the reference checkout)",
                 allow_module_level=True)
 
-REPORT = pathlib.Path(__file__).resolve().parents[1] / "gpurun_out"
+REPORT = pathlib.Path(os.environ.get("CPM_TEST_REPORT_DIR",
+                                    pathlib.Path(__file__).resolve().parents[1] / "test_reports"))
 
 
 def _ours(w, seed=0, stream=0):
