@@ -240,3 +240,77 @@ def test_sorting_statistics_match_reference(engine_lib):
                    ("cells", 0.10), ("heterotypic", 0.10), ("activity", 0.15)):
         o, r = summary[k]["ours_mean"], summary[k]["ref_mean"]
         assert abs(o - r) <= tol * abs(r), (k, summary[k])
+
+
+def _observables_3d(lat, prev):
+    ids = (lat & 0xFFFFFF).astype(np.int64)
+    vols = np.bincount(ids.ravel())[1:]
+    alive = vols > 0
+    lat64 = lat.astype(np.int64)
+    surf = np.zeros_like(vols)
+    for dz in (-1, 0, 1):
+        for dy in (-1, 0, 1):
+            for dx in (-1, 0, 1):
+                if dz == dy == dx == 0:
+                    continue
+                nb = np.roll(lat64, (-dz, -dy, -dx), axis=(0, 1, 2))
+                diff = (nb != lat64) & (ids > 0)
+                surf += np.bincount(ids[diff], minlength=len(vols) + 1)[1:]
+    return {"mean_volume": float(vols[alive].mean()), "sd_volume": float(vols[alive].std()),
+            "mean_surface": float(surf[alive].mean()), "cells": int(alive.sum()),
+            "activity": float((lat != prev).mean())}
+
+
+def test_tissue3d_statistics_match_reference(engine_lib):
+    """A 64^3 Voronoi tissue (2 types, integer J in [4, 16], V* = 500,
+    lambda_V = 1, S* = 350, lambda_S = 0.2, T = 20) after 200 MCS, 4 seeds
+    each.  The reference runs its 3D kernel (src/kernels3d.cu, non-shared,
+    grid sync per attempt) with 4^3-thread blocks, 4 sites per thread and
+    2x2x2 checkerboard squares."""
+    w = W.tissue_3d(n=64, volume=500, seed=6)
+    w.J = np.rint(w.J).astype(np.float32)
+    mcs, tail = 200, 5
+    ours, refs = [], []
+    for seed in range(1, 5):
+        e = _ours(w, seed=seed)
+        e.run_mcs(mcs - tail)
+        e.synchronize()
+        e.pull_from_gpu()
+        prev = e.get_state().view(np.uint32).copy()
+        e.run_mcs(tail)
+        e.synchronize()
+        e.pull_from_gpu()
+        ours.append(_observables_3d(e.get_state().view(np.uint32), prev))
+
+        r = _ref(w)
+        kw = dict(threads_per_block=4, positions_per_thread=4, positions_per_checkerboard=2)
+        r.run(mcs - tail, seed=seed, **kw)
+        r.synchronize()
+        prev = r.pull()
+        r.run(tail, seed=seed + 1000, **kw)
+        r.synchronize()
+        refs.append(_observables_3d(r.pull(), prev))
+
+    summary = {}
+    for k in ours[0]:
+        a = np.array([o[k] for o in ours], float)
+        b = np.array([o[k] for o in refs], float)
+        summary[k] = {"ours_mean": a.mean(), "ours_sd": a.std(ddof=1),
+                      "ref_mean": b.mean(), "ref_sd": b.std(ddof=1)}
+    REPORT.mkdir(exist_ok=True)
+    (REPORT / "reference_tissue3d_stats.json").write_text(json.dumps(summary, indent=1))
+    # Stated tolerances (relative to the reference's mean over seeds):
+    #   mean volume, mean surface, surviving cells   5 %
+    #   volume spread                                 15 %
+    #   site activity                                 40 %
+    # The tissue nearly freezes (cells shrink to ~62 voxels under the steep
+    # surface term), and the rare moves left are sensitive to the schedule.
+    # An oracle run that commits every copy at once, as the reference's
+    # live reads do, has 12 % less activity than the phase-snapshot rule
+    # this engine follows.  The rest of the gap comes from the reference's
+    # random site per attempt and its self-picks of :208.  The state
+    # itself (volumes, surfaces, cells) agrees within a few percent.
+    for k, tol in (("mean_volume", 0.05), ("mean_surface", 0.05), ("cells", 0.05),
+                   ("sd_volume", 0.15), ("activity", 0.40)):
+        o, r = summary[k]["ours_mean"], summary[k]["ref_mean"]
+        assert abs(o - r) <= tol * abs(r), (k, summary[k])
