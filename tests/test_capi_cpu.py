@@ -68,3 +68,22 @@ def test_static_sweep_refuses_handle_only_terms_before_touching_cuda(engine_lib)
     p = StaticParams()
     assert f(2, 2, 8, 1, 4, ptr, ptr, ptr, ptr, 0, ctypes.byref(p), 0, 0, 0, 1, None,
              None) == 1  # a side below 3
+
+
+def test_c_example_compiles_and_links(engine_lib, tmp_path):
+    """tests/capi/example2d.c, a C caller of include/gpucpm.h only, builds
+    with the system C compiler and links against the library (it runs in
+    tests/test_gpu_api.py)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("cc") or shutil.which("gcc")
+    if cc is None:
+        return
+    lib_dir = ROOT / "gpu-cpm_gb300"
+    out = tmp_path / "example2d"
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-I", str(ROOT / "include"),
+                        str(ROOT / "tests" / "capi" / "example2d.c"), "-L", str(lib_dir),
+                        "-lgpucpm_gb300", f"-Wl,-rpath,{lib_dir}", "-o", str(out)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert out.exists()

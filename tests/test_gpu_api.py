@@ -190,3 +190,37 @@ def test_barrier_timeout_is_reported_not_hung(engine_lib):
     sim.push_to_gpu()
     sim.run(**_run_kw(10))
     sim.synchronize()
+
+
+def test_c_example_matches_python(engine_lib, tmp_path):
+    """tests/capi/example2d.c (the C-ABI alone) prints the same centroids as
+    the same run through gpucpm.Cpm."""
+    import pathlib
+    import shutil
+    import subprocess
+
+    import gpucpm
+    root = pathlib.Path(__file__).resolve().parents[1]
+    cc = shutil.which("cc") or shutil.which("gcc")
+    assert cc, "no C compiler"
+    lib_dir = root / "gpu-cpm_gb300"
+    exe = tmp_path / "example2d"
+    subprocess.run([cc, "-std=c99", "-I", str(root / "include"),
+                    str(root / "tests" / "capi" / "example2d.c"), "-L", str(lib_dir),
+                    "-lgpucpm_gb300", f"-Wl,-rpath,{lib_dir}", "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0, out.stderr
+    got = np.array([[float(v) for v in line.split()] for line in out.stdout.split("\n") if line])
+
+    sim = gpucpm.Cpm(256, 2, 10, 20, False)
+    sim.set_seed(7, 0)
+    sim.add_cell(1, 100, 100)
+    sim.add_cell(1, 200, 200)
+    sim.add_cell(1, 200, 100)
+    sim.set_constraints(cell_type=1, lambda_area=10, target_area=200)
+    sim.set_constraints(cell_type=0, other_cell_type=1, adhesion=10)
+    sim.push_to_gpu()
+    sim.run(**_run_kw(2000))
+    sim.synchronize()
+    want = sim.get_centroids()
+    np.testing.assert_allclose(got, want, rtol=0, atol=1e-6)  # printed with 6 decimals
