@@ -224,3 +224,39 @@ def test_c_example_matches_python(engine_lib, tmp_path):
     sim.synchronize()
     want = sim.get_centroids()
     np.testing.assert_allclose(got, want, rtol=0, atol=1e-6)  # printed with 6 decimals
+
+
+def test_two_engines_interleaved_equal_each_alone(engine_lib):
+    """Handles share no state: two engines whose runs interleave on their own
+    streams end exactly as each does alone."""
+    import gpucpm
+    from gpucpm import workloads as W
+
+    def make(w, seed):
+        e = gpucpm.create_box(w.lattice.shape[1], w.lattice.shape[0], 1, 2, w.ncells,
+                              w.temperature)
+        e.lattice(0)[...] = w.lattice.view(np.int32)
+        w.apply(e, replica=0)
+        e.set_seed(seed, 0)
+        e.push_to_gpu()
+        return e
+
+    wa = W.random_small((96, 80), 60, seed=31, temperature=9.0)
+    wb = W.random_small((64, 72), 40, seed=32, temperature=7.0)
+    alone = []
+    for w, seed in ((wa, 1), (wb, 2)):
+        e = make(w, seed)
+        for _ in range(4):
+            e.run_mcs(5)
+        e.synchronize()
+        e.pull_from_gpu()
+        alone.append(e.lattice(0).copy())
+    ea, eb = make(wa, 1), make(wb, 2)
+    for _ in range(4):
+        ea.run_mcs(5)
+        eb.run_mcs(5)
+    for e in (ea, eb):
+        e.synchronize()
+        e.pull_from_gpu()
+    np.testing.assert_array_equal(ea.lattice(0), alone[0])
+    np.testing.assert_array_equal(eb.lattice(0), alone[1])
