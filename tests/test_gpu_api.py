@@ -260,3 +260,35 @@ def test_two_engines_interleaved_equal_each_alone(engine_lib):
         e.pull_from_gpu()
     np.testing.assert_array_equal(ea.lattice(0), alone[0])
     np.testing.assert_array_equal(eb.lattice(0), alone[1])
+
+
+def test_create_run_destroy_does_not_leak(engine_lib):
+    """Engines with every optional buffer (field, act stamps, persistence
+    state) release all device memory when destroyed."""
+    import torch
+
+    import gpucpm
+
+    def cycle():
+        sim = gpucpm.Cpm(64, 3, 20, 10, True, 2, 1)
+        for k in range(5):
+            sim.add_cell(1, 10 + 9 * k, 12, 20)
+        sim.set_constraints(cell_type=1, lambda_area=2, target_area=100)
+        sim.set_constraints(cell_type=0, other_cell_type=1, adhesion=10)
+        sim.set_constraints(cell_type=1, lambda_persistence=5.0, persistence_diffusion=0.5,
+                            persistence_time=3)
+        sim.push_to_gpu()
+        sim.run_mcs(3)
+        sim.synchronize()
+        assert sim.persistence_exists and sim.act_exists
+        del sim
+        gc.collect()
+
+    cycle()  # first use: module loads, context growth
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(10):
+        cycle()
+    torch.cuda.synchronize()
+    free1 = torch.cuda.mem_get_info()[0]
+    assert free0 - free1 < 8 * 1024 * 1024, (free0, free1)  # under one engine's worth
