@@ -56,7 +56,7 @@ def parse_args():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--workload", default="tissue_2d",
                    choices=["tissue_2d", "tissue_2d_8192", "tissue_3d", "sorting_2d",
-                            "ensemble", "sorting_batch", "gradient", "gradient_check"])
+                            "sorting_2d_256", "ensemble", "sorting_batch", "gradient", "gradient_check"])
     p.add_argument("--replicas", type=int, default=None,
                    help="replicas of --workload ensemble (256) / gradient (512)")
     p.add_argument("--mcs", type=int, default=None, help="MCS per step")
@@ -84,6 +84,11 @@ def build_workload(name):
         return W.tissue_3d()
     if name == "sorting_2d":
         return W.sorting_2d()
+    if name == "sorting_2d_256":
+        # the same recipe at the reference's own sorting size (a power of two,
+        # which its neighbour wrap needs): 655 5x5 cells, the density of 400
+        # cells on 200^2
+        return W.sorting_2d(n=256, ncells=655)
     raise ValueError(name)
 
 
@@ -94,6 +99,12 @@ def describe(w, mcs):
             "mcs_per_step": mcs, "neighbourhood": "moore8" if w.ndim == 2 else "moore26",
             "l2": "flushed between steps (512 MB write, outside the timed events)",
             "seed": 0}
+
+
+def data_of(w):
+    if w.name.startswith("tissue"):
+        return "synthetic (seeded Voronoi tissue)"
+    return "synthetic (seeded 5x5 squares, two-type sorting)"
 
 
 def measured_peak_hbm():
@@ -231,27 +242,35 @@ def reference_gpu_baseline(w, timed_mcs=100, probe_mcs=10):
     as in its examples (updates_per_barrier = 1, global_sync = 1) and the
     partial_dispatch kernel variant.  J and T are rounded to integers as the
     reference stores them.  Returns None when the reference build is absent.
+
+    3D runs the non-shared variant only: the shared one asks for 128 KB of
+    dynamic shared memory without the opt-in above 48 KB and cannot launch
+    (the opt-in is commented out at src/cpm.cu:450).  Its blocks have tpb^3 threads
+    and each thread makes ppt^3 attempts per MCS, one grid sync each, so
+    ppt stops at 16 and the 26-neighbour sweep gets fewer MCS per probe.
     """
     try:
         from oracle import ref_gpu
     except Exception:
         return None
-    if not ref_gpu.available() or w.ndim != 2:
+    if not ref_gpu.available() or w.ndim not in (2, 3):
         return None
     import torch
     n = w.lattice.shape[0]
-    r = ref_gpu.RefGpu(n, 2, w.ncells, w.temperature, device=torch.cuda.current_device())
+    r = ref_gpu.RefGpu(n, w.ndim, w.ncells, w.temperature, device=torch.cuda.current_device())
     r.apply(w)
+    if w.ndim == 3:
+        timed_mcs, probe_mcs = max(1, timed_mcs // 2), max(1, probe_mcs // 2)
     best = None
     tried = []
-    for shared in (0, 1):
-        for tpb in (4, 8, 16, 32):
+    for shared in ((0, 1) if w.ndim == 2 else (0,)):
+        for tpb in ((4, 8, 16, 32) if w.ndim == 2 else (4, 8)):
             cap = r.max_coop_blocks(tpb, shared)
-            for ppt in (2, 4, 8, 16, 32, 64):
+            for ppt in ((2, 4, 8, 16, 32, 64) if w.ndim == 2 else (2, 4, 8, 16)):
                 if n % (tpb * ppt):
                     continue
                 blocks = n // (tpb * ppt)
-                if blocks * blocks > cap:
+                if blocks ** w.ndim > cap:
                     continue
                 for ppc in (1, 2, 4, 8):
                     if ppc > ppt or ppt % ppc or (shared and ppt % (2 * ppc)):
@@ -313,7 +332,7 @@ def run_reference(args, world, rank):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u32+f32",
-            "data": "synthetic (seeded Voronoi tissue)", "config": cfg,
+            "data": data_of(w), "config": cfg,
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": f"1 MCS of the {w.name} lattice per step, "
                                        f"{threads} OpenMP threads; the reference has no "
@@ -471,7 +490,7 @@ def run_ours(args, world, rank, local):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "u32+f32", "data": "synthetic (seeded Voronoi tissue)",
+            "dtype": "u32+f32", "data": data_of(w),
             "config": dict(describe(w, mcs), tile=sim.sweep_config()["tile"]),
             "roofline": roofline,
             "issue_roofline": issue_roofline(args.workload, value / world, clocks, torch,

@@ -47,12 +47,15 @@ constexpr int kSweepSmemMax = 227 * 1024;  // usable shared memory per block
 constexpr int kInitThreads = 256;
 
 // Warp tile: CX x CY x CZ targets of one slot, staged with their one-site
-// halo in the warp's own shared memory.  Three compiled variants per
+// halo in the warp's own shared memory.  Four compiled variants per
 // dimensionality; the autotuner (cpm_autotune) picks one per engine.  The
 // sweep's result does not depend on the variant.
-//   2D  v0 32 x 8 (66 x 17 sites)   v1 32 x 4    v2 32 x 16
-//   3D  v0 32 x 2 x 2 (66 x 5 x 5)  v1 32 x 4 x 2  v2 32 x 4 x 4
-constexpr int kTileVariants = 3;
+//   2D  v0 32 x 6 (66 x 13 sites)   v1 32 x 8      v2 32 x 16     v3 32 x 1
+//   3D  v0 32 x 2 x 2 (66 x 5 x 5)  v1 32 x 4 x 2  v2 32 x 4 x 4  v3 32 x 1 x 1
+// v3 is for lattices too small to give every warp of the GPU a wide tile
+// (256^2 has 85 tiles of 32 x 6 per slot): one row of targets per warp cuts
+// the serial chain of a phase to one iteration of each pass.
+constexpr int kTileVariants = 4;
 template <int NDIM, int V>
 struct TileGeom;
 template <>
@@ -68,6 +71,10 @@ struct TileGeom<2, 2> {
   static constexpr int CX = 32, CY = 16, CZ = 1;
 };
 template <>
+struct TileGeom<2, 3> {
+  static constexpr int CX = 32, CY = 1, CZ = 1;
+};
+template <>
 struct TileGeom<3, 0> {
   static constexpr int CX = 32, CY = 2, CZ = 2;
 };
@@ -78,6 +85,10 @@ struct TileGeom<3, 1> {
 template <>
 struct TileGeom<3, 2> {
   static constexpr int CX = 32, CY = 4, CZ = 4;
+};
+template <>
+struct TileGeom<3, 3> {
+  static constexpr int CX = 32, CY = 1, CZ = 1;
 };
 
 // Launch shape of one sweep configuration.

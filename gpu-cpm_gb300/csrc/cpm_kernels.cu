@@ -1108,12 +1108,14 @@ const void* sweep_fn(int ndim, bool perim, int variant, bool scores, bool act, b
     switch (variant) {
       case 1: return sweep_fn_v<2, 1>(perim, scores, false, one);
       case 2: return sweep_fn_v<2, 2>(perim, scores, false, one);
+      case 3: return sweep_fn_v<2, 3>(perim, scores, false, one);
       default: return sweep_fn_v<2, 0>(perim, act ? false : scores, act, one);
     }
   }
   switch (variant) {
     case 1: return sweep_fn_v<3, 1>(perim, false, false, one);
     case 2: return sweep_fn_v<3, 2>(perim, false, false, one);
+    case 3: return sweep_fn_v<3, 3>(perim, false, false, one);
     default: return sweep_fn_v<3, 0>(perim, false, act, one);
   }
 }
@@ -1559,6 +1561,7 @@ SweepShape sweep_shape(int ndim, int variant, bool scores) {
     switch (variant) {
       case 1: return shape_of<2, 1, true>();
       case 2: return shape_of<2, 2, true>();
+      case 3: return shape_of<2, 3, true>();
       default: return shape_of<2, 0, true>();
     }
   }
@@ -1566,12 +1569,14 @@ SweepShape sweep_shape(int ndim, int variant, bool scores) {
     switch (variant) {
       case 1: return shape_of<2, 1>();
       case 2: return shape_of<2, 2>();
+      case 3: return shape_of<2, 3>();
       default: return shape_of<2, 0>();
     }
   }
   switch (variant) {
     case 1: return shape_of<3, 1>();
     case 2: return shape_of<3, 2>();
+    case 3: return shape_of<3, 3>();
     default: return shape_of<3, 0>();
   }
 }

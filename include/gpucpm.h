@@ -313,7 +313,7 @@ int cpm_run_graph(cpm_handle* h, int mcs);
  * (src/python_wrapper.cpp:182-227). */
 int cpm_autotune(cpm_handle* h, int probe_mcs, int* chosen, float* ms_per_mcs);
 
-/* Select a tile variant (0, 1 or 2) or a dispatch explicitly / describe the
+/* Select a tile variant (0 to 3) or a dispatch explicitly / describe the
  * current launch: warp tile extent in targets, warps per block, grid size
  * and dispatch. */
 int cpm_set_variant(cpm_handle* h, int variant);

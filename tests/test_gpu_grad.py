@@ -29,13 +29,18 @@ def _ensemble_workloads(n=3, side=48, seed=50):
     return out
 
 
-def test_scores_match_oracle_and_leave_dynamics_unchanged(engine_lib):
+@pytest.mark.parametrize("variant", [None, 3])
+def test_scores_match_oracle_and_leave_dynamics_unchanged(engine_lib, variant):
+    """variant None: the engine's default tile; 3: the one-row tile, whose
+    score kernels have their own instantiation."""
     import torch
 
     import gpucpm
     ws = _ensemble_workloads()
     spec = gpucpm.ScoreSpec.make(PAIRS, lambda_perim=True)
     b = gpucpm.Batch(2, [w.lattice.shape[::-1] for w in ws], [w.ncells for w in ws])
+    if variant is not None:
+        b.set_variant(variant)
     for r, w in enumerate(ws):
         b.lattice(r)[...] = w.lattice.view(np.int32)
         w.apply(b, replica=r)
