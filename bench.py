@@ -226,9 +226,15 @@ def cpu_baseline(w, target_s=10.0, max_mcs=20):
         sim.run(extra, nthreads=threads)
     total = first + (time.perf_counter() - t1)
     mcs = 1 + extra
+    # one more MCS on one thread: the per-core rate beside the all-core one
+    t2 = time.perf_counter()
+    sim.run(1, nthreads=1)
+    one = time.perf_counter() - t2
     return {"value": w.nsites * mcs / total, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{mcs} MCS of the {'x'.join(map(str, w.lattice.shape[::-1]))} "
-                      f"{w.name} lattice from its seeded initial state ({total:.1f} s)"}
+                      f"{w.name} lattice from its seeded initial state ({total:.1f} s)",
+            "single_thread": {"value": w.nsites / one, "unit": UNIT, "cores": 1,
+                              "sample": f"the next MCS on one thread ({one:.2f} s)"}}
 
 
 def reference_gpu_baseline(w, timed_mcs=100, probe_mcs=10):
