@@ -492,6 +492,9 @@ class _Engine:
         return v.value, ms.value
 
     def set_variant(self, variant):
+        """Warp tile in targets: 0 = 32x6 (3D 32x2x2), 1 = 32x8 (32x4x2),
+        2 = 32x16 (32x4x4), 3 = 32x1 (32x1x1, for lattices too small to
+        give every warp a wider tile).  The result does not depend on it."""
         self._call("cpm_set_variant", int(variant))
 
     def set_dispatch(self, dispatch):

@@ -302,7 +302,8 @@ int cpm_run_graph(cpm_handle* h, int mcs);
 #define CPM_DISPATCH_HYBRID 2
 
 /* Project autotuner: times `probe_mcs` MCS of every compiled tile variant
- * (warp tile shape and warps per block), under both dispatches for a batch,
+ * (warp tile shape and warps per block), under each dispatch for a batch
+ * (grid, replica, and hybrid where it splits the batch into two parts),
  * three times each (the fastest run counts: a first launch also loads its
  * module; a GPU coming out of idle should be warmed up first),
  * on a saved copy of the current state, restores the state, and makes the
