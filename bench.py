@@ -597,7 +597,8 @@ def run_ensemble(args, world, rank, local):
     batched_ms = dev_s / args.steps * 1e3
 
     # The same replicas as a per-replica launch loop: one single-lattice
-    # engine per replica, launched back to back on one stream.
+    # engine per replica, each with the tile its own autotuner picks,
+    # launched back to back on one stream.
     loop_ms = None
     engines = [] if not args.no_loop else None
     if engines is not None:
@@ -612,6 +613,7 @@ def run_ensemble(args, world, rank, local):
             engines.append(e)
         for e in engines:
             e.run_mcs(2)  # warm-up
+            e.autotune(probe_mcs=4)
         torch.cuda.synchronize()
         t0 = torch.cuda.Event(enable_timing=True)
         t1 = torch.cuda.Event(enable_timing=True)
@@ -652,8 +654,8 @@ def run_ensemble(args, world, rank, local):
             "gpu_launches": int(launches),
             "batched_vs_loop": None if loop_ms is None else {
                 "batched_ms": batched_ms, "loop_ms": loop_ms, "speedup": loop_ms / batched_ms,
-                "loop": "one single-lattice engine per replica, launched back to back "
-                        "on one stream"},
+                "loop": "one single-lattice engine per replica, each with its own "
+                        "autotuned tile, launched back to back on one stream"},
             "autotune": {"variant": variant, "probe_ms_per_mcs": tuned_ms,
                          "dispatch": b.sweep_config()["dispatch"]},
             "step_ms": step_ms, "e2e": None}
