@@ -45,6 +45,7 @@ for _p in (str(ROOT), str(PKG)):
 METRIC = "copy-attempts/s"
 UNIT = "attempts/s"
 BYTES_PER_ATTEMPT = 8
+REFERENCE_RELAX_MCS = 100  # reference arm: MCS run before its timed steps (20 s at most)
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -71,6 +72,11 @@ def parse_args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-reference-gpu", action="store_true",
                    help="skip timing the reference's own CUDA sweep on this GPU")
+    p.add_argument("--no-secondary", action="store_true",
+                   help="default workload: skip the compact results of the 256^3 tissue, "
+                        "the ragged ensemble and the gradient ensemble")
+    p.add_argument("--no-fd", action="store_true",
+                   help="gradient workloads: time only (no finite-difference comparison)")
     return p.parse_args()
 
 
@@ -237,17 +243,41 @@ def cpu_baseline(w, target_s=10.0, max_mcs=20):
                               "sample": f"the next MCS on one thread ({one:.2f} s)"}}
 
 
-def reference_gpu_baseline(w, timed_mcs=100, probe_mcs=10):
+# The reference's synchronisation modes (its run() knobs, src/kernels2d.cu:
+# 179-195, src/kernels3d.cu:140-156):
+#   grid_each     grid sync before every attempt (its examples' setting)
+#   grid_region   grid sync after every ppc^2 attempts, each thread finishing
+#                 its ppc x ppc sub-square first (updates_per_barrier =
+#                 updates_per_checkerboard_switch = ppc^2); still race-free,
+#                 since sub-squares of one colour never touch
+#   block_each    block sync only (its notebook's setting at 2048^2 and above):
+#                 blocks drift apart within an MCS, racy
+#   none          no sync inside an MCS (its notebook's final run), racy
+# Racy modes launch once per MCS (inner_iterations = 1, as the notebook
+# does), so that blocks meet at every MCS boundary.
+REF_MODES = (
+    ("grid_each", dict(global_sync=1, block_sync=0), False, False),
+    ("grid_region", dict(global_sync=1, block_sync=0), True, False),
+    ("block_each", dict(global_sync=0, block_sync=1), False, True),
+    ("block_region", dict(global_sync=0, block_sync=1), True, True),
+    ("none", dict(global_sync=0, block_sync=0), False, True),
+)
+
+
+def reference_gpu_baseline(w, timed_mcs=100, probe_mcs=10, top=6):
     """The reference's own CUDA sweep (oracle/_ref, its src/kernels.cu built
-    for sm_103a) on the same lattice and GPU, at its best launch geometry.
+    for sm_103a) on the same lattice and GPU, at its best launch geometry and
+    synchronisation mode.
 
     Geometry: every threads_per_block / positions_per_thread /
     positions_per_checkerboard / shared combination the reference accepts
     for this side (D divisible by tpb * ppt, ppc dividing ppt, grid
-    co-resident for its cooperative launch), with one attempt per grid sync
-    as in its examples (updates_per_barrier = 1, global_sync = 1) and the
-    partial_dispatch kernel variant.  J and T are rounded to integers as the
-    reference stores them.  Returns None when the reference build is absent.
+    co-resident for its cooperative launch), first with one attempt per grid
+    sync as in its examples; the `top` fastest geometries are then timed in
+    every other mode of REF_MODES.  The partial_dispatch kernel variant; J
+    and T rounded to integers as the reference stores them.  Reports the best
+    race-free mode and the best of all modes (racy ones marked).  Returns
+    None when the reference build is absent.
 
     3D runs the non-shared variant only: the shared one asks for 128 KB of
     dynamic shared memory without the opt-in above 48 KB and cannot launch
@@ -267,8 +297,22 @@ def reference_gpu_baseline(w, timed_mcs=100, probe_mcs=10):
     r.apply(w)
     if w.ndim == 3:
         timed_mcs, probe_mcs = max(1, timed_mcs // 2), max(1, probe_mcs // 2)
-    best = None
-    tried = []
+
+    def knobs(mode, geo):
+        name, sync, region, racy = mode
+        ppc = geo["positions_per_checkerboard"]
+        per = ppc ** w.ndim if region else 1
+        return dict(geo, updates_per_barrier=per, updates_per_checkerboard_switch=per, **sync)
+
+    def timed(mode, geo, mcs, seed):
+        k = knobs(mode, geo)
+        r.push(w.lattice)
+        t0 = time.perf_counter()
+        r.run(mcs, seed=seed, inner_iterations=1 if mode[3] else mcs, **k)  # an error ends the leg
+        r.synchronize()
+        return time.perf_counter() - t0
+
+    geos = []
     for shared in ((0, 1) if w.ndim == 2 else (0,)):
         for tpb in ((4, 8, 16, 32) if w.ndim == 2 else (4, 8)):
             cap = r.max_coop_blocks(tpb, shared)
@@ -289,33 +333,49 @@ def reference_gpu_baseline(w, timed_mcs=100, probe_mcs=10):
                     # tiles are valid.
                     if shared and tpb * 2 * ppc != 64:
                         continue
-                    geo = dict(threads_per_block=tpb, positions_per_thread=ppt,
-                               positions_per_checkerboard=ppc, shared=shared)
-                    r.push(w.lattice)
-                    t0 = time.perf_counter()
-                    r.run(probe_mcs, seed=7, **geo)   # an error ends the leg
-                    r.synchronize()
-                    dt = time.perf_counter() - t0
-                    tried.append((dt, geo))
-                    if best is None or dt < best[0]:
-                        best = (dt, geo)
-    if best is None:
+                    geos.append(dict(threads_per_block=tpb, positions_per_thread=ppt,
+                                     positions_per_checkerboard=ppc, shared=shared))
+    if not geos:
         return None
-    geo = best[1]
-    r.push(w.lattice)
-    r.run(probe_mcs, seed=11, **geo)  # warm-up
-    r.synchronize()
-    t0 = time.perf_counter()
-    r.run(timed_mcs, seed=13, **geo)
-    r.synchronize()
-    dt = time.perf_counter() - t0
-    return {"value": w.nsites * timed_mcs / dt, "unit": UNIT, "mcs_per_s": timed_mcs / dt,
-            "mcs": timed_mcs, "geometry": geo, "geometries_tried": len(tried),
+    probes = sorted((timed(REF_MODES[0], g, probe_mcs, 7), i) for i, g in enumerate(geos))
+    tried = [(dt, REF_MODES[0], geos[i]) for dt, i in probes]
+    for mode in REF_MODES[1:]:
+        for _, i in probes[:top]:
+            g = geos[i]
+            if g["shared"] and mode[0] != "grid_each":
+                continue  # the shared branch is only validated with a grid sync per attempt
+            tried.append((timed(mode, g, probe_mcs, 7), mode, g))
+
+    def final(entry):
+        _, mode, geo = entry
+        timed(mode, geo, probe_mcs, 11)  # warm-up
+        dt = timed(mode, geo, timed_mcs, 13)
+        return {"value": w.nsites * timed_mcs / dt, "unit": UNIT, "mcs_per_s": timed_mcs / dt,
+                "mcs": timed_mcs, "mode": mode[0], "racy": mode[3],
+                "run_knobs": knobs(mode, geo)}
+
+    best_free = final(min((t for t in tried if not t[1][3]), key=lambda t: t[0]))
+    best_any_entry = min(tried, key=lambda t: t[0])
+    best_any = best_free if not best_any_entry[1][3] else final(best_any_entry)
+    if best_any["value"] < best_free["value"]:
+        best_any = best_free
+    per_mode = {}
+    for dt, mode, geo in tried:
+        rate = w.nsites * probe_mcs / dt
+        if mode[0] not in per_mode or rate > per_mode[mode[0]]["probe_value"]:
+            per_mode[mode[0]] = {"probe_value": rate, "run_knobs": knobs(mode, geo),
+                                 "racy": mode[3]}
+    return {"value": best_any["value"], "unit": UNIT, "mcs_per_s": best_any["mcs_per_s"],
+            "mcs": timed_mcs, "mode": best_any["mode"], "racy": best_any["racy"],
+            "run_knobs": best_any["run_knobs"],
+            "best_race_free": best_free, "per_mode_probe": per_mode,
+            "geometries_tried": len(geos), "probes": len(tried),
             "build": "reference src/kernels.cu, its nvcc flags, sm_103a (oracle/ref_gpu)",
             "timing": "host wall clock around run + synchronize (the reference's own "
                       "workflow), default stream",
-            "notes": "partial_dispatch variant, updates_per_barrier=1, global_sync=1, "
-                     "J and T rounded to integers"}
+            "notes": "partial_dispatch variant, J and T rounded to integers; value is the "
+                     "best of all modes (racy modes included), best_race_free the best "
+                     "mode with a grid sync"}
 
 
 def run_reference(args, world, rank):
@@ -325,6 +385,12 @@ def run_reference(args, world, rank):
     w = build_workload(args.workload)
     threads = os.cpu_count() or 1
     sim = oracle.OracleSim(w.lattice, w.ncells, **w.oracle_kwargs(), seed=0)
+    # The GPU arm times a relaxed tissue (after its warm-up runs); relax this
+    # one too, within a bounded time, so that both time comparable states.
+    relax, t_relax = 0, time.perf_counter()
+    while relax < REFERENCE_RELAX_MCS and time.perf_counter() - t_relax < 20.0:
+        sim.run(5, nthreads=threads)
+        relax += 5
     for _ in range(args.warmup):
         sim.run(1, nthreads=threads)
     t0 = time.perf_counter()
@@ -340,7 +406,8 @@ def run_reference(args, world, rank):
             "scaling": "weak", "vs_baseline": None, "dtype": "u32+f32",
             "data": data_of(w), "config": cfg,
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"1 MCS of the {w.name} lattice per step, "
+                             "sample": f"1 MCS of the {w.name} lattice per step, after "
+                                       f"{relax} MCS of relaxation from the seeded state, "
                                        f"{threads} OpenMP threads; the reference has no "
                                        "CPU implementation, so this is the oracle port"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
@@ -397,7 +464,7 @@ def warm_gpu(seconds=0.3):
         torch.cuda.synchronize()
 
 
-def run_ours(args, world, rank, local):
+def run_ours(args, world, rank, local, emit=True):
     import numpy as np
     import torch
 
@@ -482,7 +549,7 @@ def run_ours(args, world, rank, local):
                "steps": e2e_steps, "path": "Cpm.push_to_gpu + run + synchronize + pull_from_gpu"}
 
     if rank != 0:
-        return
+        return None
     peak, peak_kind = measured_peak_hbm()
     per_launch_s = dev_s / args.steps
     attempts_per_launch = w.nsites * mcs
@@ -517,11 +584,15 @@ def run_ours(args, world, rank, local):
         if ref is not None:
             if "value" in ref:
                 ref["speedup_of_value"] = value / world / ref["value"]
+                ref["best_race_free"]["speedup_of_value"] = (
+                    value / world / ref["best_race_free"]["value"])
             line["reference_gpu"] = ref
-    print(json.dumps(line), flush=True)
+    if emit:
+        print(json.dumps(line), flush=True)
+    return line
 
 
-def run_ensemble(args, world, rank, local):
+def run_ensemble(args, world, rank, local, emit=True):
     """Batches: all replicas in one graph-captured persistent launch
     (batched) against the same replicas as a per-replica launch loop.
 
@@ -579,6 +650,9 @@ def run_ensemble(args, world, rank, local):
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     launches0 = b.kernel_launches()
+    sampler = ClockSampler(gpu_index_for(torch, local)) if rank == 0 else None
+    if sampler:
+        sampler.start()
     dist_barrier(world)
     torch.cuda.synchronize()
     with torch.cuda.stream(stream):
@@ -588,6 +662,7 @@ def run_ensemble(args, world, rank, local):
             ends[i].record(stream)
     b.synchronize()
     torch.cuda.synchronize()
+    clocks = sampler.stop() if sampler else None
     dist_barrier(world)
     launches = b.kernel_launches() - launches0
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
@@ -626,9 +701,10 @@ def run_ensemble(args, world, rank, local):
             e.synchronize()
         torch.cuda.synchronize()
         loop_ms = dist_max(world, t0.elapsed_time(t1) / 1e3) * 1e3
+        del engines
 
     if rank != 0:
-        return
+        return None
     peak, peak_kind = measured_peak_hbm()
     achieved = BYTES_PER_ATTEMPT * sites * mcs / (batched_ms / 1e3) / 1e9
     side = [s[0] for s in sizes]
@@ -658,11 +734,13 @@ def run_ensemble(args, world, rank, local):
                         "autotuned tile, launched back to back on one stream"},
             "autotune": {"variant": variant, "probe_ms_per_mcs": tuned_ms,
                          "dispatch": b.sweep_config()["dispatch"]},
-            "step_ms": step_ms, "e2e": None}
-    print(json.dumps(line), flush=True)
+            "step_ms": step_ms, "clocks": clocks, "e2e": None}
+    if emit:
+        print(json.dumps(line), flush=True)
+    return line
 
 
-def run_gradient(args, world, rank, local):
+def run_gradient(args, world, rank, local, emit=True):
     """Differentiated ensemble of two-type sorting lattices, observable O =
     heterotypic fraction at the last MCS, theta = (J_ll, J_dd, J_ld, J_lm,
     J_dm, lambda_area, T).
@@ -696,7 +774,14 @@ def run_gradient(args, world, rank, local):
     nrep = args.replicas or (131072 if check else 512)
     mcs = args.mcs or (10 if check else 500)
     w = W.sorting_grid(n=side, ncells=ncells, seed=0)
-    ens = G.Ensemble([w] * nrep, seed=0, stream_id=rank * nrep)
+    # N > 1: the ranks shard one ensemble of N * nrep replicas; the baseline
+    # and the gradient are the global ones (one all-reduce of observable
+    # totals before the backward kernel, one of the gradient after it)
+    group = None
+    if world > 1:
+        import torch.distributed as dist
+        group = dist.group.WORLD
+    ens = G.Ensemble([w] * nrep, seed=0, stream_id=rank * nrep, group=group)
     theta0 = ens.theta0()
     names = ["J_ll", "J_dd", "J_ld", "J_lm", "J_dm", "lambda_area", "T"]
 
@@ -734,6 +819,26 @@ def run_gradient(args, world, rank, local):
     fwd_s = dist_max(world, statistics.median(t_fwd))
     lr_s = dist_max(world, statistics.median(t_lr))
 
+    if args.no_fd:
+        if rank != 0:
+            return None
+        line = {"metric": METRIC, "value": nrep * w.nsites * mcs * world / lr_s, "unit": UNIT,
+                "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": lr_s * 1e3, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "u32+f32",
+                "data": "synthetic (seeded sorting grid)",
+                "config": {"workload": f"{args.workload}: {nrep} replicas of sorting_grid "
+                                       f"{side}x{side}, {ncells} cells of target area 25, "
+                                       f"O = heterotypic fraction at MCS {mcs}",
+                           "sites": nrep * w.nsites, "mcs_per_step": mcs, "seed": 0},
+                "gradient": {"forward_ms": fwd_s * 1e3,
+                             "forward_scores_backward_ms": lr_s * 1e3,
+                             "cost_ratio": lr_s / fwd_s},
+                "gpu_launches": int(launches), "clocks": clocks, "e2e": None}
+        if emit:
+            print(json.dumps(line), flush=True)
+        return line
+
     # standard error of the LR estimate from its per-replica terms
     O, sc, _ = ens.forward(theta0, mcs, [mcs], scores=True)
     o = O[:, 0].double().cpu().numpy()
@@ -748,7 +853,7 @@ def run_gradient(args, world, rank, local):
     lr = g.double().cpu().numpy()
 
     if rank != 0:
-        return
+        return None
     sites = nrep * w.nsites
     rel = np.abs(lr - fd) / np.maximum(np.abs(fd), 1e-30)
     z = (lr - fd) / np.sqrt(lr_se ** 2 + fd_se ** 2)
@@ -778,7 +883,56 @@ def run_gradient(args, world, rank, local):
             "timing": "wall clock of whole forward / differentiated steps (median), "
                       "each including restart (H2D of the initial lattices) and observation",
             "gpu_launches": int(launches), "clocks": clocks, "e2e": None}
-    print(json.dumps(line), flush=True)
+    if emit:
+        print(json.dumps(line), flush=True)
+    return line
+
+
+def secondary(args, world, rank, local):
+    """Compact results of the other benchmark configurations, measured in the
+    same process after the headline: the 256^3 tissue (attempts/s, with the
+    reference's CUDA build on it), the 256-replica ragged ensemble (one
+    graph-captured launch against a per-replica launch loop) and the
+    512 x 256^2 gradient ensemble (forward + scores + backward against the
+    forward alone).  Each carries its own clock record."""
+    import copy
+
+    def sub(**kw):
+        a = copy.copy(args)
+        a.no_e2e, a.no_cpu_baseline, a.no_reference_gpu = True, True, True
+        a.variant = a.dispatch = a.mcs = a.replicas = None
+        a.no_loop, a.no_fd, a.no_secondary = False, True, True
+        for k, v in kw.items():
+            setattr(a, k, v)
+        return a
+
+    out = {}
+    line = run_ours(sub(workload="tissue_3d", steps=3, warmup=2, no_reference_gpu=False),
+                    world, rank, local, emit=False)
+    if line is not None:
+        ref = line.get("reference_gpu") or {}
+        out["tissue_3d_256"] = {
+            "value": line["value"], "unit": UNIT, "ms_per_step": line["ms_per_step"],
+            "mcs_per_step": line["config"]["mcs_per_step"],
+            "roofline_frac": line["roofline"]["frac"], "tile": line["config"]["tile"],
+            "clocks": line["clocks"],
+            "reference_gpu": {k: ref.get(k) for k in ("value", "mode", "racy", "run_knobs",
+                                                      "speedup_of_value")}
+            if "value" in ref else ref or None}
+    line = run_ensemble(sub(workload="ensemble", steps=2, warmup=2), world, rank, local,
+                        emit=False)
+    if line is not None:
+        out["ensemble_256"] = {"value": line["value"], "unit": UNIT,
+                               "sites": line["config"]["sites"], "mcs_per_step": 500,
+                               "dispatch": line["config"]["dispatch"],
+                               "batched_vs_loop": line["batched_vs_loop"],
+                               "clocks": line["clocks"]}
+    line = run_gradient(sub(workload="gradient", steps=2, warmup=1), world, rank, local,
+                        emit=False)
+    if line is not None:
+        out["gradient_512x256"] = dict(line["gradient"], clocks=line["clocks"],
+                                       workload=line["config"]["workload"])
+    return out
 
 
 def main():
@@ -791,7 +945,13 @@ def main():
     elif args.workload in ("gradient", "gradient_check"):
         run_gradient(args, world, rank, local)
     else:
-        run_ours(args, world, rank, local)
+        secondary_keys = args.workload == "tissue_2d" and not args.no_secondary
+        line = run_ours(args, world, rank, local, emit=not secondary_keys)
+        if secondary_keys:
+            extra = secondary(args, world, rank, local)
+            if line is not None:
+                line["secondary"] = extra
+                print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

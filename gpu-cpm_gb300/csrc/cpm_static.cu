@@ -14,11 +14,14 @@
 //
 // The array is a file-scope __device__ variable: its address on a device is
 // looked up with cudaGetSymbolAddress the first time the entry point runs
-// on that device (with that device current) and cached.  Its contents
-// persist between calls, so every call first clears the parts the sweep
-// requires to start at zero.  All calls share it, so calls must not overlap
-// on the GPU.
+// on that device (with that device current) and cached for the life of the
+// process.  cudaDeviceReset destroys the context that holds the array, so
+// the cached address is stale afterwards: a process that resets a device
+// must not call this entry point on it again.  The array's contents persist
+// between calls, so every call first clears the parts the sweep requires to
+// start at zero.  All calls share it, so calls must not overlap on the GPU.
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -154,6 +157,16 @@ extern "C" int cpm_sweep_static(int dimensionality, int nx, int ny, int nz,
         params->persistence_lambda[k] != 0.0f)
       return fail(CPM_ERR_UNSUPPORTED,
                   "cpm_sweep_static: chemotaxis, act and persistence need a handle engine");
+  // Non-finite energies would make every Metropolis decision meaningless;
+  // refused as the handle setters refuse them.
+  if (!std::isfinite(params->temperature))
+    return fail(CPM_ERR_INVALID, "cpm_sweep_static: temperature must be finite");
+  for (int k = 0; k < kMaxTypes; ++k)
+    if (!std::isfinite(params->lambda_area[k]) || !std::isfinite(params->lambda_perimeter[k]))
+      return fail(CPM_ERR_INVALID, "cpm_sweep_static: lambdas must be finite");
+  for (int k = 0; k < kMaxTypes * kMaxTypes; ++k)
+    if (!std::isfinite(params->J[k]) || !std::isfinite(params->stickiness[k]))
+      return fail(CPM_ERR_INVALID, "cpm_sweep_static: adhesion and stickiness must be finite");
   const long long rows = (long long)number_of_cells + 1;
   cudaStream_t s = (cudaStream_t)stream;
 
@@ -190,8 +203,18 @@ extern "C" int cpm_sweep_static(int dimensionality, int nx, int ny, int nz,
   if (per_sm < 1) return fail(CPM_ERR_CUDA, "cpm_sweep_static: cannot place the sweep kernel");
   const long long blocks_needed = (max_tiles + sh.warps - 1) / sh.warps;
   const int grid = (int)std::max(1LL, std::min<long long>((long long)per_sm * sms, blocks_needed));
-  const long long warps = (long long)grid * sh.warps;
-  const long long list_cap = 2LL * tcx * tcy * tcz * sh.warps * ((max_tiles + warps - 1) / warps);
+  // Dirty-list space of one block and phase: two table rows per target of
+  // the tiles it sweeps.  The single-lattice sweep gives each block one
+  // contiguous band of at most ceil(tiles / grid) tiles, and a tile holds at
+  // most min(tile extent, class size) targets along each axis, so narrow
+  // lattices (nx far below the tile width) do not pay for empty tile columns.
+  // Over every shape within CPM_STATIC_MAX_SITES the lists of a launch then
+  // need at most 516,096 entries (2D, 66 x 3890) and 337,920 (3D,
+  // 66 x 642 x 6) on 152 SMs, within kListEntries.
+  const long long eff_tile = (long long)std::min(tcx, std::max(1, class_count_host(nx, 0))) *
+                             std::min(tcy, std::max(1, class_count_host(ny, 0))) *
+                             std::min(tcz, std::max(1, class_count_host(nz, 0)));
+  const long long list_cap = 2LL * eff_tile * ((max_tiles + grid - 1) / grid);
   if (list_cap * 2 * grid > kListEntries)
     return fail(CPM_ERR_INVALID,
                 "cpm_sweep_static: lattice shape needs more dirty-list space than the "

@@ -495,12 +495,17 @@ struct cpm_static_params {
  * held on every GPU that loads the library until the process exits), which
  * bounds the sizes: nx*ny*nz <= CPM_STATIC_MAX_SITES and number_of_cells <=
  * CPM_STATIC_MAX_CELLS; larger requests fail with CPM_ERR_INVALID before any
- * GPU work.  The first call on a device looks the array's address up on
- * that device (make that call before capturing a CUDA graph on it).  Every
+ * GPU work.  Every shape within those limits fits the array's dirty-list
+ * space, narrow ones (nx far below 64) included.  A non-finite temperature,
+ * lambda, adhesion or stickiness fails with CPM_ERR_INVALID.  The first call
+ * on a device looks the array's address up on that device (make that call
+ * before capturing a CUDA graph on it) and keeps it for the life of the
+ * process; after cudaDeviceReset on that device the kept address is stale,
+ * so do not call this entry point on a device the process has reset.  Every
  * call shares the one array: calls must not overlap on the GPU (two host
  * threads calling at once on different streams would race).  The call works
- * on `stream` (NULL: the default stream) and returns after that work has
- * finished, with the status of the sweep; counters_out, if not NULL,
+ * on `stream` (NULL: the default stream) and waits for that stream before it
+ * returns, with the status of the sweep; counters_out, if not NULL,
  * receives {evaluated, accepted} of this call. */
 int cpm_sweep_static(int dimensionality, int nx, int ny, int nz,
                      int number_of_cells, uint32_t* lattice, int32_t* area,

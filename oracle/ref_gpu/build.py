@@ -1,8 +1,9 @@
 """Build recipe of the reference's own CUDA sweep (test infrastructure only).
 
-* cubin: compiled from the reference sources where they lie
-  (/root/reference/src/kernels.cu, which includes kernels2d.cu,
-  kernels3d.cu and random.cu) with the reference's nvcc flags from its
+* cubin: compiled from the reference sources where they lie (the reference
+  checkout's src/kernels.cu, which includes kernels2d.cu, kernels3d.cu and
+  random.cu; the directory is --ref-src, else $GPUCPM_REFERENCE_SRC, else
+  the checkout at /root/reference/src) with the reference's nvcc flags from its
   setup.py:79-86 (-std=c++17 -use_fast_math -maxrregcount=40), the target
   changed from compute_70/sm_70 (which nvcc 13 rejects) to sm_103a, and
   without -rdc (cooperative grid sync needs no device linking here).  Built
@@ -19,14 +20,23 @@ import subprocess
 
 HERE = pathlib.Path(__file__).resolve().parent
 OUT = HERE.parent / "_ref"
-REF_SRC = pathlib.Path("/root/reference/src")
+DEFAULT_REF_SRC = "/root/reference/src"
+
+
+def ref_src(path=None):
+    """Directory of the reference's CUDA sources: `path`, else the
+    GPUCPM_REFERENCE_SRC environment variable, else the default checkout."""
+    return pathlib.Path(path or os.environ.get("GPUCPM_REFERENCE_SRC") or DEFAULT_REF_SRC)
+
+
 CUBIN = OUT / "gpucpm_ref_sm103a.cubin"
 DRIVER = OUT / "libref_driver.so"
 CUDA = pathlib.Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 
 
-def build_cubin(force=False):
+def build_cubin(force=False, src_dir=None):
     """Compile the reference kernels if the checkout is present."""
+    REF_SRC = ref_src(src_dir)
     src = REF_SRC / "kernels.cu"
     if not src.exists():
         return CUBIN if CUBIN.exists() else None
@@ -59,11 +69,15 @@ def build_driver(force=False):
     return DRIVER
 
 
-def build(force=False):
-    cubin = build_cubin(force)
+def build(force=False, src_dir=None):
+    cubin = build_cubin(force, src_dir)
     driver = build_driver(force)
     return cubin, driver
 
 
 if __name__ == "__main__":
-    print(build(force=True))
+    import argparse
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--ref-src", default=None,
+                    help="directory of the reference's src/ (kernels.cu and its includes)")
+    print(build(force=True, src_dir=ap.parse_args().ref_src))

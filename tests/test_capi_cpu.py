@@ -68,6 +68,20 @@ def test_static_sweep_refuses_handle_only_terms_before_touching_cuda(engine_lib)
     p = StaticParams()
     assert f(2, 2, 8, 1, 4, ptr, ptr, ptr, ptr, 0, ctypes.byref(p), 0, 0, 0, 1, None,
              None) == 1  # a side below 3
+    # non-finite energies are refused as the handle setters refuse them
+    for field, idx in (("temperature", None), ("lambda_area", 1), ("lambda_perimeter", 2),
+                       ("J", 5), ("stickiness", 7)):
+        for bad in (float("nan"), float("inf")):
+            p = StaticParams()
+            p.temperature = 5.0
+            if idx is None:
+                p.temperature = bad
+            else:
+                getattr(p, field)[idx] = bad
+            rc = f(2, 8, 8, 1, 4, ptr, ptr, ptr, ptr, 0, ctypes.byref(p), 0, 0, 0, 1, None,
+                   None)
+            assert rc == 1, (field, bad)  # CPM_ERR_INVALID
+            assert b"finite" in engine_lib.cpm_last_error(None)
 
 
 def test_c_example_compiles_and_links(engine_lib, tmp_path):
