@@ -67,6 +67,9 @@ def parse_args():
     p.add_argument("--variant", type=int, default=None,
                    help="tile variant instead of the autotuner's choice (profiling runs: "
                         "timing under a profiler can change the tuner's pick)")
+    p.add_argument("--fill", choices=["parity", "vector", "tma"], default=None,
+                   help="single 2D lattices: how tiles are staged instead of the engine's "
+                        "default (see cpm_set_fill)")
     p.add_argument("--dispatch", choices=["grid", "replica", "hybrid"], default=None,
                    help="batches: dispatch instead of the autotuner's choice")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -77,6 +80,9 @@ def parse_args():
                         "the ragged ensemble and the gradient ensemble")
     p.add_argument("--no-fd", action="store_true",
                    help="gradient workloads: time only (no finite-difference comparison)")
+    p.add_argument("--fd-params", default=None,
+                   help="gradient workloads: comma-separated parameters to difference "
+                        "(default: all of J_ll,J_dd,J_ld,J_lm,J_dm,lambda_area,T)")
     return p.parse_args()
 
 
@@ -484,6 +490,9 @@ def run_ours(args, world, rank, local, emit=True):
     sim.push_to_gpu()
     if args.variant is not None:
         sim.set_variant(args.variant)
+    if getattr(args, "fill", None):
+        sim.set_fill({"parity": gpucpm.FILL_PARITY, "vector": gpucpm.FILL_VECTOR,
+                      "tma": gpucpm.FILL_TMA}[args.fill])
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
 
     for _ in range(args.warmup):
@@ -564,7 +573,8 @@ def run_ours(args, world, rank, local, emit=True):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "u32+f32", "data": data_of(w),
-            "config": dict(describe(w, mcs), tile=sim.sweep_config()["tile"]),
+            "config": dict(describe(w, mcs), tile=sim.sweep_config()["tile"],
+                           fill=sim.sweep_config()["fill"]),
             "roofline": roofline,
             "issue_roofline": issue_roofline(args.workload, value / world, clocks, torch,
                                              local),
@@ -847,7 +857,11 @@ def run_gradient(args, world, rank, local, emit=True):
     terms = (o - b)[:, None] * cum
     lr_np = terms.mean(axis=0)
     lr_se = terms.std(axis=0, ddof=1) / np.sqrt(nrep)
-    fd, fd_per = G.crn_finite_difference(ens, theta0, mcs, rel_step=0.01, per_replica=True)
+    fd_params = None
+    if args.fd_params:
+        fd_params = [names.index(n) for n in args.fd_params.split(",")]
+    fd, fd_per = G.crn_finite_difference(ens, theta0, mcs, rel_step=0.01, per_replica=True,
+                                         params=fd_params)
     fd = fd.numpy()
     fd_se = fd_per.numpy().std(axis=0, ddof=1) / np.sqrt(nrep)
     lr = g.double().cpu().numpy()
@@ -876,7 +890,7 @@ def run_gradient(args, world, rank, local, emit=True):
                                                                  atol=1e-3 * np.abs(lr).max())),
                          "fd_step": "central, +-1% of each parameter, common random numbers",
                          "params": per_param,
-                         "max_rel_diff": float(rel.max()),
+                         "max_rel_diff": float(np.nanmax(rel)),
                          "within_5pct": [n for k, n in enumerate(names) if rel[k] <= 0.05],
                          "resolvable": [n for k, n in enumerate(names)
                                         if abs(fd[k]) > 20 * np.hypot(lr_se[k], fd_se[k])]},
@@ -890,8 +904,9 @@ def run_gradient(args, world, rank, local, emit=True):
 
 def secondary(args, world, rank, local):
     """Compact results of the other benchmark configurations, measured in the
-    same process after the headline: the 256^3 tissue (attempts/s, with the
-    reference's CUDA build on it), the 256-replica ragged ensemble (one
+    same process after the headline: the 256^3 tissue and the 256^2 sorting
+    recipe (attempts/s, each with the reference's CUDA build on it), the
+    256-replica ragged ensemble (one
     graph-captured launch against a per-replica launch loop) and the
     512 x 256^2 gradient ensemble (forward + scores + backward against the
     forward alone).  Each carries its own clock record."""
@@ -900,7 +915,7 @@ def secondary(args, world, rank, local):
     def sub(**kw):
         a = copy.copy(args)
         a.no_e2e, a.no_cpu_baseline, a.no_reference_gpu = True, True, True
-        a.variant = a.dispatch = a.mcs = a.replicas = None
+        a.variant = a.dispatch = a.mcs = a.replicas = a.fill = None
         a.no_loop, a.no_fd, a.no_secondary = False, True, True
         for k, v in kw.items():
             setattr(a, k, v)
@@ -918,7 +933,26 @@ def secondary(args, world, rank, local):
             "clocks": line["clocks"],
             "reference_gpu": {k: ref.get(k) for k in ("value", "mode", "racy", "run_knobs",
                                                       "speedup_of_value")}
-            if "value" in ref else ref or None}
+            if "value" in ref else ref or None,
+            "reference_gpu_race_free": {k: (ref.get("best_race_free") or {}).get(k)
+                                        for k in ("value", "mode", "run_knobs",
+                                                  "speedup_of_value")}
+            if "value" in ref else None}
+    line = run_ours(sub(workload="sorting_2d_256", steps=3, warmup=3, no_reference_gpu=False),
+                    world, rank, local, emit=False)
+    if line is not None:
+        ref = line.get("reference_gpu") or {}
+        out["sorting_256"] = {
+            "value": line["value"], "unit": UNIT, "ms_per_step": line["ms_per_step"],
+            "mcs_per_step": line["config"]["mcs_per_step"], "tile": line["config"]["tile"],
+            "fill": line["config"]["fill"], "clocks": line["clocks"],
+            "reference_gpu": {k: ref.get(k) for k in ("value", "mode", "racy", "run_knobs",
+                                                      "speedup_of_value")}
+            if "value" in ref else ref or None,
+            "reference_gpu_race_free": {k: (ref.get("best_race_free") or {}).get(k)
+                                        for k in ("value", "mode", "run_knobs",
+                                                  "speedup_of_value")}
+            if "value" in ref else None}
     line = run_ensemble(sub(workload="ensemble", steps=2, warmup=2), world, rank, local,
                         emit=False)
     if line is not None:

@@ -14,11 +14,15 @@
 //     __constant__ struct in every setter, src/kernels.cu:50-53);
 //   * every call returns a status and keeps a message (the reference prints
 //     CUDA errors and carries on, src/cpm.cu:52-56).
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -111,6 +115,16 @@ struct cpm_handle {
   } cfg[kTileVariants];
   int variant = 0;
   int dispatch = CPM_DISPATCH_GRID;  // CPM_DISPATCH_*
+  // 2D single lattices whose width is a multiple of 4 run the row-tile sweep
+  // (cpm_sweep2d.cu).  fill: CPM_FILL_PARITY = the parity-split sweep_kernel,
+  // CPM_FILL_VECTOR = row tiles staged with 16-byte loads, CPM_FILL_TMA = row
+  // tiles whose interior tiles are copied by the tensor-map engine (the
+  // default where the maps could be encoded).
+  int fill = CPM_FILL_PARITY;
+  bool row_ok = false, tma_ok = false;
+  struct alignas(64) TileMap {
+    unsigned char bytes[128];  // CUtensorMap of the lattice, box of one variant
+  } tmap[kTileVariants];
   std::vector<unsigned long long> attempts;  // per replica, host-counted
 
   // Graph-captured run (cpm_run_graph): the captured launch reads and
@@ -118,7 +132,7 @@ struct cpm_handle {
   unsigned long long* d_tick = nullptr;
   bool d_tick_stale = true;
   cudaGraphExec_t graph_exec = nullptr;
-  int graph_mcs = 0, graph_variant = -1, graph_dispatch = -1;
+  int graph_mcs = 0, graph_variant = -1, graph_dispatch = -1, graph_fill = -1;
   int graph_launches = 1;  // sweep kernels per replay (2 for hybrid)
   cudaStream_t graph_stream = nullptr;
 
@@ -195,6 +209,39 @@ void free_all(cpm_handle* h) {
   cudaFree(h->d_tick);
   if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
+}
+
+// Tensor maps of a single 2D lattice for the row-tile sweep: the lattice as a
+// ny x nx array of 32-bit words, one box of 72 x (2 CY + 1) words per tile
+// variant.  cuTensorMapEncodeTiled is reached through the runtime's driver
+// entry point, so the library does not link the driver library itself.
+// False (and no maps) when the entry point or the encoding is unavailable.
+bool encode_tile_maps(cpm_handle* h) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                         cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  });
+  if (!encode) return false;
+  const DevReplica& R = h->reps[0];
+  for (int v = 0; v < kTileVariants; ++v) {
+    const cuuint64_t dims[2] = {(cuuint64_t)R.nx, (cuuint64_t)R.ny};
+    const cuuint64_t strides[1] = {(cuuint64_t)R.nx * 4};
+    const cuuint32_t box[2] = {72u, (cuuint32_t)row_tile_rows(v)};
+    const cuuint32_t estr[2] = {1u, 1u};
+    if (encode(reinterpret_cast<CUtensorMap*>(h->tmap[v].bytes), CU_TENSOR_MAP_DATA_TYPE_UINT32,
+               2, h->d_lat + R.lat_off, dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return false;
+  }
+  return true;
 }
 
 void default_params(DevParams& p, float T) {
@@ -305,6 +352,11 @@ int build_engine(int n, int ndim, const int* nx, const int* ny, const int* nz,
     return e == cudaErrorMemoryAllocation ? CPM_ERR_ALLOC : CPM_ERR_CUDA;
   }
   std::memset(h->h_lat, 0, sizeof(uint32_t) * sites);
+  if (n == 1 && ndim == 2 && row_tiles_fit(nx[0], ny[0])) {
+    h->row_ok = true;
+    h->tma_ok = encode_tile_maps(h);
+    h->fill = h->tma_ok ? CPM_FILL_TMA : CPM_FILL_VECTOR;
+  }
 
   // One launch configuration per tile variant: warp tiles per slot and
   // replica (prefix over replicas), grid, dirty-list capacity.
@@ -744,7 +796,14 @@ cudaError_t enqueue_sweep(const cpm_handle* h, int v, int d, const SweepArgs& a,
   *nlaunch = 0;
   auto one = [&](const SweepArgs& x, int grid) {
     cudaError_t e = cudaMemsetAsync(h->d_ctl, 0, sizeof(uint32_t) * kCtlErr, h->stream);
-    if (e == cudaSuccess) e = launch_sweep(h->ndim, perim, v, x, grid, h->stream, scores);
+    const bool row = h->fill != CPM_FILL_PARITY && h->row_ok && !scores && !h->act_active &&
+                     !h->persist_active && x.nrep == 1 && x.rep_map == nullptr &&
+                     !x.block_local;
+    if (e == cudaSuccess && row)
+      e = launch_sweep2d(perim, v, x, h->tmap[v].bytes, h->fill == CPM_FILL_TMA ? 1 : 0, grid,
+                         c.shape.warps, h->stream);
+    else if (e == cudaSuccess)
+      e = launch_sweep(h->ndim, perim, v, x, grid, h->stream, scores);
     if (e == cudaSuccess) ++*nlaunch;
     return e;
   };
@@ -1287,7 +1346,8 @@ int cpm_run_graph(cpm_handle* h, int mcs) {
     return h->fail(CPM_ERR_STATE, "graph runs need a non-default stream");
   if (int rc = upload_params(h)) return rc;
   if (!h->graph_exec || h->graph_mcs != mcs || h->graph_variant != h->variant ||
-      h->graph_dispatch != h->dispatch || h->graph_stream != h->stream) {
+      h->graph_dispatch != h->dispatch || h->graph_fill != h->fill ||
+      h->graph_stream != h->stream) {
     if (h->graph_exec) {
       cudaGraphExecDestroy(h->graph_exec);
       h->graph_exec = nullptr;
@@ -1311,6 +1371,7 @@ int cpm_run_graph(cpm_handle* h, int mcs) {
     h->graph_launches = nl;
     h->graph_variant = h->variant;
     h->graph_dispatch = h->dispatch;
+    h->graph_fill = h->fill;
     h->graph_stream = h->stream;
   }
   if (h->d_tick_stale) {
@@ -1690,6 +1751,25 @@ int cpm_set_variant(cpm_handle* h, int variant) {
   if (variant < 0 || variant >= kTileVariants)
     return h->fail(CPM_ERR_INVALID, "tile variant %d out of range [0, %d)", variant, kTileVariants);
   h->variant = variant;
+  return CPM_OK;
+}
+
+int cpm_set_fill(cpm_handle* h, int fill) {
+  if (!h) return CPM_ERR_INVALID;
+  if (fill != CPM_FILL_PARITY && fill != CPM_FILL_VECTOR && fill != CPM_FILL_TMA)
+    return h->fail(CPM_ERR_INVALID, "fill %d is not parity (0), vector (1) or tma (2)", fill);
+  if (fill != CPM_FILL_PARITY && !h->row_ok)
+    return h->fail(CPM_ERR_UNSUPPORTED, "row tiles need one 2D lattice with nx a multiple of "
+                                        "4, nx >= 72 and ny >= 66");
+  if (fill == CPM_FILL_TMA && !h->tma_ok)
+    return h->fail(CPM_ERR_UNSUPPORTED, "the tensor maps of this lattice could not be encoded");
+  h->fill = fill;
+  return CPM_OK;
+}
+
+int cpm_get_fill(const cpm_handle* h, int* fill) {
+  if (!h || !fill) return CPM_ERR_INVALID;
+  *fill = h->fill;
   return CPM_OK;
 }
 

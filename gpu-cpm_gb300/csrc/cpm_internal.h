@@ -257,6 +257,14 @@ void set_thread_error(const char* message);
 // Launchers (cpm_kernels.cu).  Each returns the cudaError_t of its launch.
 cudaError_t launch_sweep(int ndim, bool perim, int variant, const SweepArgs& a,
                          int grid, cudaStream_t s, bool scores = false);
+// The row-tile sweep of one 2D lattice (cpm_sweep2d.cu): tmap points to the
+// 128-byte CUtensorMap of the variant's box (72 x row_tile_rows(variant)
+// words); use_tma = 0 stages every tile with vector loads.  At most
+// warps_cap warps per block.
+cudaError_t launch_sweep2d(bool perim, int variant, const SweepArgs& a, const void* tmap,
+                           int use_tma, int grid, int warps_cap, cudaStream_t s);
+bool row_tiles_fit(int nx, int ny);
+int row_tile_rows(int variant);
 int sweep_max_blocks_per_sm(int ndim, bool perim, int variant, bool scores = false);
 // checkpoints: host array of ncheck (<= kMaxCheckpoints) MCS counts.
 cudaError_t launch_lr_backward(const float* scores, const float* dl_do,

@@ -59,11 +59,11 @@
 #include <cstdint>
 
 #include "cpm_device.cuh"
+#include "cpm_sweep_common.cuh"
 
 namespace gpucpm {
 namespace {
 
-constexpr unsigned kFull = 0xffffffffu;
 
 __device__ __forceinline__ int find_task_replica(const int* pre, int nrep,
                                                  int task) {
@@ -93,11 +93,6 @@ __device__ __forceinline__ int find_site_replica(const DevReplica* reps,
   return lo;
 }
 
-__device__ __forceinline__ unsigned lanemask_lt() {
-  unsigned m;
-  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
-  return m;
-}
 
 // Shared-memory layout of a staged warp tile.  Logical column c of a staged
 // row lives at (c & 1) * HALF + (c >> 1): target columns (odd logical
@@ -162,79 +157,6 @@ SweepShape shape_of() {
   return s;
 }
 
-// Chemotaxis: unit copy direction (target minus source) dotted with the
-// field at the source site, every step rounded as written (the oracle
-// repeats it).  As in the reference, the direction is the raw difference of
-// the wrapped coordinates in 2D (src/kernels2d.cu:302-309) and the nearest
-// image in 3D (src/kernels3d.cu:275-299).  F: the replica's field, `sites`
-// values per component.
-__device__ __forceinline__ int wrap_coord(int v, int n) {
-  return v < 0 ? v + n : (v >= n ? v - n : v);
-}
-
-// Coordinates of the source of an attempt: neighbour `kdir` (the order of
-// Stage::nb_offset) of the target (x, y, z), wrapped.
-template <int NDIM>
-__device__ __forceinline__ void source_coords(int kdir, int x, int y, int z, int nx, int ny,
-                                              int nz, int& sx, int& sy, int& sz) {
-  int ox, oy, oz;
-  if (NDIM == 2) {
-    const int m = kdir + (kdir >= 4);
-    oz = 0;
-    oy = m / 3 - 1;
-    ox = m % 3 - 1;
-  } else {
-    const int m = kdir + (kdir >= 13);
-    oz = m / 9 - 1;
-    oy = (m / 3) % 3 - 1;
-    ox = m % 3 - 1;
-  }
-  sx = wrap_coord(x + ox, nx);
-  sy = wrap_coord(y + oy, ny);
-  sz = NDIM == 3 ? wrap_coord(z + oz, nz) : 0;
-}
-
-// Unit copy direction (target minus source) of neighbour kdir: the raw
-// difference of the wrapped coordinates in 2D (src/kernels2d.cu:302-309),
-// the nearest image in 3D (src/kernels3d.cu:275-299); FP32, rounded as
-// written (the oracle repeats it).  Also returns the source coordinates.
-template <int NDIM>
-__device__ __forceinline__ void unit_dir(int kdir, int x, int y, int z, int nx, int ny, int nz,
-                                         float& ux, float& uy, float& uz, int& sx, int& sy,
-                                         int& sz) {
-  source_coords<NDIM>(kdir, x, y, z, nx, ny, nz, sx, sy, sz);
-  int dx = x - sx, dy = y - sy, dz = z - sz;
-  if (NDIM == 3) {
-    if (dx > nx / 2) dx -= nx;
-    if (dx < -(nx / 2)) dx += nx;
-    if (dy > ny / 2) dy -= ny;
-    if (dy < -(ny / 2)) dy += ny;
-    if (dz > nz / 2) dz -= nz;
-    if (dz < -(nz / 2)) dz += nz;
-  }
-  const float fx = (float)dx, fy = (float)dy, fz = (float)dz;
-  float s2 = __fmul_rn(fx, fx);
-  s2 = __fmaf_rn(fy, fy, s2);
-  if (NDIM == 3) s2 = __fmaf_rn(fz, fz, s2);
-  const float len = __fsqrt_rn(s2);
-  ux = __fdiv_rn(fx, len);
-  uy = __fdiv_rn(fy, len);
-  uz = NDIM == 3 ? __fdiv_rn(fz, len) : 0.0f;
-}
-
-template <int NDIM>
-__device__ __forceinline__ float chemo_dot(const float* F, long long sites, int x, int y,
-                                           int z, int kdir, int nx, int ny, int nz) {
-  float ux, uy, uz;
-  int sx, sy, sz;
-  unit_dir<NDIM>(kdir, x, y, z, nx, ny, nz, ux, uy, uz, sx, sy, sz);
-  const long long site = ((long long)sz * ny + sy) * nx + sx;
-  float c = __fmul_rn(ux, __ldg(F + site));
-  c = __fmaf_rn(uy, __ldg(F + sites + site), c);
-  if (NDIM == 3) c = __fmaf_rn(uz, __ldg(F + 2 * sites + site), c);
-  return c;
-}
-
 // Act model (src/kernels2d.cu:338-473, src/kernels3d.cu:347-470): the
 // geometric mean of max(amax + act[i] - tick, 0) over site (x, y, z) and
 // those of its neighbours that hold `id`, as exp2 of the mean log2 (own
@@ -264,60 +186,6 @@ __device__ __forceinline__ float act_mean(const uint32_t* L, const uint32_t* A, 
         ++count;
       }
   return exp2_own(__fdiv_rn(sum, (float)count));
-}
-
-// Per-phase view of the double-buffered tables.
-template <int NDIM>
-struct PhaseTables {
-  const unsigned long long* rap;  // read copy (tables at phase start)
-  const long long* rcs;
-  unsigned long long* wap;        // other copy: receives this phase's deltas
-  long long* wcs;
-  unsigned long long* dap;        // this phase's deltas (replayed next phase)
-  long long* dcs;
-  uint32_t* list;                 // this block's dirty list for the phase
-  unsigned* cnt;                  // its length (shared memory)
-};
-
-// One accepted copy's change of one table row: added to the other table
-// copy and to the phase delta table.  Reductions only (no value comes
-// back), so the accepting warp does not wait on L2.  The row goes on the
-// block's dirty list separately (warp-aggregated, duplicates allowed).
-template <int NDIM>
-__device__ __forceinline__ void add_delta(const PhaseTables<NDIM>& pt,
-                                          long long row, int darea, int dperim,
-                                          const long long* img, long long sign) {
-  const unsigned long long pd = pack_delta(darea, dperim);
-  atomicAdd(pt.wap + row, pd);
-  atomicAdd(pt.dap + row, pd);
-#pragma unroll
-  for (int k = 0; k < NDIM; ++k) {
-    const unsigned long long v = (unsigned long long)(sign * img[k]);
-    atomicAdd(reinterpret_cast<unsigned long long*>(pt.wcs + row * NDIM + k), v);
-    atomicAdd(reinterpret_cast<unsigned long long*>(pt.dcs + row * NDIM + k), v);
-  }
-}
-
-// Replays the deltas of the rows on a block's dirty list into `ap`/`cs`,
-// strided over the block's threads.  A row can be on several lists (or
-// twice on one); taking its delta with an exchange hands it to exactly one
-// of them and leaves the delta table zeroed for the phase after next.
-template <int NDIM>
-__device__ __forceinline__ void replay(const uint32_t* list, unsigned n,
-                                       unsigned long long* dap, long long* dcs,
-                                       unsigned long long* ap, long long* cs) {
-  for (unsigned j = threadIdx.x; j < n; j += blockDim.x) {
-    const uint32_t row = __ldcg(list + j);
-    const unsigned long long d = atomicExch(dap + row, 0ull);
-    if (d) atomicAdd(ap + row, d);
-#pragma unroll
-    for (int k = 0; k < NDIM; ++k) {
-      const long long idx = (long long)row * NDIM + k;
-      const unsigned long long dc =
-          atomicExch(reinterpret_cast<unsigned long long*>(dcs + idx), 0ull);
-      if (dc) atomicAdd(reinterpret_cast<unsigned long long*>(cs + idx), dc);
-    }
-  }
 }
 
 // Warp-reduces a lane's score partial sums and adds them, by lane 0, to the

@@ -1,0 +1,575 @@
+// cpm_sweep2d.cu — the 2D sweep of a single lattice with TMA-staged,
+// row-major warp tiles.
+//
+//   sweep2d_kernel<PERIM, CY>  the checkerboard Metropolis sweep of one 2D
+//                              lattice whose width is a multiple of 4 sites
+//                              (the tissue workloads); same schedule, same
+//                              random stream and the same FP32 operation order
+//                              as sweep_kernel (cpm_kernels.cu), so its
+//                              results are bit-identical.  Replaces
+//                              copyAttempt (src/kernels2d.cu:44-583) for
+//                              these lattices.
+//
+// What differs from sweep_kernel is how a warp tile reaches shared memory and
+// how the passes read it:
+//  * A tile of 32 x CY targets of one slot spans 64 x 2CY lattice sites; it is
+//    staged with its halo as a row-major box of 72 x (2CY + 1) words starting
+//    at lattice column 64 tx - 4 (a multiple of 4, so every staged row starts
+//    on a 16-byte boundary).  Interior tiles are copied by one
+//    cp.async.bulk.tensor.2d issued by lane 0 and completed on a per-warp
+//    mbarrier; tiles on the periodic seam (the copy engine cannot wrap) load
+//    the same box with 16-byte vector loads, one wrapped coordinate per
+//    vector.  Either way the staging costs the warp a handful of
+//    instructions per tile instead of one load and one store per site.
+//  * Target column c of the tile sits at staged column 2c + 4 + parity, so a
+//    lane reads a target's row of three sites with two 8-byte loads: a
+//    3 x 3 neighbourhood is six ld.shared.v2 instead of nine scalar loads, and
+//    32 lanes read 256 consecutive bytes (two wavefronts, no conflict).
+//  * Parameters of the one replica are loaded once per launch.
+//
+// Coherence.  Lattice words are written with generic stores and read back by
+// the copy engine (async proxy) in later phases: the issuing lane executes
+// fence.proxy.async after the grid barrier (which orders every SM's writes)
+// and before each copy.  Within a phase every site a tile's attempts read is
+// either one of its own targets or a site of another class, which no attempt
+// of the phase writes, so a copy never races with a store it depends on.
+#include <cuda.h>  // CUtensorMap (the map itself is encoded on the host)
+
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <type_traits>
+
+#include "cpm_sweep_common.cuh"
+
+namespace gpucpm {
+namespace {
+
+constexpr int kPitch = 72;              // words per staged row
+constexpr int kVecPerRow = kPitch / 4;  // 16-byte vectors per staged row
+
+template <int CY>
+struct RowTile {
+  static constexpr int SR = 2 * CY + 1;  // staged rows
+  static constexpr int WORDS = SR * kPitch;
+  static constexpr int NT = 32 * CY;     // targets
+  static constexpr unsigned BYTES = WORDS * 4u;
+};
+
+// Per-warp shared memory.  The tile leads and the struct is 128-byte
+// aligned, as the copy engine's destination must be.
+template <int CY>
+struct alignas(128) Warp2Smem {
+  uint32_t tile[RowTile<CY>::WORDS];
+  unsigned long long bar;  // mbarrier of the tile copy
+  uint2 qb[RowTile<CY>::NT];
+  uint16_t qa[RowTile<CY>::NT];
+};
+
+template <int CY>
+constexpr int row_tile_warps(int cap) {
+  const int w = (int)(kSweepSmemMax / sizeof(Warp2Smem<CY>));
+  return w < cap ? w : cap;
+}
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Lane 0: arm the warp's barrier for one tile and start the copy of the box
+// whose top-left lattice site is (x, y).
+__device__ __forceinline__ void tma_load_tile(uint32_t dst, uint32_t bar, const CUtensorMap* map,
+                                              int x, int y, unsigned bytes) {
+  asm volatile("fence.proxy.async;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+// Waits for the copy that completes phase `parity` of the barrier, bounded
+// by the sweep's barrier timeout; false (and kErrTimeout) if it ran out.
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, int* err) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = global_timer_ns();
+  for (unsigned spins = 1;; ++spins) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((spins & 63u) == 0 && global_timer_ns() - t0 > kBarrierTimeoutNs) {
+      atomicOr(err, kErrTimeout);
+      return false;
+    }
+  }
+}
+
+// The three sites of staged row `row` around target column qx of parity PAR
+// (left, centre, right), from two 8-byte loads.
+template <int PAR>
+__device__ __forceinline__ void row3(const uint32_t* tile, int row, int qx, uint32_t& l,
+                                     uint32_t& c, uint32_t& r) {
+  const uint32_t* p = tile + row * kPitch + 2 * qx + 2 + 2 * PAR;
+  const uint2 A = *reinterpret_cast<const uint2*>(p);
+  const uint2 B = *reinterpret_cast<const uint2*>(p + 2);
+  if (PAR) {
+    l = A.x;
+    c = A.y;
+    r = B.x;
+  } else {
+    l = A.y;
+    c = B.x;
+    r = B.y;
+  }
+}
+
+// Target (qx, qy) and its Moore neighbours in (dy, dx) lexicographic order.
+template <int PAR>
+__device__ __forceinline__ uint32_t nbhd(const uint32_t* tile, int qx, int qy, uint32_t* nb) {
+  uint32_t t;
+  row3<PAR>(tile, 2 * qy, qx, nb[0], nb[1], nb[2]);
+  row3<PAR>(tile, 2 * qy + 1, qx, nb[3], t, nb[4]);
+  row3<PAR>(tile, 2 * qy + 2, qx, nb[5], nb[6], nb[7]);
+  return t;
+}
+
+// staged index of target (qx, qy) and offset of neighbour k
+template <int PAR>
+__device__ __forceinline__ int center_idx(int qx, int qy) {
+  return (2 * qy + 1) * kPitch + 2 * qx + 4 + PAR;
+}
+__device__ __forceinline__ int nb_off(int k) {
+  const int m = k + (k >= 4);
+  return (m / 3 - 1) * kPitch + (m % 3 - 1);
+}
+
+template <bool PERIM, int CY>
+__global__ void __launch_bounds__(32 * kMaxSweepWarps, 1)
+    sweep2d_kernel(const __grid_constant__ SweepArgs a, const __grid_constant__ CUtensorMap tmap,
+                   const int use_tma) {
+  using RT = RowTile<CY>;
+  constexpr unsigned long long NSLOTS = 9;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ int s_ok;
+  __shared__ unsigned s_cnt[2];
+  __shared__ unsigned long long s_tick0;
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int wpb = blockDim.x >> 5;
+  Warp2Smem<CY>& ws = reinterpret_cast<Warp2Smem<CY>*>(smem_raw)[warp];
+  const uint32_t tile_s = smem_addr(ws.tile), bar_s = smem_addr(&ws.bar);
+  const uint32_t k0 = (uint32_t)a.seed, k1 = (uint32_t)(a.seed >> 32);
+  int* err = reinterpret_cast<int*>(&a.ctl[kCtlErr]);
+  auto blist = [&](int b) { return a.dlist + (2LL * blockIdx.x + b) * a.list_cap; };
+  unsigned episode = 0;
+  unsigned long long n_eval = 0, n_acc = 0;  // warp-uniform
+  uint32_t bar_parity = 0;
+  bool fill_ok = true;  // warp-uniform: false once a tile copy timed out
+  if (tid < 2) s_cnt[tid] = 0;
+  if (tid == 0) s_tick0 = a.tick_ptr ? __ldcg(a.tick_ptr) : a.tick0;
+  if (lane == 0) {
+    mbar_init(bar_s, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+
+  // The one replica's constants.
+  const DevParams* P = a.params + __ldg(&a.reps[0].pset);
+  const unsigned fixed_mask = __ldg(&P->fixed_mask);
+  const bool stick_on = __ldg(&P->stick_on) != 0;
+  const bool chemo_on = __ldg(&P->chemo_on) != 0;
+  const bool perim_on = PERIM && __ldg(&P->perim_on) != 0;
+  const float T = __ldg(&P->temperature);
+  const int nx = __ldg(&a.reps[0].nx), ny = __ldg(&a.reps[0].ny);
+  const int ncells = __ldg(&a.reps[0].ncells);
+  const long long lat_off = __ldg(&a.reps[0].lat_off);
+  const long long cell_off = __ldg(&a.reps[0].cell_off);
+  uint32_t* L = a.lat + lat_off;
+
+  auto tables = [&](int cur) {
+    PhaseTables<2> pt;
+    pt.rap = cur ? a.ap[1] : a.ap[0];
+    pt.rcs = cur ? a.cs[1] : a.cs[0];
+    pt.wap = cur ? a.ap[0] : a.ap[1];
+    pt.wcs = cur ? a.cs[0] : a.cs[1];
+    pt.dap = cur ? a.dap[1] : a.dap[0];
+    pt.dcs = cur ? a.dcs[1] : a.dcs[0];
+    pt.list = blist(cur);
+    pt.cnt = &s_cnt[cur];
+    return pt;
+  };
+  auto replay_phase = [&](int prv) {
+    const unsigned n = min(s_cnt[prv], (unsigned)a.list_cap);  // see kErrListFull
+    replay<2>(blist(prv), n, prv ? a.dap[1] : a.dap[0], prv ? a.dcs[1] : a.dcs[0],
+              prv ? a.ap[1] : a.ap[0], prv ? a.cs[1] : a.cs[0]);
+  };
+
+  // Stage tile (tx, ty) of slot (cx, cy): 72 x SR words from lattice column
+  // 64 tx - 4 and row yorig.
+  auto stage = [&](int X0, int yorig) {
+    const bool interior =
+        use_tma && X0 >= 0 && X0 + kPitch <= nx && yorig >= 0 && yorig + RT::SR <= ny;
+    if (interior) {
+      if (lane == 0) tma_load_tile(tile_s, bar_s, &tmap, X0, yorig, RT::BYTES);
+      fill_ok = mbar_wait_bounded(bar_s, bar_parity, err) && fill_ok;
+      bar_parity ^= 1u;
+      fill_ok = __all_sync(kFull, fill_ok);
+    } else {
+      for (int v = lane; v < RT::SR * kVecPerRow; v += 32) {
+        const int row = v / kVecPerRow, col = v - row * kVecPerRow;
+        int gy = yorig + row;
+        gy = gy < 0 ? gy + ny : (gy >= ny ? gy - ny : gy);
+        int gx = X0 + 4 * col;
+        gx = gx < 0 ? gx + nx : (gx >= nx ? gx - nx : gx);
+        const uint4 val = __ldcg(reinterpret_cast<const uint4*>(L + (long long)gy * nx + gx));
+        *reinterpret_cast<uint4*>(ws.tile + row * kPitch + 4 * col) = val;
+      }
+      __syncwarp();
+    }
+  };
+
+  // One warp tile, column parity PAR (= cx).
+  auto run_tile = [&](auto par, const PhaseTables<2>& pt, const int tx, const int ty,
+                      const int cy, const unsigned long long phase) {
+    constexpr int PAR = decltype(par)::value;
+    const int ncx = nx >> 1, ncy = class_count(ny, cy);
+    const int i0 = tx * 32, j0 = ty * CY;
+    const int cntx = min(32, ncx - i0), cnty = min(CY, ncy - j0);
+    const int X0 = 2 * i0 - 4;
+    const int yorig = class_coord(ny, cy, j0) - 1;
+    stage(X0, yorig);
+    if (!fill_ok) return;  // a copy timed out: the phase's barrier reports it
+
+    // ---- pass 1: boundary test ---------------------------------------
+    int na = 0;
+#pragma unroll
+    for (int qy = 0; qy < CY; ++qy) {
+      bool bnd = false;
+      if (lane < cntx && qy < cnty) {
+        uint32_t nb[8];
+        const uint32_t t = nbhd<PAR>(ws.tile, lane, qy, nb);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) bnd |= nb[k] != t;
+      }
+      const unsigned ball = __ballot_sync(kFull, bnd);
+      if (bnd) ws.qa[na + __popc(ball & lanemask_lt())] = (uint16_t)(qy * 32 + lane);
+      na += __popc(ball);
+    }
+    __syncwarp();
+
+    // ---- pass 2: random draw and source pick -------------------------
+    int nbq = 0;
+    for (int base = 0; base < na; base += 32) {
+      const int j = base + lane;
+      bool keep = false;
+      uint2 entry = make_uint2(0u, 0u);
+      if (j < na) {
+        const int q = ws.qa[j];
+        const int qx = q & 31, qy = q >> 5;
+        const int x = 2 * (i0 + qx) + PAR;
+        const int y = class_coord(ny, cy, j0 + qy);
+        const long long site = (long long)y * nx + x;
+        uint32_t c0 = (uint32_t)site, c1 = (uint32_t)phase, c2 = a.stream0,
+                 c3 = (uint32_t)(phase >> 32);
+        philox4x32_10(c0, c1, c2, c3, k0, k1);
+        const int kdir = (int)__umulhi(c0, 8u);
+        const int c = center_idx<PAR>(qx, qy);
+        const uint32_t tv = ws.tile[c], sv = ws.tile[c + nb_off(kdir)];
+        keep = sv != tv;
+        uint32_t medium = 0;  // 1: the source is replaced by the medium
+        if (fixed_mask && keep) {
+          // a target of a fixed type never changes; a source of a fixed type
+          // proposes the medium instead (src/kernels2d.cu:280-290)
+          if ((fixed_mask >> ((tv >> 24) & (kMaxTypes - 1))) & 1u) {
+            keep = false;
+          } else if ((fixed_mask >> ((sv >> 24) & (kMaxTypes - 1))) & 1u) {
+            medium = 1;
+            keep = tv != 0u;
+          }
+        }
+        entry = make_uint2((uint32_t)q | ((uint32_t)kdir << 16) | (medium << 24), c1);
+      }
+      const unsigned ball = __ballot_sync(kFull, keep);
+      if (keep) ws.qb[nbq + __popc(ball & lanemask_lt())] = entry;
+      nbq += __popc(ball);
+    }
+    __syncwarp();
+
+    // ---- pass 3: dH, Metropolis test, commit -------------------------
+    for (int base = 0; base < nbq; base += 32) {
+      const int j = base + lane;
+      bool accepted = false;
+      long long push_s = -1, push_t = -1;  // table rows this lane changed
+      if (j < nbq) {
+        const uint2 entry = ws.qb[j];
+        const int q = (int)(entry.x & 0xFFFFu), kdir = (int)((entry.x >> 16) & 0xFFu);
+        const int qx = q & 31, qy = q >> 5;
+        uint32_t nb[8];
+        const uint32_t t = nbhd<PAR>(ws.tile, qx, qy, nb);
+        const uint32_t s =
+            (entry.x >> 24) ? 0u : ws.tile[center_idx<PAR>(qx, qy) + nb_off(kdir)];
+        const uint32_t is = s & 0xFFFFFFu, it = t & 0xFFFFFFu;
+        if (is > (uint32_t)ncells || it > (uint32_t)ncells) {
+          atomicOr(err, kErrBadId);
+        } else {
+          const int ts = (int)(s >> 24) & (kMaxTypes - 1);
+          const int tt = (int)(t >> 24) & (kMaxTypes - 1);
+          const long long rs = cell_off + is, rt = cell_off + it;
+          const unsigned long long aps = s ? __ldcg(pt.rap + rs) : 0ull;
+          const unsigned long long apt = t ? __ldcg(pt.rap + rt) : 0ull;
+          // centroid sums, needed only on acceptance, fetched with the row
+          // so that an accepted attempt waits on one L2 round trip
+          long long cs_s[2], cs_t[2];
+#pragma unroll
+          for (int k = 0; k < 2; ++k) {
+            cs_s[k] = s ? __ldcg(pt.rcs + rs * 2 + k) : 0;
+            cs_t[k] = t ? __ldcg(pt.rcs + rt * 2 + k) : 0;
+          }
+          float e_old = 0.0f, e_new = 0.0f;
+          int cnt_s = 0, cnt_t = 0;
+          const float* Jt = P->J + tt * kMaxTypes;
+          const float* Js = P->J + ts * kMaxTypes;
+#pragma unroll
+          for (int k = 0; k < 8; ++k) {
+            const uint32_t v = nb[k];
+            const int tn = (int)(v >> 24) & (kMaxTypes - 1);
+            if (v != t) e_old = __fadd_rn(e_old, __ldg(Jt + tn));
+            if (v != s) e_new = __fadd_rn(e_new, __ldg(Js + tn));
+            cnt_s += v == s;
+            cnt_t += v == t;
+          }
+          if (stick_on) {
+            // stickiness of the old configuration, summed in neighbour order
+            // and added to its adhesion as one term
+            float e_st = 0.0f;
+            const float* St = P->stick + tt * kMaxTypes;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+              const uint32_t v = nb[k];
+              const int tn = (int)(v >> 24) & (kMaxTypes - 1);
+              if (v != t) e_st = __fadd_rn(e_st, __ldg(St + tn));
+            }
+            e_old = __fadd_rn(e_old, e_st);
+          }
+          float dH = __fsub_rn(e_new, e_old);
+          const int x = 2 * (i0 + qx) + PAR;
+          const int y = class_coord(ny, cy, j0 + qy);
+          {
+            // chemotaxis first, as in the reference's sum; lambda of the
+            // source type, of the target type for a medium source
+            float chemo = 0.0f;
+            if (chemo_on) {
+              const float lam = __ldg(&P->chemo[ts ? ts : tt]);
+              if (lam != 0.0f)
+                chemo = __fmul_rn(-lam, chemo_dot<2>(a.field + 2 * lat_off,
+                                                     (long long)nx * ny, x, y, 0, kdir, nx,
+                                                     ny, 1));
+            }
+            dH = __fadd_rn(chemo, dH);
+          }
+          const int dps = 8 - 2 * cnt_s;
+          const int dpt = 2 * cnt_t - 8;
+          if (perim_on) {
+            if (s) {
+              const long long qv = (long long)dps *
+                  (2LL * (unpack_perim(aps) - __ldg(&P->tgt_perim[ts])) + dps);
+              dH = __fmaf_rn(__ldg(&P->lam_perim[ts]), __ll2float_rn(qv), dH);
+            }
+            if (t) {
+              const long long qv = (long long)dpt *
+                  (2LL * (unpack_perim(apt) - __ldg(&P->tgt_perim[tt])) + dpt);
+              dH = __fmaf_rn(__ldg(&P->lam_perim[tt]), __ll2float_rn(qv), dH);
+            }
+          }
+          if (s) {
+            const long long qv = 1 + 2LL * (unpack_area(aps) - __ldg(&P->tgt_area[ts]));
+            dH = __fmaf_rn(__ldg(&P->lam_area[ts]), __ll2float_rn(qv), dH);
+          }
+          if (t) {
+            const long long qv = 1 - 2LL * (unpack_area(apt) - __ldg(&P->tgt_area[tt]));
+            dH = __fmaf_rn(__ldg(&P->lam_area[tt]), __ll2float_rn(qv), dH);
+          }
+          bool ok;
+          if (dH < 0.0f) {
+            ok = true;
+          } else if (!(T > 0.0f)) {
+            ok = false;
+          } else {
+            const float u = __fmul_rn(__uint2float_rn((entry.y >> 8) | 1u), 0x1p-24f);
+            ok = u < exp_neg(__fdiv_rn(-dH, T));
+          }
+          if (ok) {
+            accepted = true;
+            L[(long long)y * nx + x] = s;
+            const int crd[2] = {x, y};
+            const int dim[2] = {nx, ny};
+            long long img[2];
+            if (s) {
+#pragma unroll
+              for (int k = 0; k < 2; ++k)
+                img[k] = nearest_image(crd[k], dim[k], unpack_area(aps), cs_s[k]);
+              add_delta<2>(pt, rs, 1, dps, img, 1);
+              push_s = rs;
+            }
+            if (t) {
+#pragma unroll
+              for (int k = 0; k < 2; ++k)
+                img[k] = nearest_image(crd[k], dim[k], unpack_area(apt), cs_t[k]);
+              add_delta<2>(pt, rt, -1, dpt, img, -1);
+              push_t = rt;
+            }
+          }
+        }
+      }
+      n_acc += __popc(__ballot_sync(kFull, accepted));
+      // the changed rows onto the block's dirty list: one shared-memory
+      // atomic per warp and batch
+      const unsigned bs = __ballot_sync(kFull, push_s >= 0);
+      const unsigned bt = __ballot_sync(kFull, push_t >= 0);
+      if (bs | bt) {  // warp-uniform
+        const unsigned npush = (unsigned)(__popc(bs) + __popc(bt));
+        unsigned at = 0;
+        if (lane == 0) at = atomicAdd(pt.cnt, npush);
+        at = __shfl_sync(kFull, at, 0);
+        if ((long long)at + npush > a.list_cap) {
+          if (lane == 0) atomicOr(err, kErrListFull);
+        } else {
+          if (push_s >= 0) pt.list[at + __popc(bs & lanemask_lt())] = (uint32_t)push_s;
+          if (push_t >= 0)
+            pt.list[at + __popc(bs) + __popc(bt & lanemask_lt())] = (uint32_t)push_t;
+        }
+      }
+    }
+    n_eval += nbq;
+    __syncwarp();  // the tile buffers are rewritten by the next tile
+  };
+
+  int step = 0;
+  for (int m = 0; m < a.mcs; ++m) {
+    const unsigned long long tick = s_tick0 + (unsigned long long)m;
+    for (int si = 0; si < a.nslot_active; ++si, ++step) {
+      const int cur = step & 1, prv = cur ^ 1;
+      const PhaseTables<2> pt = tables(cur);
+      if (step > 0) replay_phase(prv);
+      const int slot = a.slots[si];
+      const int cx = slot % 3, cy = (slot / 3) % 3;
+      const unsigned long long phase = tick * NSLOTS + (unsigned long long)slot;
+      // tiles of the slot: 32 target columns by CY target rows
+      const int tnx = ((nx >> 1) + 31) / 32;
+      const int tny = (class_count(ny, cy) + CY - 1) / CY;
+      const int ntiles = tnx * tny;
+      // each block sweeps one contiguous band of tile rows, the same in
+      // every phase; its warps take the band's tiles in turn
+      const int per_b = ntiles / (int)gridDim.x, extra = ntiles % (int)gridDim.x;
+      const int tb0 = (int)blockIdx.x * per_b + min((int)blockIdx.x, extra);
+      const int tb1 = tb0 + per_b + ((int)blockIdx.x < extra ? 1 : 0);
+      int task = tb0 + warp;
+      int tx = task % tnx, ty = task / tnx;
+      for (; task < tb1; task += wpb) {
+        if (cx)
+          run_tile(std::integral_constant<int, 1>{}, pt, tx, ty, cy, phase);
+        else
+          run_tile(std::integral_constant<int, 0>{}, pt, tx, ty, cy, phase);
+        tx += wpb;
+        while (tx >= tnx) {
+          tx -= tnx;
+          ++ty;
+        }
+      }
+      __syncthreads();
+      if (tid == 0) s_cnt[prv] = 0;
+      if (!grid_barrier(a.ctl, ++episode, &s_ok)) return;
+    }
+  }
+  if (step > 0) replay_phase((step - 1) & 1);
+
+  if (lane == 0) {
+    if (n_eval) atomicAdd(&a.counters[0], n_eval);
+    if (n_acc) atomicAdd(&a.counters[1], n_acc);
+  }
+  if (a.tick_ptr && a.tick_advance && blockIdx.x == 0 && tid == 0 && a.mcs > 0)
+    *a.tick_ptr = s_tick0 + (unsigned long long)a.mcs;
+}
+
+template <int CY>
+const void* sweep2d_fn(bool perim) {
+  return perim ? (const void*)sweep2d_kernel<true, CY> : (const void*)sweep2d_kernel<false, CY>;
+}
+
+const void* sweep2d_fn_v(bool perim, int variant) {
+  switch (variant) {
+    case 1: return sweep2d_fn<8>(perim);
+    case 2: return sweep2d_fn<16>(perim);
+    case 3: return sweep2d_fn<1>(perim);
+    default: return sweep2d_fn<6>(perim);
+  }
+}
+
+template <int CY>
+SweepShape row_shape(int warps_cap) {
+  SweepShape s;
+  s.variant = 0;
+  s.cx = 32;
+  s.cy = CY;
+  s.cz = 1;
+  s.warps = row_tile_warps<CY>(warps_cap);
+  s.smem = sizeof(Warp2Smem<CY>) * (size_t)s.warps;
+  return s;
+}
+
+}  // namespace
+
+int row_tile_rows(int variant) {
+  switch (variant) {
+    case 1: return 2 * 8 + 1;
+    case 2: return 2 * 16 + 1;
+    case 3: return 2 * 1 + 1;
+    default: return 2 * 6 + 1;
+  }
+}
+
+bool row_tiles_fit(int nx, int ny) {
+  // vector loads need rows on 16-byte boundaries; one periodic wrap per
+  // staged coordinate needs the lattice wider than a staged row and taller
+  // than two staged boxes
+  return nx % 4 == 0 && nx >= kPitch && ny >= 2 * row_tile_rows(2);
+}
+
+cudaError_t launch_sweep2d(bool perim, int variant, const SweepArgs& a, const void* tmap,
+                           int use_tma, int grid, int warps_cap, cudaStream_t s) {
+  SweepShape sh;
+  switch (variant) {
+    case 1: sh = row_shape<8>(warps_cap); break;
+    case 2: sh = row_shape<16>(warps_cap); break;
+    case 3: sh = row_shape<1>(warps_cap); break;
+    default: sh = row_shape<6>(warps_cap); break;
+  }
+  const void* fn = sweep2d_fn_v(perim, variant);
+  cudaError_t e =
+      cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem);
+  if (e != cudaSuccess) return e;
+  alignas(64) CUtensorMap map;
+  std::memcpy(&map, tmap, sizeof map);
+  int tma = use_tma ? 1 : 0;
+  void* args[] = {const_cast<SweepArgs*>(&a), &map, &tma};
+  return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(32 * sh.warps), args, sh.smem, s);
+}
+
+}  // namespace gpucpm

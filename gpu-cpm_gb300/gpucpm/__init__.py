@@ -58,6 +58,10 @@ CPM_FLAG_ACT = 2
 DISPATCH_GRID = 0
 DISPATCH_REPLICA = 1
 DISPATCH_HYBRID = 2
+FILL_PARITY = 0
+FILL_VECTOR = 1
+FILL_TMA = 2
+FILL_NAMES = {FILL_PARITY: "parity", FILL_VECTOR: "vector", FILL_TMA: "tma"}
 
 
 class CpmError(RuntimeError):
@@ -206,6 +210,8 @@ def library():
         "cpm_set_variant": [H, ctypes.c_int],
         "cpm_sweep_config": [H, ip, ip, ip, ip, ip, ip, ip],
         "cpm_set_dispatch": [H, ctypes.c_int],
+        "cpm_set_fill": [H, ctypes.c_int],
+        "cpm_get_fill": [H, ip],
         "cpm_recount": [H],
         "cpm_set_centroid_sums_r": [H, ctypes.c_int, ctypes.c_void_p],
         "cpm_get_params_r": [H, ctypes.c_int, ctypes.POINTER(StaticParams)],
@@ -539,14 +545,26 @@ class _Engine:
                    vals.ctypes.data)
 
     def sweep_config(self):
-        """dict(variant, tile, warps_per_block, grid, dispatch) of the launch
-        runs use."""
+        """dict(variant, tile, warps_per_block, grid, dispatch, fill) of the
+        launch runs use."""
         vals = [ctypes.c_int() for _ in range(7)]
         self._call("cpm_sweep_config", *[ctypes.byref(v) for v in vals])
         v, tx, ty, tz, w, g, d = (x.value for x in vals)
         return {"variant": v, "tile": (tx, ty, tz), "warps_per_block": w, "grid": g,
                 "dispatch": {DISPATCH_REPLICA: "replica",
-                             DISPATCH_HYBRID: "hybrid"}.get(d, "grid")}
+                             DISPATCH_HYBRID: "hybrid"}.get(d, "grid"),
+                "fill": FILL_NAMES[self.fill]}
+
+    @property
+    def fill(self):
+        """How the sweep stages its tiles: FILL_PARITY, FILL_VECTOR or
+        FILL_TMA (see cpm_set_fill)."""
+        f = ctypes.c_int()
+        self._call("cpm_get_fill", ctypes.byref(f))
+        return f.value
+
+    def set_fill(self, fill):
+        self._call("cpm_set_fill", int(fill))
 
 
 class Cpm(_Engine):

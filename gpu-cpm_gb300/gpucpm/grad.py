@@ -197,15 +197,21 @@ def reduce_gradient(grad, group=None):
 
 
 def crn_finite_difference(ensemble, theta, mcs, rel_step=0.01, checkpoint=None,
-                          per_replica=False):
+                          per_replica=False, params=None):
     """Central differences of mean_r O at `checkpoint` (default: mcs) with
     step rel_step * |theta_k| (rel_step for a zero entry), every pair of runs
     on the same random numbers.  With per_replica, also returns the [R, K]
-    per-replica differences whose mean over replicas is the estimate."""
+    per-replica differences whose mean over replicas is the estimate.
+    `params` (indices) limits the differences to those parameters; the
+    others are NaN."""
     theta = torch.as_tensor(theta, dtype=torch.float64)
     cp = [checkpoint or mcs]
     cols = []
+    R = len(ensemble.workloads)
     for k in range(len(theta)):
+        if params is not None and k not in params:
+            cols.append(torch.full((R,), float("nan"), dtype=torch.float64))
+            continue
         h = rel_step * (abs(float(theta[k])) or 1.0)
         tp, tm = theta.clone(), theta.clone()
         tp[k] += h

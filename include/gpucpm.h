@@ -323,6 +323,25 @@ int cpm_sweep_config(const cpm_handle* h, int* variant, int* tile_x,
                      int* tile_y, int* tile_z, int* warps_per_block,
                      int* grid, int* dispatch);
 
+/* How warp tiles reach shared memory in the sweep of one 2D lattice.  No
+ * counterpart in the reference (its tile load is src/kernels2d.cu:109-176).
+ *   CPM_FILL_PARITY  the general sweep: scalar loads, even and odd columns
+ *                    in separate halves of the tile
+ *   CPM_FILL_VECTOR  row-major tiles from 16-byte vector loads
+ *   CPM_FILL_TMA     row-major tiles, interior tiles copied by the tensor
+ *                    memory accelerator (cp.async.bulk.tensor), tiles on the
+ *                    periodic seam from vector loads
+ * Row-major tiles need a single 2D lattice with nx a multiple of 4,
+ * nx >= 72 and ny >= 66; such lattices start in CPM_FILL_TMA (CPM_FILL_VECTOR
+ * where the tensor maps cannot be encoded), all others in CPM_FILL_PARITY.
+ * The result does not depend on the fill: it selects the kernel only
+ * (CPM_ERR_UNSUPPORTED for a fill the lattice cannot use). */
+#define CPM_FILL_PARITY 0
+#define CPM_FILL_VECTOR 1
+#define CPM_FILL_TMA 2
+int cpm_set_fill(cpm_handle* h, int fill);
+int cpm_get_fill(const cpm_handle* h, int* fill);
+
 /* Replaces Cpm::synchronize (src/cpm.cu:653-655).  Waits for the handle's
  * stream and reports device-side errors (CPM_ERR_TIMEOUT, CPM_ERR_CUDA). */
 int cpm_synchronize(cpm_handle* h);

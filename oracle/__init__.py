@@ -92,6 +92,8 @@ def lib():
                                       ctypes.c_void_p, ctypes.c_void_p]
         l.orc_persist_update.argtypes = [ctypes.POINTER(Params)] + [ctypes.c_void_p] * 6 + [
             ctypes.c_int, ctypes.c_int]
+        l.orc_dh_error.argtypes = [ctypes.POINTER(Params)] + [ctypes.c_void_p] * 3 + [
+            ctypes.c_int, ctypes.c_void_p]
         _lib = l
     return _lib
 
@@ -261,6 +263,21 @@ class OracleSim:
                              ctypes.byref(spec), scores.ctypes.data)
         self.tick += int(mcs)
         return scores
+
+    def dh_error(self, nthreads=0):
+        """FP32 dH (the sweep's arithmetic) against an FP64 recomputation over
+        every (target, neighbouring source of another id) pair of the current
+        state: dict(pairs, max_abs, max_rel, max_rel_dh, max_accept_prob_diff,
+        sign_flips); max_rel divides by the sum of the terms' magnitudes,
+        max_rel_dh by max(|dH64|, 1).  Adhesion, stickiness, perimeter and
+        area terms."""
+        out = np.zeros(6, np.float64)
+        lib().orc_dh_error(ctypes.byref(self.params), self.lattice.ctypes.data,
+                           self.area.ctypes.data, self.perim.ctypes.data, int(nthreads),
+                           out.ctypes.data)
+        return {"pairs": int(out[0]), "max_abs": float(out[1]), "max_rel": float(out[2]),
+                "max_rel_dh": float(out[5]), "max_accept_prob_diff": float(out[3]),
+                "sign_flips": int(out[4])}
 
     def recount(self):
         """Tables recomputed from scratch from the current lattice."""

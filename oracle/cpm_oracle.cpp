@@ -55,6 +55,7 @@
 // Build: oracle/build.py (g++ -O2 -ffp-contract=off -fopenmp).  Contraction
 // must stay off so that no a*b+c is fused behind the code's back.
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -866,6 +867,119 @@ void orc_persist_update(const orc_params* pp, const int32_t* area, const int64_t
     if (l2 == 0.0) continue;
     for (int k = 0; k < 3; ++k) prefdir[3 * c + k] = np[k] / l2;
   }
+}
+
+// FP32 dH of the sweep against an FP64 recomputation, over every (target,
+// source) pair a sweep could evaluate in the current state: each site and
+// each Moore neighbour holding another id.  The FP32 value follows attempt()
+// step for step (adhesion and stickiness summed in neighbour order, one
+// fused multiply-add per constraint); the FP64 value sums the same terms
+// (parameters widened from their FP32 values, integers exact) in double.
+// Terms covered: adhesion, stickiness, perimeter and area (the tissue
+// workloads').  out[0] pairs, out[1] max |dH32 - dH64|, out[2] max of that
+// over the sum of the terms' magnitudes (the scale FP32 rounding works on),
+// out[3] max |min(1, e^(-dH32/T)) - min(1, e^(-dH64/T))|, out[4] pairs whose
+// sign of dH differs, out[5] max |dH32 - dH64| / max(|dH64|, 1).  Test
+// infrastructure.
+void orc_dh_error(const orc_params* pp, const uint32_t* lat, const int32_t* area,
+                  const int32_t* perim, int nthreads, double* out) {
+  const Params& p = *reinterpret_cast<const Params*>(pp);
+  const int nx = p.nx, ny = p.ny, nz = p.nz;
+  const int N = p.ndim == 2 ? 8 : 26;
+  const bool perim_on = perimeter_enabled(p);
+  const int64_t sites = (int64_t)nx * ny * nz;
+  double n_all = 0, max_abs = 0, max_rel = 0, max_pd = 0, flips = 0, max_rel_dh = 0;
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 4096) reduction(+ : n_all, flips) \
+    reduction(max : max_abs, max_rel, max_pd, max_rel_dh)
+  for (int64_t site = 0; site < sites; ++site) {
+    const int x = (int)(site % nx), y = (int)((site / nx) % ny), z = (int)(site / ((int64_t)nx * ny));
+    uint32_t nb[26];
+    int m = 0;
+    const int zlo = p.ndim == 3 ? -1 : 0, zhi = p.ndim == 3 ? 1 : 0;
+    for (int dz = zlo; dz <= zhi; ++dz)
+      for (int dy = -1; dy <= 1; ++dy)
+        for (int dx = -1; dx <= 1; ++dx) {
+          if (!dz && !dy && !dx) continue;
+          nb[m++] = lat[((int64_t)wrap(z + dz, nz) * ny + wrap(y + dy, ny)) * nx + wrap(x + dx, nx)];
+        }
+    const uint32_t t = lat[site];
+    const int tt = (int)(t >> 24);
+    for (int kdir = 0; kdir < N; ++kdir) {
+      const uint32_t s = nb[kdir];
+      if (s == t) continue;
+      const int ts = (int)(s >> 24);
+      float e_old = 0.0f, e_new = 0.0f, e_st = 0.0f;
+      double d_old = 0.0, d_new = 0.0, scale = 0.0;
+      int cnt_s = 0, cnt_t = 0;
+      for (int k = 0; k < N; ++k) {
+        const int tn = (int)(nb[k] >> 24);
+        if (nb[k] != t) {
+          e_old = e_old + p.J[tt * kMaxTypes + tn];
+          e_st = e_st + p.stick[tt * kMaxTypes + tn];
+          d_old += (double)p.J[tt * kMaxTypes + tn] + (double)p.stick[tt * kMaxTypes + tn];
+          scale += std::fabs((double)p.J[tt * kMaxTypes + tn]) +
+                   std::fabs((double)p.stick[tt * kMaxTypes + tn]);
+        }
+        if (nb[k] != s) {
+          e_new = e_new + p.J[ts * kMaxTypes + tn];
+          d_new += (double)p.J[ts * kMaxTypes + tn];
+          scale += std::fabs((double)p.J[ts * kMaxTypes + tn]);
+        }
+        cnt_s += nb[k] == s;
+        cnt_t += nb[k] == t;
+      }
+      e_old = e_old + e_st;
+      float dH = e_new - e_old;
+      double dD = d_new - d_old;
+      const int dps = N - 2 * cnt_s, dpt = 2 * cnt_t - N;
+      const uint32_t is = s & 0xFFFFFFu, it = t & 0xFFFFFFu;
+      if (perim_on) {
+        if (s) {
+          const int64_t q = (int64_t)dps * (2 * ((int64_t)perim[is] - p.tgt_perim[ts]) + dps);
+          dH = std::fma(p.lam_perim[ts], (float)q, dH);
+          dD += (double)p.lam_perim[ts] * (double)q;
+          scale += std::fabs((double)p.lam_perim[ts] * (double)q);
+        }
+        if (t) {
+          const int64_t q = (int64_t)dpt * (2 * ((int64_t)perim[it] - p.tgt_perim[tt]) + dpt);
+          dH = std::fma(p.lam_perim[tt], (float)q, dH);
+          dD += (double)p.lam_perim[tt] * (double)q;
+          scale += std::fabs((double)p.lam_perim[tt] * (double)q);
+        }
+      }
+      if (s) {
+        const int64_t q = 1 + 2 * ((int64_t)area[is] - p.tgt_area[ts]);
+        dH = std::fma(p.lam_area[ts], (float)q, dH);
+        dD += (double)p.lam_area[ts] * (double)q;
+        scale += std::fabs((double)p.lam_area[ts] * (double)q);
+      }
+      if (t) {
+        const int64_t q = 1 - 2 * ((int64_t)area[it] - p.tgt_area[tt]);
+        dH = std::fma(p.lam_area[tt], (float)q, dH);
+        dD += (double)p.lam_area[tt] * (double)q;
+        scale += std::fabs((double)p.lam_area[tt] * (double)q);
+      }
+      const double err = std::fabs((double)dH - dD);
+      n_all += 1;
+      max_abs = std::max(max_abs, err);
+      max_rel = std::max(max_rel, err / std::max(scale, 1.0));
+      max_rel_dh = std::max(max_rel_dh, err / std::max(std::fabs(dD), 1.0));
+      if ((dH < 0.0f) != (dD < 0.0)) flips += 1;
+      if (p.temperature > 0.0f) {
+        const double T = (double)p.temperature;
+        const double p32 = dH < 0.0f ? 1.0 : std::exp(-(double)dH / T);
+        const double p64 = dD < 0.0 ? 1.0 : std::exp(-dD / T);
+        max_pd = std::max(max_pd, std::fabs(p32 - p64));
+      }
+    }
+  }
+  out[0] = n_all;
+  out[1] = max_abs;
+  out[2] = max_rel;
+  out[3] = max_pd;
+  out[4] = flips;
+  out[5] = max_rel_dh;
 }
 
 }  // extern "C"

@@ -679,3 +679,34 @@ def test_first_mcs_3d_matches_reference_dh_formula(case):
     np.testing.assert_array_equal(sim.lattice, lat)
     np.testing.assert_array_equal(sim.area, area)
     np.testing.assert_array_equal(sim.perim, perim)
+
+
+def test_fp32_dh_error_on_the_4096_tissue():
+    """The sweep's FP32 dH against an FP64 recomputation on the 4096^2 tissue
+    (FP32 J ~ U[2,20], lambda_area 1, lambda_P 0.5, T 20), over every
+    (target, source of another id) pair of the seeded state and of the state
+    after 5 MCS, about 2e7 pairs each.  The error is a few FP32 roundings on
+    the scale of the terms summed (adhesion ~20 per neighbour, constraint
+    terms up to ~1e3 in the seeded state), so it is bounded relative to the
+    sum of the terms' magnitudes, not to dH itself, which can be small after
+    cancellation.  Bounds: 1e-6 of that scale, and no Metropolis probability
+    moved by more than 1e-5.  The figures go to
+    test_reports/dh_fp32_vs_fp64.json."""
+    import json
+    import os
+    import pathlib
+    from gpucpm import workloads as W
+    w = W.tissue_2d()
+    sim = oracle.OracleSim(w.lattice, w.ncells, **w.oracle_kwargs(), seed=3)
+    res = {"seeded": sim.dh_error()}
+    sim.run(5)
+    res["after_5_mcs"] = sim.dh_error()
+    report = pathlib.Path(os.environ.get("CPM_TEST_REPORT_DIR",
+                                         pathlib.Path(__file__).resolve().parents[1] /
+                                         "test_reports"))
+    report.mkdir(exist_ok=True)
+    (report / "dh_fp32_vs_fp64.json").write_text(json.dumps(res, indent=1))
+    for r in res.values():
+        assert r["pairs"] > 10_000_000
+        assert r["max_rel"] < 1e-6, r
+        assert r["max_accept_prob_diff"] < 1e-5, r
