@@ -28,11 +28,18 @@
 //  * Parameters of the one replica are loaded once per launch.
 //
 // Coherence.  Lattice words are written with generic stores and read back by
-// the copy engine (async proxy) in later phases: the issuing lane executes
-// fence.proxy.async after the grid barrier (which orders every SM's writes)
-// and before each copy.  Within a phase every site a tile's attempts read is
-// either one of its own targets or a site of another class, which no attempt
-// of the phase writes, so a copy never races with a store it depends on.
+// the copy engine (async proxy) in later phases: every warp's issuing lane
+// executes fence.proxy.async.global once per phase, after the grid barrier
+// (which orders every SM's writes) and before the phase's first copy.  Within
+// a phase every site a tile's attempts read is either one of its own targets
+// or a site of another class, which no attempt of the phase writes, so a copy
+// never races with a store it depends on (a copied box also holds columns of
+// neighbouring tiles' targets, which the tile never reads).
+//
+// Work split.  Each block sweeps one contiguous band of a slot's tiles, the
+// same band in every phase; its warps claim the band's tiles one at a time
+// from a shared counter, so that the phase ends within about one tile on
+// every warp although tiles differ in how many attempts they evaluate.
 #include <cuda.h>  // CUtensorMap (the map itself is encoded on the host)
 
 #include <algorithm>
@@ -93,10 +100,12 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
 }
 
 // Lane 0: arm the warp's barrier for one tile and start the copy of the box
-// whose top-left lattice site is (x, y).
+// whose top-left lattice site is (x, y).  The shared-memory proxy fence
+// orders the warp's earlier generic reads and writes of the tile buffer
+// before the copy engine's writes into it.
 __device__ __forceinline__ void tma_load_tile(uint32_t dst, uint32_t bar, const CUtensorMap* map,
                                               int x, int y, unsigned bytes) {
-  asm volatile("fence.proxy.async;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
                : "memory");
   asm volatile(
@@ -169,6 +178,7 @@ __global__ void __launch_bounds__(32 * kMaxSweepWarps, 1)
   __shared__ int s_ok;
   __shared__ unsigned s_cnt[2];
   __shared__ unsigned long long s_tick0;
+  __shared__ unsigned s_next[2];  // next unclaimed tile of the band (by phase parity)
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int wpb = blockDim.x >> 5;
@@ -182,6 +192,7 @@ __global__ void __launch_bounds__(32 * kMaxSweepWarps, 1)
   uint32_t bar_parity = 0;
   bool fill_ok = true;  // warp-uniform: false once a tile copy timed out
   if (tid < 2) s_cnt[tid] = 0;
+  if (tid < 2) s_next[tid] = 0;
   if (tid == 0) s_tick0 = a.tick_ptr ? __ldcg(a.tick_ptr) : a.tick0;
   if (lane == 0) {
     mbar_init(bar_s, 1);
@@ -480,18 +491,23 @@ __global__ void __launch_bounds__(32 * kMaxSweepWarps, 1)
       const int per_b = ntiles / (int)gridDim.x, extra = ntiles % (int)gridDim.x;
       const int tb0 = (int)blockIdx.x * per_b + min((int)blockIdx.x, extra);
       const int tb1 = tb0 + per_b + ((int)blockIdx.x < extra ? 1 : 0);
-      int task = tb0 + warp;
-      int tx = task % tnx, ty = task / tnx;
-      for (; task < tb1; task += wpb) {
+      // copies of this phase must see every SM's stores of the last one
+      if (lane == 0 && use_tma) asm volatile("fence.proxy.async.global;" ::: "memory");
+      // warp w starts with the band's tile w, then claims the next unclaimed
+      // one; counter step % 2 serves this phase, the other one (last used
+      // before the previous barrier) is cleared for the next phase
+      unsigned* ctr = &s_next[step & 1];
+      if (tid == 0) s_next[(step + 1) & 1] = 0u;
+      for (int k = warp; k < tb1 - tb0;) {
+        const int task = tb0 + k;
+        const int ty = task / tnx, tx = task - ty * tnx;
         if (cx)
           run_tile(std::integral_constant<int, 1>{}, pt, tx, ty, cy, phase);
         else
           run_tile(std::integral_constant<int, 0>{}, pt, tx, ty, cy, phase);
-        tx += wpb;
-        while (tx >= tnx) {
-          tx -= tnx;
-          ++ty;
-        }
+        unsigned v = 0;
+        if (lane == 0) v = atomicAdd(ctr, 1u);
+        k = wpb + (int)__shfl_sync(kFull, v, 0);
       }
       __syncthreads();
       if (tid == 0) s_cnt[prv] = 0;

@@ -70,7 +70,7 @@ def test_sharded_ensemble_equals_single_process(engine_lib):
     ens = G.Ensemble([_workload()] * (WORLD * R_SHARD), seed=3, stream_id=0)
     want, O_all = _grad(ens, MCS)
     del ens
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:
         out = m.dict()
         mp.start_processes(_worker, args=(WORLD, _free_port(), out), nprocs=WORLD,
                            start_method="spawn")

@@ -52,7 +52,7 @@ def _free_port():
 
 def test_sharded_gradient_equals_single_process():
     world = 2
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:
         out = m.dict()
         mp.start_processes(_worker, args=(world, _free_port(), out), nprocs=world,
                            start_method="spawn")
