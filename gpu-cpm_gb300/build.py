@@ -21,8 +21,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "--fmad=false",
            "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
            f"-I{INCLUDE}", f"-I{CSRC}"]
-SOURCES = ["cpm_engine.cu", "cpm_kernels.cu", "cpm_sweep2d.cu", "cpm_static.cu"]
-HEADERS = ["cpm_internal.h", "cpm_device.cuh", "cpm_sweep_common.cuh"]
+SOURCES = ["cpm_engine.cu", "cpm_kernels.cu", "cpm_sweep2d.cu", "cpm_sweep3d.cu",
+           "cpm_static.cu"]
+HEADERS = ["cpm_internal.h", "cpm_device.cuh", "cpm_sweep_common.cuh", "cpm_rowtile.cuh"]
 
 
 def _nvcc() -> str:

@@ -115,8 +115,8 @@ struct cpm_handle {
   } cfg[kTileVariants];
   int variant = 0;
   int dispatch = CPM_DISPATCH_GRID;  // CPM_DISPATCH_*
-  // 2D single lattices whose width is a multiple of 4 run the row-tile sweep
-  // (cpm_sweep2d.cu).  fill: CPM_FILL_PARITY = the parity-split sweep_kernel,
+  // Single lattices whose width is a multiple of 4 run the row-tile sweeps
+  // (cpm_sweep2d.cu, cpm_sweep3d.cu).  fill: CPM_FILL_PARITY = the parity-split sweep_kernel,
   // CPM_FILL_VECTOR = row tiles staged with 16-byte loads, CPM_FILL_TMA = row
   // tiles whose interior tiles are copied by the tensor-map engine (the
   // default where the maps could be encoded).
@@ -211,9 +211,9 @@ void free_all(cpm_handle* h) {
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
 }
 
-// Tensor maps of a single 2D lattice for the row-tile sweep: the lattice as a
-// ny x nx array of 32-bit words, one box of 72 x (2 CY + 1) words per tile
-// variant.  cuTensorMapEncodeTiled is reached through the runtime's driver
+// Tensor maps of a single lattice for the row-tile sweeps: the lattice as a
+// ny x nx (nz x ny x nx) array of 32-bit words, one box of 72 x (2 CY + 1)
+// (x (2 CZ + 1)) words per tile variant.  cuTensorMapEncodeTiled is reached through the runtime's driver
 // entry point, so the library does not link the driver library itself.
 // False (and no maps) when the entry point or the encoding is unavailable.
 bool encode_tile_maps(cpm_handle* h) {
@@ -230,12 +230,18 @@ bool encode_tile_maps(cpm_handle* h) {
   if (!encode) return false;
   const DevReplica& R = h->reps[0];
   for (int v = 0; v < kTileVariants; ++v) {
-    const cuuint64_t dims[2] = {(cuuint64_t)R.nx, (cuuint64_t)R.ny};
-    const cuuint64_t strides[1] = {(cuuint64_t)R.nx * 4};
-    const cuuint32_t box[2] = {72u, (cuuint32_t)row_tile_rows(v)};
-    const cuuint32_t estr[2] = {1u, 1u};
+    const cuuint64_t dims[3] = {(cuuint64_t)R.nx, (cuuint64_t)R.ny, (cuuint64_t)R.nz};
+    const cuuint64_t strides[2] = {(cuuint64_t)R.nx * 4, (cuuint64_t)R.nx * R.ny * 4};
+    cuuint32_t box[3] = {72u, (cuuint32_t)row_tile_rows(v), 1u};
+    if (h->ndim == 3) {
+      int rows = 0, planes = 0;
+      box_tile_extent(v, &rows, &planes);
+      box[1] = (cuuint32_t)rows;
+      box[2] = (cuuint32_t)planes;
+    }
+    const cuuint32_t estr[3] = {1u, 1u, 1u};
     if (encode(reinterpret_cast<CUtensorMap*>(h->tmap[v].bytes), CU_TENSOR_MAP_DATA_TYPE_UINT32,
-               2, h->d_lat + R.lat_off, dims, strides, box, estr,
+               (cuuint32_t)h->ndim, h->d_lat + R.lat_off, dims, strides, box, estr,
                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
@@ -352,7 +358,7 @@ int build_engine(int n, int ndim, const int* nx, const int* ny, const int* nz,
     return e == cudaErrorMemoryAllocation ? CPM_ERR_ALLOC : CPM_ERR_CUDA;
   }
   std::memset(h->h_lat, 0, sizeof(uint32_t) * sites);
-  if (n == 1 && ndim == 2 && row_tiles_fit(nx[0], ny[0])) {
+  if (n == 1 && (ndim == 2 ? row_tiles_fit(nx[0], ny[0]) : box_tiles_fit(nx[0], ny[0], nz[0]))) {
     h->row_ok = true;
     h->tma_ok = encode_tile_maps(h);
     h->fill = h->tma_ok ? CPM_FILL_TMA : CPM_FILL_VECTOR;
@@ -800,8 +806,9 @@ cudaError_t enqueue_sweep(const cpm_handle* h, int v, int d, const SweepArgs& a,
                      !h->persist_active && x.nrep == 1 && x.rep_map == nullptr &&
                      !x.block_local;
     if (e == cudaSuccess && row)
-      e = launch_sweep2d(perim, v, x, h->tmap[v].bytes, h->fill == CPM_FILL_TMA ? 1 : 0, grid,
-                         c.shape.warps, h->stream);
+      e = (h->ndim == 2 ? launch_sweep2d : launch_sweep3d)(
+          perim, v, x, h->tmap[v].bytes, h->fill == CPM_FILL_TMA ? 1 : 0, grid, c.shape.warps,
+          h->stream);
     else if (e == cudaSuccess)
       e = launch_sweep(h->ndim, perim, v, x, grid, h->stream, scores);
     if (e == cudaSuccess) ++*nlaunch;
@@ -1759,8 +1766,8 @@ int cpm_set_fill(cpm_handle* h, int fill) {
   if (fill != CPM_FILL_PARITY && fill != CPM_FILL_VECTOR && fill != CPM_FILL_TMA)
     return h->fail(CPM_ERR_INVALID, "fill %d is not parity (0), vector (1) or tma (2)", fill);
   if (fill != CPM_FILL_PARITY && !h->row_ok)
-    return h->fail(CPM_ERR_UNSUPPORTED, "row tiles need one 2D lattice with nx a multiple of "
-                                        "4, nx >= 72 and ny >= 66");
+    return h->fail(CPM_ERR_UNSUPPORTED, "row tiles need one lattice with nx a multiple of 4 "
+                                        "and nx >= 72; in 2D ny >= 66, in 3D ny, nz >= 18");
   if (fill == CPM_FILL_TMA && !h->tma_ok)
     return h->fail(CPM_ERR_UNSUPPORTED, "the tensor maps of this lattice could not be encoded");
   h->fill = fill;

@@ -265,6 +265,11 @@ cudaError_t launch_sweep2d(bool perim, int variant, const SweepArgs& a, const vo
                            int use_tma, int grid, int warps_cap, cudaStream_t s);
 bool row_tiles_fit(int nx, int ny);
 int row_tile_rows(int variant);
+// The 3D row-tile sweep (cpm_sweep3d.cu): boxes of 72 x rows x planes words.
+cudaError_t launch_sweep3d(bool perim, int variant, const SweepArgs& a, const void* tmap,
+                           int use_tma, int grid, int warps_cap, cudaStream_t s);
+bool box_tiles_fit(int nx, int ny, int nz);
+void box_tile_extent(int variant, int* rows, int* planes);
 int sweep_max_blocks_per_sm(int ndim, bool perim, int variant, bool scores = false);
 // checkpoints: host array of ncheck (<= kMaxCheckpoints) MCS counts.
 cudaError_t launch_lr_backward(const float* scores, const float* dl_do,

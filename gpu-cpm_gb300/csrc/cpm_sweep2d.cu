@@ -47,13 +47,11 @@
 #include <cstring>
 #include <type_traits>
 
+#include "cpm_rowtile.cuh"
 #include "cpm_sweep_common.cuh"
 
 namespace gpucpm {
 namespace {
-
-constexpr int kPitch = 72;              // words per staged row
-constexpr int kVecPerRow = kPitch / 4;  // 16-byte vectors per staged row
 
 template <int CY>
 struct RowTile {
@@ -77,75 +75,6 @@ template <int CY>
 constexpr int row_tile_warps(int cap) {
   const int w = (int)(kSweepSmemMax / sizeof(Warp2Smem<CY>));
   return w < cap ? w : cap;
-}
-
-__device__ __forceinline__ uint32_t smem_addr(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// Lane 0: arm the warp's barrier for one tile and start the copy of the box
-// whose top-left lattice site is (x, y).  The shared-memory proxy fence
-// orders the warp's earlier generic reads and writes of the tile buffer
-// before the copy engine's writes into it.
-__device__ __forceinline__ void tma_load_tile(uint32_t dst, uint32_t bar, const CUtensorMap* map,
-                                              int x, int y, unsigned bytes) {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
-               : "memory");
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
-      : "memory");
-}
-
-// Waits for the copy that completes phase `parity` of the barrier, bounded
-// by the sweep's barrier timeout; false (and kErrTimeout) if it ran out.
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, int* err) {
-  if (mbar_try_wait(bar, parity)) return true;
-  const unsigned long long t0 = global_timer_ns();
-  for (unsigned spins = 1;; ++spins) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if ((spins & 63u) == 0 && global_timer_ns() - t0 > kBarrierTimeoutNs) {
-      atomicOr(err, kErrTimeout);
-      return false;
-    }
-  }
-}
-
-// The three sites of staged row `row` around target column qx of parity PAR
-// (left, centre, right), from two 8-byte loads.
-template <int PAR>
-__device__ __forceinline__ void row3(const uint32_t* tile, int row, int qx, uint32_t& l,
-                                     uint32_t& c, uint32_t& r) {
-  const uint32_t* p = tile + row * kPitch + 2 * qx + 2 + 2 * PAR;
-  const uint2 A = *reinterpret_cast<const uint2*>(p);
-  const uint2 B = *reinterpret_cast<const uint2*>(p + 2);
-  if (PAR) {
-    l = A.x;
-    c = A.y;
-    r = B.x;
-  } else {
-    l = A.y;
-    c = B.x;
-    r = B.y;
-  }
 }
 
 // Target (qx, qy) and its Moore neighbours in (dy, dx) lexicographic order.

@@ -323,7 +323,7 @@ int cpm_sweep_config(const cpm_handle* h, int* variant, int* tile_x,
                      int* tile_y, int* tile_z, int* warps_per_block,
                      int* grid, int* dispatch);
 
-/* How warp tiles reach shared memory in the sweep of one 2D lattice.  No
+/* How warp tiles reach shared memory in the sweep of one lattice.  No
  * counterpart in the reference (its tile load is src/kernels2d.cu:109-176).
  *   CPM_FILL_PARITY  the general sweep: scalar loads, even and odd columns
  *                    in separate halves of the tile
@@ -331,9 +331,10 @@ int cpm_sweep_config(const cpm_handle* h, int* variant, int* tile_x,
  *   CPM_FILL_TMA     row-major tiles, interior tiles copied by the tensor
  *                    memory accelerator (cp.async.bulk.tensor), tiles on the
  *                    periodic seam from vector loads
- * Row-major tiles need a single 2D lattice with nx a multiple of 4,
- * nx >= 72 and ny >= 66; such lattices start in CPM_FILL_TMA (CPM_FILL_VECTOR
- * where the tensor maps cannot be encoded), all others in CPM_FILL_PARITY.
+ * Row-major tiles need a single lattice with nx a multiple of 4 and
+ * nx >= 72 (in 2D ny >= 66, in 3D ny >= 18 and nz >= 18); such lattices start
+ * in CPM_FILL_TMA (CPM_FILL_VECTOR where the tensor maps cannot be encoded),
+ * all others in CPM_FILL_PARITY.
  * The result does not depend on the fill: it selects the kernel only
  * (CPM_ERR_UNSUPPORTED for a fill the lattice cannot use). */
 #define CPM_FILL_PARITY 0

@@ -1,14 +1,15 @@
-"""The row-tile sweep of single 2D lattices (cpm_sweep2d.cu) against the
-oracle, bit for bit, under each way of staging tiles:
+"""The row-tile sweeps of single lattices (cpm_sweep2d.cu, cpm_sweep3d.cu)
+against the oracle, bit for bit, under each way of staging tiles:
 
   parity  the general sweep_kernel (scalar loads, parity-split tiles)
   vector  row-major tiles from 16-byte vector loads
   tma     row-major tiles, interior tiles copied by cp.async.bulk.tensor
 
 Shapes cover partial tiles in x (nx = 76: 38 target columns, a full and a
-6-wide tile), an odd height (a one-row slot of the last row class), every
-tile variant, and the periodic seam on all four sides; terms cover the
-perimeter, stickiness, a fixed type and a chemotaxis field.  Graph-captured
+6-wide tile), odd heights and depths (one-row or one-plane slots of the last
+class), every tile variant in 2D and 3D, and the periodic seam on every
+side; terms cover the perimeter, stickiness, a fixed type and a chemotaxis
+field.  Graph-captured
 runs and plain runs agree."""
 import numpy as np
 import pytest
@@ -35,9 +36,15 @@ def _terms(w, seed):
     w.stick[1, 2], w.stick[2, 1], w.stick[1, 0] = g.integers(1, 6, 3).astype(np.float32)
     w.fixed = np.zeros(nt, bool)
     w.fixed[nt - 1] = True
-    ny, nx = w.lattice.shape
-    yy, xx = np.mgrid[0:ny, 0:nx]
-    w.field = np.stack([np.sin(2 * np.pi * yy / ny) * 3.0, np.cos(2 * np.pi * xx / nx)])
+    if w.ndim == 2:
+        ny, nx = w.lattice.shape
+        yy, xx = np.mgrid[0:ny, 0:nx]
+        w.field = np.stack([np.sin(2 * np.pi * yy / ny) * 3.0, np.cos(2 * np.pi * xx / nx)])
+    else:
+        nz, ny, nx = w.lattice.shape
+        zz, yy, xx = np.mgrid[0:nz, 0:ny, 0:nx]
+        w.field = np.stack([np.sin(2 * np.pi * yy / ny) * 3.0, np.cos(2 * np.pi * xx / nx),
+                            np.sin(2 * np.pi * zz / nz) * 1.5])
     w.chemo = np.zeros(nt, np.float32)
     w.chemo[1] = 2.5
     return w
@@ -50,6 +57,10 @@ def _terms(w, seed):
     ((130, 144), 120, 1, True, 10),    # 32 x 8 tiles
     ((132, 200), 150, 2, False, 10),   # 32 x 16 tiles
     ((96, 72), 50, 3, True, 20),       # one-row tiles, nx = one staged row
+    ((18, 20, 72), 60, 0, True, 6),    # 3D, 32 x 2 x 2 tiles, every term
+    ((19, 21, 76), 60, 1, False, 5),   # 3D, odd ny and nz, partial x tiles
+    ((20, 18, 80), 50, 2, True, 4),    # 3D, 32 x 4 x 4 tiles
+    ((18, 19, 72), 40, 3, False, 6),   # 3D, one-row tiles
 ])
 def test_row_tiles_match_oracle(engine_lib, fill, shape, ncells, variant, terms, mcs):
     w = W.random_small(shape, ncells, ntypes=3, seed=500 + ncells, temperature=9.0)
