@@ -568,7 +568,9 @@ def run_ours(args, world, rank, local, emit=True):
                 "frac": achieved / peak, "peak_source": f"{peak_kind} HBM copy (burst)",
                 "traffic": tpa * attempts_per_launch if tpa is not None else None,
                 "algorithmic_bytes_per_launch": BYTES_PER_ATTEMPT * attempts_per_launch,
-                "kernel": "sweep_kernel (one cooperative launch per step)"}
+                "kernel": (("sweep2d_kernel" if w.ndim == 2 else "sweep3d_kernel")
+                           if sim.sweep_config()["fill"] != "parity" else "sweep_kernel")
+                          + " (one cooperative launch per step)"}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
