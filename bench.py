@@ -67,7 +67,7 @@ def parse_args():
     p.add_argument("--variant", type=int, default=None,
                    help="tile variant instead of the autotuner's choice (profiling runs: "
                         "timing under a profiler can change the tuner's pick)")
-    p.add_argument("--fill", choices=["parity", "vector", "tma"], default=None,
+    p.add_argument("--fill", choices=["parity", "vector", "tma", "cluster"], default=None,
                    help="single 2D lattices: how tiles are staged instead of the engine's "
                         "default (see cpm_set_fill)")
     p.add_argument("--dispatch", choices=["grid", "replica", "hybrid"], default=None,
@@ -492,7 +492,7 @@ def run_ours(args, world, rank, local, emit=True):
         sim.set_variant(args.variant)
     if getattr(args, "fill", None):
         sim.set_fill({"parity": gpucpm.FILL_PARITY, "vector": gpucpm.FILL_VECTOR,
-                      "tma": gpucpm.FILL_TMA}[args.fill])
+                      "tma": gpucpm.FILL_TMA, "cluster": gpucpm.FILL_CLUSTER}[args.fill])
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
 
     for _ in range(args.warmup):
@@ -503,6 +503,9 @@ def run_ours(args, world, rank, local, emit=True):
     if args.variant is None:
         warm_gpu()
         variant, tuned_ms = sim.autotune(probe_mcs=8)
+        if getattr(args, "fill", None):  # a pinned fill stays pinned
+            sim.set_fill({"parity": gpucpm.FILL_PARITY, "vector": gpucpm.FILL_VECTOR,
+                          "tma": gpucpm.FILL_TMA, "cluster": gpucpm.FILL_CLUSTER}[args.fill])
     else:
         variant, tuned_ms = args.variant, None
     sim.synchronize()
@@ -568,9 +571,12 @@ def run_ours(args, world, rank, local, emit=True):
                 "frac": achieved / peak, "peak_source": f"{peak_kind} HBM copy (burst)",
                 "traffic": tpa * attempts_per_launch if tpa is not None else None,
                 "algorithmic_bytes_per_launch": BYTES_PER_ATTEMPT * attempts_per_launch,
-                "kernel": (("sweep2d_kernel" if w.ndim == 2 else "sweep3d_kernel")
-                           if sim.sweep_config()["fill"] != "parity" else "sweep_kernel")
-                          + " (one cooperative launch per step)"}
+                "kernel": {"parity": "sweep_kernel (one cooperative launch per step)",
+                           "cluster": "sweep2d_kernel, cluster mode (one launch of one "
+                                      "thread-block cluster per step)"}.get(
+                    sim.sweep_config()["fill"],
+                    ("sweep2d_kernel" if w.ndim == 2 else "sweep3d_kernel")
+                    + " (one cooperative launch per step)")}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -582,7 +588,8 @@ def run_ours(args, world, rank, local, emit=True):
                                              local),
             "e2e": e2e,
             "autotune": {"variant": variant, "probe_ms_per_mcs": tuned_ms,
-                         "dispatch": sim.sweep_config()["dispatch"]},
+                         "dispatch": sim.sweep_config()["dispatch"],
+                         "fill": sim.sweep_config()["fill"]},
             "gpu_launches": int(launches), "clocks": clocks,
             "mcs_per_s": value / w.nsites / world,
             "wall_s": wall, "step_ms": step_ms}

@@ -122,6 +122,11 @@ struct cpm_handle {
   // default where the maps could be encoded).
   int fill = CPM_FILL_PARITY;
   bool row_ok = false, tma_ok = false;
+  // CPM_FILL_CLUSTER: small 2D lattices swept by one thread-block cluster of
+  // cl_G blocks, cl_H rows each, dirty lists of cl_cap entries per block
+  bool cluster_ok = false;
+  int cl_G = 0, cl_H = 0;
+  long long cl_cap = 0;
   struct alignas(64) TileMap {
     unsigned char bytes[128];  // CUtensorMap of the lattice, box of one variant
   } tmap[kTileVariants];
@@ -362,6 +367,8 @@ int build_engine(int n, int ndim, const int* nx, const int* ny, const int* nz,
     h->row_ok = true;
     h->tma_ok = encode_tile_maps(h);
     h->fill = h->tma_ok ? CPM_FILL_TMA : CPM_FILL_VECTOR;
+    if (ndim == 2)
+      h->cluster_ok = cluster_sweep_plan(nx[0], ny[0], &h->cl_G, &h->cl_H, &h->cl_cap);
   }
 
   // One launch configuration per tile variant: warp tiles per slot and
@@ -805,7 +812,12 @@ cudaError_t enqueue_sweep(const cpm_handle* h, int v, int d, const SweepArgs& a,
     const bool row = h->fill != CPM_FILL_PARITY && h->row_ok && !scores && !h->act_active &&
                      !h->persist_active && x.nrep == 1 && x.rep_map == nullptr &&
                      !x.block_local;
-    if (e == cudaSuccess && row)
+    if (e == cudaSuccess && row && h->fill == CPM_FILL_CLUSTER) {
+      SweepArgs xc = x;
+      xc.list_cap = h->cl_cap;
+      e = launch_sweep2d_cluster(perim, v, xc, h->tmap[3].bytes, h->reps[0].nx, h->cl_G,
+                                 h->cl_H, h->stream);
+    } else if (e == cudaSuccess && row)
       e = (h->ndim == 2 ? launch_sweep2d : launch_sweep3d)(
           perim, v, x, h->tmap[v].bytes, h->fill == CPM_FILL_TMA ? 1 : 0, grid, c.shape.warps,
           h->stream);
@@ -1447,9 +1459,21 @@ int cpm_autotune(cpm_handle* h, int probe_mcs, int* chosen, float* ms_per_mcs) {
     for (int v = 0; v < kTileVariants; ++v)
       if (d != CPM_DISPATCH_HYBRID || (h->cfg[v].hyb_ng > 0 && h->cfg[v].hyb_ng < h->nrep))
         pairs.emplace_back(v, d);
+  // A lattice that one thread-block cluster can hold is also tried in the
+  // cluster sweep (every one of its tile heights), unless the caller chose
+  // the parity-split sweep.
+  const int row_fill = h->fill == CPM_FILL_CLUSTER ? (h->tma_ok ? CPM_FILL_TMA : CPM_FILL_VECTOR)
+                                                   : h->fill;
+  const bool try_cluster = h->cluster_ok && h->fill != CPM_FILL_PARITY;
+  if (try_cluster)
+    for (int v = 0; v < kTileVariants; ++v) pairs.emplace_back(v, -1);
+  int best_fill = row_fill;
   const int npairs = (int)pairs.size();
   for (int i = 0; i < 3 * npairs && e == cudaSuccess; ++i) {
-    const int v = pairs[i % npairs].first, d = pairs[i % npairs].second;
+    const int v = pairs[i % npairs].first;
+    const bool cl = pairs[i % npairs].second < 0;
+    const int d = cl ? CPM_DISPATCH_GRID : pairs[i % npairs].second;
+    h->fill = cl ? CPM_FILL_CLUSTER : row_fill;
     SweepArgs a = sweep_args(h, v, d);
     a.tick0 = tick;
     a.mcs = probe_mcs;
@@ -1466,8 +1490,10 @@ int cpm_autotune(cpm_handle* h, int probe_mcs, int* chosen, float* ms_per_mcs) {
       best = ms;
       best_v = v;
       best_d = d;
+      best_fill = h->fill;
     }
   }
+  h->fill = best_fill;
   if (e == cudaSuccess) e = copy(false);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
   cudaFree(save);
@@ -1763,8 +1789,14 @@ int cpm_set_variant(cpm_handle* h, int variant) {
 
 int cpm_set_fill(cpm_handle* h, int fill) {
   if (!h) return CPM_ERR_INVALID;
-  if (fill != CPM_FILL_PARITY && fill != CPM_FILL_VECTOR && fill != CPM_FILL_TMA)
-    return h->fail(CPM_ERR_INVALID, "fill %d is not parity (0), vector (1) or tma (2)", fill);
+  if (fill != CPM_FILL_PARITY && fill != CPM_FILL_VECTOR && fill != CPM_FILL_TMA &&
+      fill != CPM_FILL_CLUSTER)
+    return h->fail(CPM_ERR_INVALID, "fill %d is not parity (0), vector (1), tma (2) or "
+                                    "cluster (3)", fill);
+  if (fill == CPM_FILL_CLUSTER && !h->cluster_ok)
+    return h->fail(CPM_ERR_UNSUPPORTED, "no thread-block cluster holds this lattice (one 2D "
+                                        "lattice that fits row tiles and ~190 KB of rows per "
+                                        "block of a 16- or 8-block cluster)");
   if (fill != CPM_FILL_PARITY && !h->row_ok)
     return h->fail(CPM_ERR_UNSUPPORTED, "row tiles need one lattice with nx a multiple of 4 "
                                         "and nx >= 72; in 2D ny >= 66, in 3D ny, nz >= 18");
@@ -1943,6 +1975,11 @@ int cpm_sweep_config(const cpm_handle* h, int* variant, int* tile_x, int* tile_y
   if (warps_per_block) *warps_per_block = c.shape.warps;
   if (grid) *grid = grid_of(h, h->variant, h->dispatch);
   if (dispatch) *dispatch = h->dispatch;
+  if (h->fill == CPM_FILL_CLUSTER) {  // one cluster, its own tile heights
+    if (tile_y) *tile_y = cluster_tile_rows(h->variant);
+    if (tile_z) *tile_z = 1;
+    if (grid) *grid = h->cl_G;
+  }
   return CPM_OK;
 }
 

@@ -265,6 +265,14 @@ cudaError_t launch_sweep2d(bool perim, int variant, const SweepArgs& a, const vo
                            int use_tma, int grid, int warps_cap, cudaStream_t s);
 bool row_tiles_fit(int nx, int ny);
 int row_tile_rows(int variant);
+// Cluster mode of the 2D row-tile sweep (small single lattices): plan (G
+// blocks of one cluster, H rows per block, dirty-list entries per block)
+// and launch.  The plan is false where no cluster of that shape fits.
+bool cluster_sweep_plan(int nx, int ny, int* G, int* H, long long* list_cap);
+cudaError_t launch_sweep2d_cluster(bool perim, int variant, const SweepArgs& a, const void* tmap,
+                                   int nx, int G, int H, cudaStream_t s);
+// Target rows per tile of the cluster sweep's variants.
+int cluster_tile_rows(int variant);
 // The 3D row-tile sweep (cpm_sweep3d.cu): boxes of 72 x rows x planes words.
 cudaError_t launch_sweep3d(bool perim, int variant, const SweepArgs& a, const void* tmap,
                            int use_tma, int grid, int warps_cap, cudaStream_t s);

@@ -40,6 +40,19 @@
 // same band in every phase; its warps claim the band's tiles one at a time
 // from a shared counter, so that the phase ends within about one tile on
 // every warp although tiles differ in how many attempts they evaluate.
+//
+// Cluster mode (CLU, one-row tiles).  A small lattice is swept by one
+// thread-block cluster of G blocks instead of the whole grid: block r keeps
+// lattice rows [r H, r H + H) in its own shared memory for the whole launch,
+// stages tiles from the strips (rows of other blocks through distributed
+// shared memory), writes its targets (always its own rows) in place, keeps
+// its dirty lists in shared memory, and the phases end at the cluster's
+// hardware barrier (barrier.cluster, release / acquire at cluster scope)
+// instead of the grid barrier in global memory.  The cell tables stay in
+// global memory with the same double buffering.  Neighbour rows read from
+// another block in a phase are of the other row class, which no attempt of
+// the phase writes.
+#include <cooperative_groups.h>
 #include <cuda.h>  // CUtensorMap (the map itself is encoded on the host)
 
 #include <algorithm>
@@ -97,10 +110,18 @@ __device__ __forceinline__ int nb_off(int k) {
   return (m / 3 - 1) * kPitch + (m % 3 - 1);
 }
 
-template <bool PERIM, int CY>
-__global__ void __launch_bounds__(32 * kMaxSweepWarps, 1)
+// Warps per block of the cluster sweep by tile height: one one-row tile per
+// warp covers the 1,024 targets a block of a 16-block cluster has per phase
+// on 256^2; taller tiles need fewer warps, which then get more registers.
+// One more warp replays the dirty list while the others work their tiles.
+__host__ __device__ constexpr int cluster_warps(int cy) {
+  return (cy == 1 ? 31 : (cy == 8 ? 8 : 16)) + 1;  // + the replay warp (1,024 threads at most)
+}
+
+template <bool PERIM, int CY, bool CLU = false>
+__global__ void __launch_bounds__(32 * (CLU ? cluster_warps(CY) : kMaxSweepWarps), 1)
     sweep2d_kernel(const __grid_constant__ SweepArgs a, const __grid_constant__ CUtensorMap tmap,
-                   const int use_tma) {
+                   const int use_tma, const int strip_rows) {
   using RT = RowTile<CY>;
   constexpr unsigned long long NSLOTS = 9;
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -111,11 +132,21 @@ __global__ void __launch_bounds__(32 * kMaxSweepWarps, 1)
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int wpb = blockDim.x >> 5;
-  Warp2Smem<CY>& ws = reinterpret_cast<Warp2Smem<CY>*>(smem_raw)[warp];
+  // (cluster mode) this block's strip of rows leads the dynamic shared memory
+  const int strip_words = CLU ? (strip_rows * __ldg(&a.reps[0].nx) + 31) & ~31 : 0;
+  uint32_t* const strip = reinterpret_cast<uint32_t*>(smem_raw);
+  Warp2Smem<CY>& ws =
+      reinterpret_cast<Warp2Smem<CY>*>(smem_raw + 4 * (size_t)strip_words)[warp];
+  // (cluster mode) the block's two dirty lists follow the warp areas
+  uint32_t* const slist = reinterpret_cast<uint32_t*>(
+      smem_raw + 4 * (size_t)strip_words + sizeof(Warp2Smem<CY>) * (size_t)wpb);
   const uint32_t tile_s = smem_addr(ws.tile), bar_s = smem_addr(&ws.bar);
   const uint32_t k0 = (uint32_t)a.seed, k1 = (uint32_t)(a.seed >> 32);
   int* err = reinterpret_cast<int*>(&a.ctl[kCtlErr]);
-  auto blist = [&](int b) { return a.dlist + (2LL * blockIdx.x + b) * a.list_cap; };
+  auto blist = [&](int b) {
+    return CLU ? slist + (long long)b * a.list_cap
+               : a.dlist + (2LL * blockIdx.x + b) * a.list_cap;
+  };
   unsigned episode = 0;
   unsigned long long n_eval = 0, n_acc = 0;  // warp-uniform
   uint32_t bar_parity = 0;
@@ -143,6 +174,19 @@ __global__ void __launch_bounds__(32 * kMaxSweepWarps, 1)
   const long long cell_off = __ldg(&a.reps[0].cell_off);
   uint32_t* L = a.lat + lat_off;
 
+  // Cluster mode: load this block's rows, then meet the other blocks so that
+  // every strip is in place before any block reads it.
+  cooperative_groups::cluster_group cluster = cooperative_groups::this_cluster();
+  const int crank = CLU ? (int)cluster.block_rank() : 0;
+  const int row0 = crank * strip_rows;
+  const int row1 = CLU ? min(ny, row0 + strip_rows) : 0;
+  if constexpr (CLU) {
+    const int nvec = row0 < row1 ? (row1 - row0) * (nx / 4) : 0;
+    const uint4* src = reinterpret_cast<const uint4*>(L + (long long)row0 * nx);
+    for (int v = tid; v < nvec; v += blockDim.x) reinterpret_cast<uint4*>(strip)[v] = __ldcg(src + v);
+    cluster.sync();
+  }
+
   auto tables = [&](int cur) {
     PhaseTables<2> pt;
     pt.rap = cur ? a.ap[1] : a.ap[0];
@@ -157,13 +201,30 @@ __global__ void __launch_bounds__(32 * kMaxSweepWarps, 1)
   };
   auto replay_phase = [&](int prv) {
     const unsigned n = min(s_cnt[prv], (unsigned)a.list_cap);  // see kErrListFull
-    replay<2>(blist(prv), n, prv ? a.dap[1] : a.dap[0], prv ? a.dcs[1] : a.dcs[0],
-              prv ? a.ap[1] : a.ap[0], prv ? a.cs[1] : a.cs[0]);
+    replay<2, CLU>(blist(prv), n, prv ? a.dap[1] : a.dap[0], prv ? a.dcs[1] : a.dcs[0],
+                   prv ? a.ap[1] : a.ap[0], prv ? a.cs[1] : a.cs[0]);
   };
 
   // Stage tile (tx, ty) of slot (cx, cy): 72 x SR words from lattice column
   // 64 tx - 4 and row yorig.
   auto stage = [&](int X0, int yorig) {
+    if constexpr (CLU) {
+      // from the strips: rows of other blocks through distributed shared memory
+      for (int v = lane; v < RT::SR * kVecPerRow; v += 32) {
+        const int row = v / kVecPerRow, col = v - row * kVecPerRow;
+        int gy = yorig + row;
+        gy = gy < 0 ? gy + ny : (gy >= ny ? gy - ny : gy);
+        int gx = X0 + 4 * col;
+        gx = gx < 0 ? gx + nx : (gx >= nx ? gx - nx : gx);
+        const int owner = gy / strip_rows;
+        const uint32_t* rs =
+            cluster.map_shared_rank(strip, owner) + (gy - owner * strip_rows) * nx + gx;
+        *reinterpret_cast<uint4*>(ws.tile + row * kPitch + 4 * col) =
+            *reinterpret_cast<const uint4*>(rs);
+      }
+      __syncwarp();
+      return;
+    }
     const bool interior =
         use_tma && X0 >= 0 && X0 + kPitch <= nx && yorig >= 0 && yorig + RT::SR <= ny;
     if (interior) {
@@ -186,12 +247,16 @@ __global__ void __launch_bounds__(32 * kMaxSweepWarps, 1)
   };
 
   // One warp tile, column parity PAR (= cx).
-  auto run_tile = [&](auto par, const PhaseTables<2>& pt, const int tx, const int ty,
+  // Tile (tx, target rows j0 ...) of slot (cx, cy); rows at and beyond jend
+  // belong to another tile row (the slot's end, or another block's strip in
+  // cluster mode).
+  auto run_tile = [&](auto par, const PhaseTables<2>& pt, const int tx, const int j0,
+                      const int jend,
                       const int cy, const unsigned long long phase) {
     constexpr int PAR = decltype(par)::value;
-    const int ncx = nx >> 1, ncy = class_count(ny, cy);
-    const int i0 = tx * 32, j0 = ty * CY;
-    const int cntx = min(32, ncx - i0), cnty = min(CY, ncy - j0);
+    const int ncx = nx >> 1;
+    const int i0 = tx * 32;
+    const int cntx = min(32, ncx - i0), cnty = min(CY, jend - j0);
     const int X0 = 2 * i0 - 4;
     const int yorig = class_coord(ny, cy, j0) - 1;
     stage(X0, yorig);
@@ -357,7 +422,10 @@ __global__ void __launch_bounds__(32 * kMaxSweepWarps, 1)
           }
           if (ok) {
             accepted = true;
-            L[(long long)y * nx + x] = s;
+            if constexpr (CLU)
+              strip[(y - row0) * nx + x] = s;  // targets lie in this block's rows
+            else
+              L[(long long)y * nx + x] = s;
             const int crd[2] = {x, y};
             const int dim[2] = {nx, ny};
             long long img[2];
@@ -407,7 +475,20 @@ __global__ void __launch_bounds__(32 * kMaxSweepWarps, 1)
     for (int si = 0; si < a.nslot_active; ++si, ++step) {
       const int cur = step & 1, prv = cur ^ 1;
       const PhaseTables<2> pt = tables(cur);
-      if (step > 0) replay_phase(prv);
+      // (cluster mode: the block's last warp replays while the others work
+      // their tiles; the replay touches only the copy this phase does not
+      // read, through atomics that commute with the phase's own)
+      const int tile_warps = CLU ? wpb - 1 : wpb;
+      if (step > 0) {
+        if (!CLU) {
+          replay_phase(prv);
+        } else if (warp == wpb - 1) {
+          const unsigned n = min(s_cnt[prv], (unsigned)a.list_cap);
+          replay_lanes<2, true>(blist(prv), n, prv ? a.dap[1] : a.dap[0],
+                                prv ? a.dcs[1] : a.dcs[0], prv ? a.ap[1] : a.ap[0],
+                                prv ? a.cs[1] : a.cs[0], lane, 32);
+        }
+      }
       const int slot = a.slots[si];
       const int cx = slot % 3, cy = (slot / 3) % 3;
       const unsigned long long phase = tick * NSLOTS + (unsigned long long)slot;
@@ -416,31 +497,53 @@ __global__ void __launch_bounds__(32 * kMaxSweepWarps, 1)
       const int tny = (class_count(ny, cy) + CY - 1) / CY;
       const int ntiles = tnx * tny;
       // each block sweeps one contiguous band of tile rows, the same in
-      // every phase; its warps take the band's tiles in turn
-      const int per_b = ntiles / (int)gridDim.x, extra = ntiles % (int)gridDim.x;
-      const int tb0 = (int)blockIdx.x * per_b + min((int)blockIdx.x, extra);
-      const int tb1 = tb0 + per_b + ((int)blockIdx.x < extra ? 1 : 0);
+      // every phase; its warps take the band's tiles in turn.  In cluster
+      // mode the band is the tile rows whose targets lie in the block's rows.
+      const int ncy = class_count(ny, cy);
+      int tb0, tb1, jlo = 0, jhi = 0;
+      if constexpr (CLU) {
+        if (cy < 2) {
+          jlo = (row0 - cy + 1) / 2;
+          jhi = min(ncy, (row1 - cy + 1) / 2);
+        } else if ((ny - 1) >= row0 && (ny - 1) < row1) {
+          jhi = 1;
+        }
+        tb0 = 0;
+        tb1 = jhi > jlo ? tnx * ((jhi - jlo + CY - 1) / CY) : 0;
+      } else {
+        const int per_b = ntiles / (int)gridDim.x, extra = ntiles % (int)gridDim.x;
+        tb0 = (int)blockIdx.x * per_b + min((int)blockIdx.x, extra);
+        tb1 = tb0 + per_b + ((int)blockIdx.x < extra ? 1 : 0);
+      }
       // copies of this phase must see every SM's stores of the last one
-      if (lane == 0 && use_tma) asm volatile("fence.proxy.async.global;" ::: "memory");
+      if (!CLU && lane == 0 && use_tma) asm volatile("fence.proxy.async.global;" ::: "memory");
       // warp w starts with the band's tile w, then claims the next unclaimed
       // one; counter step % 2 serves this phase, the other one (last used
       // before the previous barrier) is cleared for the next phase
       unsigned* ctr = &s_next[step & 1];
       if (tid == 0) s_next[(step + 1) & 1] = 0u;
-      for (int k = warp; k < tb1 - tb0;) {
+      for (int k = warp; warp < tile_warps && k < tb1 - tb0;) {
         const int task = tb0 + k;
         const int ty = task / tnx, tx = task - ty * tnx;
+        const int j0 = CLU ? jlo + ty * CY : ty * CY, jend = CLU ? jhi : ncy;
         if (cx)
-          run_tile(std::integral_constant<int, 1>{}, pt, tx, ty, cy, phase);
+          run_tile(std::integral_constant<int, 1>{}, pt, tx, j0, jend, cy, phase);
         else
-          run_tile(std::integral_constant<int, 0>{}, pt, tx, ty, cy, phase);
+          run_tile(std::integral_constant<int, 0>{}, pt, tx, j0, jend, cy, phase);
         unsigned v = 0;
         if (lane == 0) v = atomicAdd(ctr, 1u);
-        k = wpb + (int)__shfl_sync(kFull, v, 0);
+        k = tile_warps + (int)__shfl_sync(kFull, v, 0);
       }
       __syncthreads();
       if (tid == 0) s_cnt[prv] = 0;
-      if (!grid_barrier(a.ctl, ++episode, &s_ok)) return;
+      if constexpr (CLU) {
+        // the hardware barrier of the cluster's blocks (all co-scheduled, as
+        // the threads of a block are for __syncthreads), with release and
+        // acquire at cluster scope for the strips and the global tables
+        cluster.sync();
+      } else {
+        if (!grid_barrier(a.ctl, ++episode, &s_ok)) return;
+      }
     }
   }
   if (step > 0) replay_phase((step - 1) & 1);
@@ -451,6 +554,15 @@ __global__ void __launch_bounds__(32 * kMaxSweepWarps, 1)
   }
   if (a.tick_ptr && a.tick_advance && blockIdx.x == 0 && tid == 0 && a.mcs > 0)
     *a.tick_ptr = s_tick0 + (unsigned long long)a.mcs;
+  if constexpr (CLU) {
+    // this block's rows back to the lattice in global memory; no block
+    // leaves while another may still read its shared memory
+    const int nvec = row0 < row1 ? (row1 - row0) * (nx / 4) : 0;
+    uint4* dst = reinterpret_cast<uint4*>(L + (long long)row0 * nx);
+    __syncthreads();
+    for (int v = tid; v < nvec; v += blockDim.x) dst[v] = reinterpret_cast<const uint4*>(strip)[v];
+    cluster.sync();
+  }
 }
 
 template <int CY>
@@ -512,9 +624,134 @@ cudaError_t launch_sweep2d(bool perim, int variant, const SweepArgs& a, const vo
   if (e != cudaSuccess) return e;
   alignas(64) CUtensorMap map;
   std::memcpy(&map, tmap, sizeof map);
-  int tma = use_tma ? 1 : 0;
-  void* args[] = {const_cast<SweepArgs*>(&a), &map, &tma};
+  int tma = use_tma ? 1 : 0, strip_rows = 0;
+  void* args[] = {const_cast<SweepArgs*>(&a), &map, &tma, &strip_rows};
   return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(32 * sh.warps), args, sh.smem, s);
+}
+
+// Cluster mode.  Blocks of cluster_warps(CY) warps; each block's shared memory
+// holds its strip of H rows, the warp areas and its two dirty lists.
+namespace {
+
+// Tile rows and warps of the cluster sweep's variants (v0..v3): taller
+// tiles fill the compacted batches better, one-row tiles give every warp of
+// a block a tile on the smallest strips.
+constexpr int kClusterCY[4] = {2, 4, 8, 1};
+constexpr int kClusterW[4] = {cluster_warps(2), cluster_warps(4), cluster_warps(8),
+                              cluster_warps(1)};
+
+template <int CY>
+const void* cluster_fn_cy(bool perim) {
+  return perim ? (const void*)sweep2d_kernel<true, CY, true>
+               : (const void*)sweep2d_kernel<false, CY, true>;
+}
+const void* cluster_fn(bool perim, int v) {
+  switch (v) {
+    case 0: return cluster_fn_cy<2>(perim);
+    case 1: return cluster_fn_cy<4>(perim);
+    case 2: return cluster_fn_cy<8>(perim);
+    default: return cluster_fn_cy<1>(perim);
+  }
+}
+size_t warp_area(int v) {
+  switch (v) {
+    case 0: return sizeof(Warp2Smem<2>);
+    case 1: return sizeof(Warp2Smem<4>);
+    case 2: return sizeof(Warp2Smem<8>);
+    default: return sizeof(Warp2Smem<1>);
+  }
+}
+
+long long cluster_list_cap(int nx, int H) {
+  // two rows per target of the block's tiles in one phase: at most H / 2 + 1
+  // target rows of one class per strip, tiles rounded up by at most 7 rows,
+  // 32 targets per row of a tile column
+  return 2LL * 32 * (((nx >> 1) + 31) / 32) * (H / 2 + 1 + 7);
+}
+
+size_t cluster_smem(int nx, int H, int v) {
+  const size_t strip = (size_t)(((long long)H * nx + 31) & ~31LL) * 4;
+  return strip + warp_area(v) * (size_t)kClusterW[v] + 2 * 4 * (size_t)cluster_list_cap(nx, H);
+}
+
+cudaLaunchConfig_t cluster_config(int G, int v, size_t smem, cudaStream_t s,
+                                  cudaLaunchAttribute* attr) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(G);
+  cfg.blockDim = dim3(32 * kClusterW[v]);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = G;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cfg;
+}
+
+cudaError_t cluster_attributes(bool perim, int v, size_t smem) {
+  const void* fn = cluster_fn(perim, v);
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  return e;
+}
+}  // namespace
+
+bool cluster_sweep_plan(int nx, int ny, int* G, int* H, long long* list_cap) {
+  if (!row_tiles_fit(nx, ny)) return false;
+  for (int g : {16, 8}) {
+    const int h = (ny + g - 1) / g;
+    bool fits = true;
+    for (int v = 0; v < 4 && fits; ++v) {
+      const size_t smem = cluster_smem(nx, h, v);
+      if (smem > (size_t)kSweepSmemMax - 1024) {
+        fits = false;
+        break;
+      }
+      for (bool perim : {false, true}) {
+        if (cluster_attributes(perim, v, smem) != cudaSuccess) {
+          fits = false;
+          break;
+        }
+        cudaLaunchAttribute attr[1];
+        cudaLaunchConfig_t cfg = cluster_config(g, v, smem, nullptr, attr);
+        int n = 0;
+        if (cudaOccupancyMaxActiveClusters(&n, cluster_fn(perim, v), &cfg) != cudaSuccess ||
+            n < 1) {
+          fits = false;
+          break;
+        }
+      }
+    }
+    cudaGetLastError();  // (a refused size is not an error of the engine)
+    if (!fits) continue;
+    *G = g;
+    *H = h;
+    *list_cap = cluster_list_cap(nx, h);
+    return true;
+  }
+  return false;
+}
+
+int cluster_tile_rows(int variant) {
+  return kClusterCY[variant >= 0 && variant < 4 ? variant : 3];
+}
+
+cudaError_t launch_sweep2d_cluster(bool perim, int variant, const SweepArgs& a, const void* tmap,
+                                   int nx, int G, int H, cudaStream_t s) {
+  const int v = variant >= 0 && variant < 4 ? variant : 3;
+  const size_t smem = cluster_smem(nx, H, v);
+  cudaError_t e = cluster_attributes(perim, v, smem);
+  if (e != cudaSuccess) return e;
+  alignas(64) CUtensorMap map;
+  std::memcpy(&map, tmap, sizeof map);
+  int tma = 0, strip_rows = H;
+  void* args[] = {const_cast<SweepArgs*>(&a), &map, &tma, &strip_rows};
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg = cluster_config(G, v, smem, s, attr);
+  return cudaLaunchKernelExC(&cfg, cluster_fn(perim, v), args);
 }
 
 }  // namespace gpucpm

@@ -128,23 +128,35 @@ __device__ __forceinline__ void add_delta(const PhaseTables<NDIM>& pt,
 // Replays the deltas of the rows on a block's dirty list into `ap`/`cs`,
 // strided over the block's threads.  A row can be on several lists (or
 // twice on one); taking its delta with an exchange hands it to exactly one
-// of them and leaves the delta table zeroed for the phase after next.
-template <int NDIM>
+// of them and leaves the delta table zeroed for the phase after next.  All
+// exchanges of a row are issued before any add, so a row costs one round
+// trip to L2.  SMEM_LIST: the list lives in shared memory (cluster sweep).
+// replay_lanes takes entries first, first + stride, ... (one warp's lanes).
+template <int NDIM, bool SMEM_LIST = false>
+__device__ __forceinline__ void replay_lanes(const uint32_t* list, unsigned n,
+                                             unsigned long long* dap, long long* dcs,
+                                             unsigned long long* ap, long long* cs,
+                                             unsigned first, unsigned stride) {
+  for (unsigned j = first; j < n; j += stride) {
+    const uint32_t row = SMEM_LIST ? list[j] : __ldcg(list + j);
+    const unsigned long long d = atomicExch(dap + row, 0ull);
+    unsigned long long dc[NDIM];
+#pragma unroll
+    for (int k = 0; k < NDIM; ++k)
+      dc[k] = atomicExch(reinterpret_cast<unsigned long long*>(dcs + (long long)row * NDIM + k),
+                         0ull);
+    if (d) atomicAdd(ap + row, d);
+#pragma unroll
+    for (int k = 0; k < NDIM; ++k)
+      if (dc[k])
+        atomicAdd(reinterpret_cast<unsigned long long*>(cs + (long long)row * NDIM + k), dc[k]);
+  }
+}
+template <int NDIM, bool SMEM_LIST = false>
 __device__ __forceinline__ void replay(const uint32_t* list, unsigned n,
                                        unsigned long long* dap, long long* dcs,
                                        unsigned long long* ap, long long* cs) {
-  for (unsigned j = threadIdx.x; j < n; j += blockDim.x) {
-    const uint32_t row = __ldcg(list + j);
-    const unsigned long long d = atomicExch(dap + row, 0ull);
-    if (d) atomicAdd(ap + row, d);
-#pragma unroll
-    for (int k = 0; k < NDIM; ++k) {
-      const long long idx = (long long)row * NDIM + k;
-      const unsigned long long dc =
-          atomicExch(reinterpret_cast<unsigned long long*>(dcs + idx), 0ull);
-      if (dc) atomicAdd(reinterpret_cast<unsigned long long*>(cs + idx), dc);
-    }
-  }
+  replay_lanes<NDIM, SMEM_LIST>(list, n, dap, dcs, ap, cs, threadIdx.x, blockDim.x);
 }
 
 }  // namespace

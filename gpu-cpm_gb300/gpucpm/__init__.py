@@ -61,7 +61,9 @@ DISPATCH_HYBRID = 2
 FILL_PARITY = 0
 FILL_VECTOR = 1
 FILL_TMA = 2
-FILL_NAMES = {FILL_PARITY: "parity", FILL_VECTOR: "vector", FILL_TMA: "tma"}
+FILL_CLUSTER = 3
+FILL_NAMES = {FILL_PARITY: "parity", FILL_VECTOR: "vector", FILL_TMA: "tma",
+              FILL_CLUSTER: "cluster"}
 
 
 class CpmError(RuntimeError):
@@ -557,8 +559,8 @@ class _Engine:
 
     @property
     def fill(self):
-        """How the sweep stages its tiles: FILL_PARITY, FILL_VECTOR or
-        FILL_TMA (see cpm_set_fill)."""
+        """How the sweep stages its tiles: FILL_PARITY, FILL_VECTOR, FILL_TMA
+        or FILL_CLUSTER (see cpm_set_fill)."""
         f = ctypes.c_int()
         self._call("cpm_get_fill", ctypes.byref(f))
         return f.value

@@ -331,6 +331,12 @@ int cpm_sweep_config(const cpm_handle* h, int* variant, int* tile_x,
  *   CPM_FILL_TMA     row-major tiles, interior tiles copied by the tensor
  *                    memory accelerator (cp.async.bulk.tensor), tiles on the
  *                    periodic seam from vector loads
+ *   CPM_FILL_CLUSTER (small 2D lattices) one thread-block cluster of 16 (or 8)
+ *                    blocks holds the lattice in its shared memory, one
+ *                    strip of rows per block, for a whole run; one-row
+ *                    tiles are staged from the strips and the phases end at
+ *                    a barrier inside the cluster.  cpm_autotune tries it
+ *                    wherever it fits and keeps it when it is faster.
  * Row-major tiles need a single lattice with nx a multiple of 4 and
  * nx >= 72 (in 2D ny >= 66, in 3D ny >= 18 and nz >= 18); such lattices start
  * in CPM_FILL_TMA (CPM_FILL_VECTOR where the tensor maps cannot be encoded),
@@ -340,6 +346,7 @@ int cpm_sweep_config(const cpm_handle* h, int* variant, int* tile_x,
 #define CPM_FILL_PARITY 0
 #define CPM_FILL_VECTOR 1
 #define CPM_FILL_TMA 2
+#define CPM_FILL_CLUSTER 3
 int cpm_set_fill(cpm_handle* h, int fill);
 int cpm_get_fill(const cpm_handle* h, int* fill);
 

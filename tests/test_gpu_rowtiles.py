@@ -4,6 +4,8 @@ against the oracle, bit for bit, under each way of staging tiles:
   parity  the general sweep_kernel (scalar loads, parity-split tiles)
   vector  row-major tiles from 16-byte vector loads
   tma     row-major tiles, interior tiles copied by cp.async.bulk.tensor
+  cluster (2D) the lattice held in the shared memory of one thread-block
+          cluster, one-row tiles staged from its strips
 
 Shapes cover partial tiles in x (nx = 76: 38 target columns, a full and a
 6-wide tile), odd heights and depths (one-row or one-plane slots of the last
@@ -20,13 +22,13 @@ from test_gpu_parity import assert_same, finish, make_engine
 
 pytestmark = pytest.mark.gpu
 
-FILLS = ("parity", "vector", "tma")
+FILLS = ("parity", "vector", "tma", "cluster")
 
 
 def _fill_code(name):
     import gpucpm
     return {"parity": gpucpm.FILL_PARITY, "vector": gpucpm.FILL_VECTOR,
-            "tma": gpucpm.FILL_TMA}[name]
+            "tma": gpucpm.FILL_TMA, "cluster": gpucpm.FILL_CLUSTER}[name]
 
 
 def _terms(w, seed):
@@ -63,6 +65,8 @@ def _terms(w, seed):
     ((18, 19, 72), 40, 3, False, 6),   # 3D, one-row tiles
 ])
 def test_row_tiles_match_oracle(engine_lib, fill, shape, ncells, variant, terms, mcs):
+    if fill == "cluster" and len(shape) == 3:
+        pytest.skip("the cluster sweep is 2D")
     w = W.random_small(shape, ncells, ntypes=3, seed=500 + ncells, temperature=9.0)
     if terms:
         _terms(w, ncells)
@@ -76,6 +80,23 @@ def test_row_tiles_match_oracle(engine_lib, fill, shape, ncells, variant, terms,
     sim.run(mcs)
     assert_same(e, sim)
     assert int(sim.counters[2]) > 0
+
+
+def test_cluster_sweep_graph_runs_and_autotune(engine_lib):
+    """The 256^2 sorting lattice in the cluster sweep: graph replays and plain
+    runs continue one trajectory, and the autotuner (which tries the cluster
+    sweep) leaves the state as it was."""
+    import gpucpm
+    w = W.sorting_2d(n=256, ncells=655)
+    e = make_engine(w, seed=9)
+    e.set_fill(gpucpm.FILL_CLUSTER)
+    e.run_graph(5)
+    e.run_mcs(3)
+    e.autotune(probe_mcs=2)
+    e.run_graph(4)
+    finish(e)
+    sim = oracle.OracleSim(w.lattice, w.ncells, **w.oracle_kwargs(), seed=9).run(12)
+    assert_same(e, sim)
 
 
 def test_row_tiles_graph_runs_and_default_fill(engine_lib):
