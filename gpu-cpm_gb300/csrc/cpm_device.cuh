@@ -142,10 +142,10 @@ __device__ __forceinline__ void st_release_gpu(unsigned* p, unsigned v) {
 }
 
 // Grid-wide barrier of a cooperative launch (all blocks co-resident).  The
-// arrival counter ctl[kCtlBarrier] and the release flag ctl[kCtlFlag] are
-// zeroed before the launch and only grow.  At the e-th barrier (e = 1, 2,
-// ...) each block adds 1 to the counter; the block that brings it to
-// gridDim.x * e publishes e in the flag, which the others poll with backoff.
+// arrival counter ctl[kCtlBarrier] is zeroed before the launch and only
+// grows.  At the e-th barrier (e = 1, 2, ...) each block adds 1 to it with a
+// release reduction and polls it with acquire loads, with backoff, until it
+// reaches gridDim.x * e.
 // The wait is bounded: after `timeout_ns` the block sets kErrTimeout and
 // every block returns false at its next barrier, so a lost block ends the
 // kernel with an error status instead of a hang.  Block-uniform result.
@@ -157,33 +157,29 @@ __device__ __forceinline__ bool grid_barrier(
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
-    __threadfence();
-    const unsigned arrived = atomicAdd(&ctl[kCtlBarrier], 1u) + 1u;
-    if (arrived == gridDim.x * episode) {
-      __threadfence();
-      st_release_gpu(&ctl[kCtlFlag], episode);
-    } else {
-      const unsigned long long t0 = global_timer_ns();
-      unsigned spins = 0, nap = 32;
-      while (ld_acquire_gpu(&ctl[kCtlFlag]) < episode) {
-        if ((++spins & 15u) == 0) {
-          if (ld_acquire_gpu(&ctl[kCtlErr]) & kErrTimeout) {
-            ok = 0;
-            break;
-          }
-          if (global_timer_ns() - t0 > timeout_ns) {
-            atomicOr((int*)&ctl[kCtlErr], kErrTimeout);
-            ok = 0;
-            break;
-          }
+    const unsigned target = gridDim.x * episode;
+    // arrival: a release reduction (nothing comes back), then acquire polls
+    // of the counter itself until every block of this episode has arrived
+    asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(&ctl[kCtlBarrier]) : "memory");
+    const unsigned long long t0 = global_timer_ns();
+    unsigned spins = 0, nap = 32;
+    while (ld_acquire_gpu(&ctl[kCtlBarrier]) < target) {
+      if ((++spins & 15u) == 0) {
+        if (ld_acquire_gpu(&ctl[kCtlErr]) & kErrTimeout) {
+          ok = 0;
+          break;
         }
-        if (spins > 64) {  // (polls are L2 round trips: most waits end before)
-          __nanosleep(nap);
-          if (nap < 128) nap <<= 1;
+        if (global_timer_ns() - t0 > timeout_ns) {
+          atomicOr((int*)&ctl[kCtlErr], kErrTimeout);
+          ok = 0;
+          break;
         }
       }
+      if (spins > 64) {  // (polls are L2 round trips: most waits end before)
+        __nanosleep(nap);
+        if (nap < 128) nap <<= 1;
+      }
     }
-    __threadfence();
     *s_ok = ok;
   }
   __syncthreads();

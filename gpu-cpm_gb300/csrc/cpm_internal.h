@@ -100,11 +100,9 @@ struct SweepShape {
 };
 SweepShape sweep_shape(int ndim, int variant, bool scores = false);
 
-// ctl[] word indices (the barrier counter and its release flag sit in
-// different 128-byte lines so that waiting blocks do not slow down arriving
-// ones)
+// ctl[] word indices (the barrier counter, the replica queue and the error
+// word sit in different 128-byte lines)
 constexpr int kCtlBarrier = 0;
-constexpr int kCtlFlag = 32;
 constexpr int kCtlQueue = 40;  // next replica to claim (replica dispatch)
 constexpr int kCtlErr = 48;  // words [0, kCtlErr) are zeroed before a launch
 constexpr int kCtlWords = 64;
