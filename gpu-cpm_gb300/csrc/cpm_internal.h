@@ -100,8 +100,7 @@ struct SweepShape {
 };
 SweepShape sweep_shape(int ndim, int variant, bool scores = false);
 
-// ctl[] word indices (the barrier counter, the replica queue and the error
-// word sit in different 128-byte lines)
+// ctl[] word indices (the barrier counter has a 128-byte line of its own)
 constexpr int kCtlBarrier = 0;
 constexpr int kCtlQueue = 40;  // next replica to claim (replica dispatch)
 constexpr int kCtlErr = 48;  // words [0, kCtlErr) are zeroed before a launch
