@@ -303,6 +303,10 @@ def reference_gpu_baseline(w, timed_mcs=100, probe_mcs=10, top=6):
         return None
     import torch
     n = w.lattice.shape[0]
+    if n & (n - 1):
+        # it would run, but on another model: the source pick wraps with a mask
+        return {"unavailable": f"side {n} is not a power of two: the reference wraps its "
+                               "neighbour pick as (x + dx) & (D - 1) (src/random.cu:25)"}
     r = ref_gpu.RefGpu(n, w.ndim, w.ncells, w.temperature, device=torch.cuda.current_device())
     r.apply(w)
     if w.ndim == 3:
