@@ -209,18 +209,38 @@ __global__ void __launch_bounds__(32 * (CLU ? cluster_warps(CY) : kMaxSweepWarps
   // 64 tx - 4 and row yorig.
   auto stage = [&](int X0, int yorig) {
     if constexpr (CLU) {
-      // from the strips: rows of other blocks through distributed shared memory
-      for (int v = lane; v < RT::SR * kVecPerRow; v += 32) {
-        const int row = v / kVecPerRow, col = v - row * kVecPerRow;
-        int gy = yorig + row;
+      // from the strips: rows of other blocks through distributed shared
+      // memory.  Lane r < SR finds staged row r's owner block and the row's
+      // address in that block's strip; the vectors take it by shuffle, and
+      // every load of the box is issued before the first store.
+      constexpr int NV = RT::SR * kVecPerRow, NIT = (NV + 31) / 32;
+      unsigned long long rowp = 0ull;
+      if (lane < RT::SR) {
+        int gy = yorig + lane;
         gy = gy < 0 ? gy + ny : (gy >= ny ? gy - ny : gy);
+        const int owner = gy / strip_rows;
+        rowp = reinterpret_cast<unsigned long long>(
+            cluster.map_shared_rank(strip, owner) + (gy - owner * strip_rows) * nx);
+      }
+      uint4 val[NIT];
+#pragma unroll
+      for (int i = 0; i < NIT; ++i) {
+        const int v = lane + 32 * i;
+        const int row = v / kVecPerRow, col = v - row * kVecPerRow;
+        const unsigned long long rp = __shfl_sync(kFull, rowp, min(row, RT::SR - 1));
         int gx = X0 + 4 * col;
         gx = gx < 0 ? gx + nx : (gx >= nx ? gx - nx : gx);
-        const int owner = gy / strip_rows;
-        const uint32_t* rs =
-            cluster.map_shared_rank(strip, owner) + (gy - owner * strip_rows) * nx + gx;
-        *reinterpret_cast<uint4*>(ws.tile + row * kPitch + 4 * col) =
-            *reinterpret_cast<const uint4*>(rs);
+        if (v < NV) {
+          val[i] = *reinterpret_cast<const uint4*>(reinterpret_cast<const uint32_t*>(rp) + gx);
+          // (one-row tiles run at 64 registers: no loads held back there)
+          if (CY == 1) *reinterpret_cast<uint4*>(ws.tile + row * kPitch + 4 * col) = val[i];
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < NIT; ++i) {
+        const int v = lane + 32 * i;
+        const int row = v / kVecPerRow, col = v - row * kVecPerRow;
+        if (CY > 1 && v < NV) *reinterpret_cast<uint4*>(ws.tile + row * kPitch + 4 * col) = val[i];
       }
       __syncwarp();
       return;
@@ -484,7 +504,7 @@ __global__ void __launch_bounds__(32 * (CLU ? cluster_warps(CY) : kMaxSweepWarps
           replay_phase(prv);
         } else if (warp == wpb - 1) {
           const unsigned n = min(s_cnt[prv], (unsigned)a.list_cap);
-          replay_lanes<2, true>(blist(prv), n, prv ? a.dap[1] : a.dap[0],
+          replay_lanes<2, true, (CY == 1 ? 1 : 4)>(blist(prv), n, prv ? a.dap[1] : a.dap[0],
                                 prv ? a.dcs[1] : a.dcs[0], prv ? a.ap[1] : a.ap[0],
                                 prv ? a.cs[1] : a.cs[0], lane, 32);
         }

@@ -131,25 +131,42 @@ __device__ __forceinline__ void add_delta(const PhaseTables<NDIM>& pt,
 // of them and leaves the delta table zeroed for the phase after next.  All
 // exchanges of a row are issued before any add, so a row costs one round
 // trip to L2.  SMEM_LIST: the list lives in shared memory (cluster sweep).
-// replay_lanes takes entries first, first + stride, ... (one warp's lanes).
-template <int NDIM, bool SMEM_LIST = false>
+// replay_lanes takes entries first, first + stride, ... (one warp's lanes),
+// U of them per round with all their exchanges in flight together (a single
+// replay warp then waits on one round trip per U x 32 entries).
+template <int NDIM, bool SMEM_LIST = false, int U = 1>
 __device__ __forceinline__ void replay_lanes(const uint32_t* list, unsigned n,
                                              unsigned long long* dap, long long* dcs,
                                              unsigned long long* ap, long long* cs,
                                              unsigned first, unsigned stride) {
-  for (unsigned j = first; j < n; j += stride) {
-    const uint32_t row = SMEM_LIST ? list[j] : __ldcg(list + j);
-    const unsigned long long d = atomicExch(dap + row, 0ull);
-    unsigned long long dc[NDIM];
+  for (unsigned j0 = first; j0 < n; j0 += U * stride) {
+    uint32_t row[U];
+    unsigned long long d[U], dc[U][NDIM];
 #pragma unroll
-    for (int k = 0; k < NDIM; ++k)
-      dc[k] = atomicExch(reinterpret_cast<unsigned long long*>(dcs + (long long)row * NDIM + k),
-                         0ull);
-    if (d) atomicAdd(ap + row, d);
+    for (int u = 0; u < U; ++u) {
+      const unsigned j = j0 + (unsigned)u * stride;
+      row[u] = 0u;
+      d[u] = 0ull;
 #pragma unroll
-    for (int k = 0; k < NDIM; ++k)
-      if (dc[k])
-        atomicAdd(reinterpret_cast<unsigned long long*>(cs + (long long)row * NDIM + k), dc[k]);
+      for (int k = 0; k < NDIM; ++k) dc[u][k] = 0ull;
+      if (j < n) {
+        row[u] = SMEM_LIST ? list[j] : __ldcg(list + j);
+        d[u] = atomicExch(dap + row[u], 0ull);
+#pragma unroll
+        for (int k = 0; k < NDIM; ++k)
+          dc[u][k] = atomicExch(
+              reinterpret_cast<unsigned long long*>(dcs + (long long)row[u] * NDIM + k), 0ull);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (d[u]) atomicAdd(ap + row[u], d[u]);
+#pragma unroll
+      for (int k = 0; k < NDIM; ++k)
+        if (dc[u][k])
+          atomicAdd(reinterpret_cast<unsigned long long*>(cs + (long long)row[u] * NDIM + k),
+                    dc[u][k]);
+    }
   }
 }
 template <int NDIM, bool SMEM_LIST = false>
