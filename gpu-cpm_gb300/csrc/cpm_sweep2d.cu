@@ -41,17 +41,20 @@
 // from a shared counter, so that the phase ends within about one tile on
 // every warp although tiles differ in how many attempts they evaluate.
 //
-// Cluster mode (CLU, one-row tiles).  A small lattice is swept by one
-// thread-block cluster of G blocks instead of the whole grid: block r keeps
-// lattice rows [r H, r H + H) in its own shared memory for the whole launch,
-// stages tiles from the strips (rows of other blocks through distributed
-// shared memory), writes its targets (always its own rows) in place, keeps
-// its dirty lists in shared memory, and the phases end at the cluster's
-// hardware barrier (barrier.cluster, release / acquire at cluster scope)
-// instead of the grid barrier in global memory.  The cell tables stay in
-// global memory with the same double buffering.  Neighbour rows read from
-// another block in a phase are of the other row class, which no attempt of
-// the phase writes.
+// Cluster mode (CLU).  A small lattice is swept by one thread-block cluster
+// of G blocks instead of the whole grid.  Block r keeps lattice rows
+// [r H, r H + H) in its own shared memory for the whole launch, together
+// with one halo row above and one below (copies of the neighbouring blocks'
+// boundary rows), every row padded with 4 periodic copies of columns on
+// each side.  Tiles are read in place from that strip: no staging.  A block
+// writes its targets (always its own rows) in place, keeps its dirty lists in
+// shared memory, and after a phase in which it changed one of its two
+// boundary rows it stores that row into the neighbour's halo (distributed
+// shared memory).  Phases end at the cluster's hardware barrier
+// (barrier.cluster, release / acquire at cluster scope) instead of the grid
+// barrier in global memory.  The cell tables stay in global memory with the
+// same double buffering.  A halo row is read only in phases of the other row
+// class, so it never changes while it is read.
 #include <cooperative_groups.h>
 #include <cuda.h>  // CUtensorMap (the map itself is encoded on the host)
 
@@ -84,30 +87,39 @@ struct alignas(128) Warp2Smem {
   uint16_t qa[RowTile<CY>::NT];
 };
 
+// Per-warp shared memory of the cluster sweep (tiles are read in place).
+template <int CY>
+struct alignas(16) WarpCluSmem {
+  uint2 qb[RowTile<CY>::NT];
+  uint16_t qa[RowTile<CY>::NT];
+};
+
 template <int CY>
 constexpr int row_tile_warps(int cap) {
   const int w = (int)(kSweepSmemMax / sizeof(Warp2Smem<CY>));
   return w < cap ? w : cap;
 }
 
-// Target (qx, qy) and its Moore neighbours in (dy, dx) lexicographic order.
+// Target (qx, qy) and its Moore neighbours in (dy, dx) lexicographic order,
+// from a tile of row pitch `pitch` words.
 template <int PAR>
-__device__ __forceinline__ uint32_t nbhd(const uint32_t* tile, int qx, int qy, uint32_t* nb) {
+__device__ __forceinline__ uint32_t nbhd(const uint32_t* tile, int pitch, int qx, int qy,
+                                         uint32_t* nb) {
   uint32_t t;
-  row3<PAR>(tile, 2 * qy, qx, nb[0], nb[1], nb[2]);
-  row3<PAR>(tile, 2 * qy + 1, qx, nb[3], t, nb[4]);
-  row3<PAR>(tile, 2 * qy + 2, qx, nb[5], nb[6], nb[7]);
+  row3<PAR>(tile + 2 * qy * pitch, 0, qx, nb[0], nb[1], nb[2]);
+  row3<PAR>(tile + (2 * qy + 1) * pitch, 0, qx, nb[3], t, nb[4]);
+  row3<PAR>(tile + (2 * qy + 2) * pitch, 0, qx, nb[5], nb[6], nb[7]);
   return t;
 }
 
 // staged index of target (qx, qy) and offset of neighbour k
 template <int PAR>
-__device__ __forceinline__ int center_idx(int qx, int qy) {
-  return (2 * qy + 1) * kPitch + 2 * qx + 4 + PAR;
+__device__ __forceinline__ int center_idx(int pitch, int qx, int qy) {
+  return (2 * qy + 1) * pitch + 2 * qx + 4 + PAR;
 }
-__device__ __forceinline__ int nb_off(int k) {
+__device__ __forceinline__ int nb_off(int pitch, int k) {
   const int m = k + (k >= 4);
-  return (m / 3 - 1) * kPitch + (m % 3 - 1);
+  return (m / 3 - 1) * pitch + (m % 3 - 1);
 }
 
 // Warps per block of the cluster sweep by tile height: one one-row tile per
@@ -129,18 +141,26 @@ __global__ void __launch_bounds__(32 * (CLU ? cluster_warps(CY) : kMaxSweepWarps
   __shared__ unsigned s_cnt[2];
   __shared__ unsigned long long s_tick0;
   __shared__ unsigned s_next[2];  // next unclaimed tile of the band (by phase parity)
+  __shared__ uint32_t s_halo[2];  // (cluster mode) halo rows holding copies of the own edge rows
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int wpb = blockDim.x >> 5;
-  // (cluster mode) this block's strip of rows leads the dynamic shared memory
-  const int strip_words = CLU ? (strip_rows * __ldg(&a.reps[0].nx) + 31) & ~31 : 0;
+  // (cluster mode) this block's strip of rows leads the dynamic shared
+  // memory: strip_rows + 2 rows (halo above, own rows, halo below) of
+  // sp = nx + 8 words, lattice column x at word 4 + x of its row
+  using WS = std::conditional_t<CLU, WarpCluSmem<CY>, Warp2Smem<CY>>;
+  const int sp = CLU ? __ldg(&a.reps[0].nx) + 8 : 0;
+  const int strip_words = CLU ? ((strip_rows + 2) * sp + 31) & ~31 : 0;
   uint32_t* const strip = reinterpret_cast<uint32_t*>(smem_raw);
-  Warp2Smem<CY>& ws =
-      reinterpret_cast<Warp2Smem<CY>*>(smem_raw + 4 * (size_t)strip_words)[warp];
+  WS& ws = reinterpret_cast<WS*>(smem_raw + 4 * (size_t)strip_words)[warp];
   // (cluster mode) the block's two dirty lists follow the warp areas
   uint32_t* const slist = reinterpret_cast<uint32_t*>(
-      smem_raw + 4 * (size_t)strip_words + sizeof(Warp2Smem<CY>) * (size_t)wpb);
-  const uint32_t tile_s = smem_addr(ws.tile), bar_s = smem_addr(&ws.bar);
+      smem_raw + 4 * (size_t)strip_words + sizeof(WS) * (size_t)wpb);
+  uint32_t tile_s = 0, bar_s = 0;
+  if constexpr (!CLU) {
+    tile_s = smem_addr(ws.tile);
+    bar_s = smem_addr(&ws.bar);
+  }
   const uint32_t k0 = (uint32_t)a.seed, k1 = (uint32_t)(a.seed >> 32);
   int* err = reinterpret_cast<int*>(&a.ctl[kCtlErr]);
   auto blist = [&](int b) {
@@ -154,7 +174,7 @@ __global__ void __launch_bounds__(32 * (CLU ? cluster_warps(CY) : kMaxSweepWarps
   if (tid < 2) s_cnt[tid] = 0;
   if (tid < 2) s_next[tid] = 0;
   if (tid == 0) s_tick0 = a.tick_ptr ? __ldcg(a.tick_ptr) : a.tick0;
-  if (lane == 0) {
+  if (!CLU && lane == 0) {
     mbar_init(bar_s, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -174,18 +194,49 @@ __global__ void __launch_bounds__(32 * (CLU ? cluster_warps(CY) : kMaxSweepWarps
   const long long cell_off = __ldg(&a.reps[0].cell_off);
   uint32_t* L = a.lat + lat_off;
 
-  // Cluster mode: load this block's rows, then meet the other blocks so that
-  // every strip is in place before any block reads it.
+  // Cluster mode: load this block's rows and its two halo rows (the rows
+  // above and below, periodic) with their padding columns, then meet the
+  // other blocks so that no block starts before every strip is in place.
   cooperative_groups::cluster_group cluster = cooperative_groups::this_cluster();
   const int crank = CLU ? (int)cluster.block_rank() : 0;
   const int row0 = crank * strip_rows;
   const int row1 = CLU ? min(ny, row0 + strip_rows) : 0;
+  const int nown = CLU ? max(0, row1 - row0) : 0;  // own rows (0: an idle block)
   if constexpr (CLU) {
-    const int nvec = row0 < row1 ? (row1 - row0) * (nx / 4) : 0;
-    const uint4* src = reinterpret_cast<const uint4*>(L + (long long)row0 * nx);
-    for (int v = tid; v < nvec; v += blockDim.x) reinterpret_cast<uint4*>(strip)[v] = __ldcg(src + v);
+    const int vpr = sp / 4;  // vectors per strip row
+    const int nvec = nown > 0 ? (nown + 2) * vpr : 0;
+    for (int v = tid; v < nvec; v += blockDim.x) {
+      const int r = v / vpr, k = v - r * vpr;
+      int gy = row0 - 1 + r;
+      gy = gy < 0 ? gy + ny : (gy >= ny ? gy - ny : gy);
+      int gx = 4 * k - 4;
+      gx = gx < 0 ? gx + nx : (gx >= nx ? gx - nx : gx);
+      reinterpret_cast<uint4*>(strip)[v] =
+          __ldcg(reinterpret_cast<const uint4*>(L + (long long)gy * nx + gx));
+    }
+    if (tid < 2 && nown > 0) {
+      // the first own row is the bottom halo of the block above, the last
+      // one the top halo of the block below
+      const int gy = tid == 0 ? (row0 == 0 ? ny - 1 : row0 - 1) : (row1 == ny ? 0 : row1);
+      const int nrank = gy / strip_rows;
+      const int nrows = min(ny, (nrank + 1) * strip_rows) - nrank * strip_rows;
+      const uint32_t local = smem_addr(strip + (tid == 0 ? nrows + 1 : 0) * sp);
+      uint32_t remote;
+      asm("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(remote) : "r"(local), "r"(nrank));
+      s_halo[tid] = remote;
+    }
     cluster.sync();
   }
+
+  // word x of a copy of an own row at shared::cluster address `row`
+  auto halo_store = [&](uint32_t row, int x, uint32_t v) {
+    auto st = [](uint32_t addr, uint32_t val) {
+      asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(addr), "r"(val) : "memory");
+    };
+    st(row + 4u * (4 + x), v);
+    if (x < 4) st(row + 4u * (4 + x + nx), v);
+    if (x >= nx - 4) st(row + 4u * (x - nx + 4), v);
+  };
 
   auto tables = [&](int cur) {
     PhaseTables<2> pt;
@@ -208,61 +259,26 @@ __global__ void __launch_bounds__(32 * (CLU ? cluster_warps(CY) : kMaxSweepWarps
   // Stage tile (tx, ty) of slot (cx, cy): 72 x SR words from lattice column
   // 64 tx - 4 and row yorig.
   auto stage = [&](int X0, int yorig) {
-    if constexpr (CLU) {
-      // from the strips: rows of other blocks through distributed shared
-      // memory.  Lane r < SR finds staged row r's owner block and the row's
-      // address in that block's strip; the vectors take it by shuffle, and
-      // every load of the box is issued before the first store.
-      constexpr int NV = RT::SR * kVecPerRow, NIT = (NV + 31) / 32;
-      unsigned long long rowp = 0ull;
-      if (lane < RT::SR) {
-        int gy = yorig + lane;
-        gy = gy < 0 ? gy + ny : (gy >= ny ? gy - ny : gy);
-        const int owner = gy / strip_rows;
-        rowp = reinterpret_cast<unsigned long long>(
-            cluster.map_shared_rank(strip, owner) + (gy - owner * strip_rows) * nx);
-      }
-      uint4 val[NIT];
-#pragma unroll
-      for (int i = 0; i < NIT; ++i) {
-        const int v = lane + 32 * i;
-        const int row = v / kVecPerRow, col = v - row * kVecPerRow;
-        const unsigned long long rp = __shfl_sync(kFull, rowp, min(row, RT::SR - 1));
-        int gx = X0 + 4 * col;
-        gx = gx < 0 ? gx + nx : (gx >= nx ? gx - nx : gx);
-        if (v < NV) {
-          val[i] = *reinterpret_cast<const uint4*>(reinterpret_cast<const uint32_t*>(rp) + gx);
-          // (one-row tiles run at 64 registers: no loads held back there)
-          if (CY == 1) *reinterpret_cast<uint4*>(ws.tile + row * kPitch + 4 * col) = val[i];
+    if constexpr (!CLU) {  // (cluster mode reads its tiles in place)
+      const bool interior =
+          use_tma && X0 >= 0 && X0 + kPitch <= nx && yorig >= 0 && yorig + RT::SR <= ny;
+      if (interior) {
+        if (lane == 0) tma_load_tile(tile_s, bar_s, &tmap, X0, yorig, RT::BYTES);
+        fill_ok = mbar_wait_bounded(bar_s, bar_parity, err) && fill_ok;
+        bar_parity ^= 1u;
+        fill_ok = __all_sync(kFull, fill_ok);
+      } else {
+        for (int v = lane; v < RT::SR * kVecPerRow; v += 32) {
+          const int row = v / kVecPerRow, col = v - row * kVecPerRow;
+          int gy = yorig + row;
+          gy = gy < 0 ? gy + ny : (gy >= ny ? gy - ny : gy);
+          int gx = X0 + 4 * col;
+          gx = gx < 0 ? gx + nx : (gx >= nx ? gx - nx : gx);
+          const uint4 val = __ldcg(reinterpret_cast<const uint4*>(L + (long long)gy * nx + gx));
+          *reinterpret_cast<uint4*>(ws.tile + row * kPitch + 4 * col) = val;
         }
+        __syncwarp();
       }
-#pragma unroll
-      for (int i = 0; i < NIT; ++i) {
-        const int v = lane + 32 * i;
-        const int row = v / kVecPerRow, col = v - row * kVecPerRow;
-        if (CY > 1 && v < NV) *reinterpret_cast<uint4*>(ws.tile + row * kPitch + 4 * col) = val[i];
-      }
-      __syncwarp();
-      return;
-    }
-    const bool interior =
-        use_tma && X0 >= 0 && X0 + kPitch <= nx && yorig >= 0 && yorig + RT::SR <= ny;
-    if (interior) {
-      if (lane == 0) tma_load_tile(tile_s, bar_s, &tmap, X0, yorig, RT::BYTES);
-      fill_ok = mbar_wait_bounded(bar_s, bar_parity, err) && fill_ok;
-      bar_parity ^= 1u;
-      fill_ok = __all_sync(kFull, fill_ok);
-    } else {
-      for (int v = lane; v < RT::SR * kVecPerRow; v += 32) {
-        const int row = v / kVecPerRow, col = v - row * kVecPerRow;
-        int gy = yorig + row;
-        gy = gy < 0 ? gy + ny : (gy >= ny ? gy - ny : gy);
-        int gx = X0 + 4 * col;
-        gx = gx < 0 ? gx + nx : (gx >= nx ? gx - nx : gx);
-        const uint4 val = __ldcg(reinterpret_cast<const uint4*>(L + (long long)gy * nx + gx));
-        *reinterpret_cast<uint4*>(ws.tile + row * kPitch + 4 * col) = val;
-      }
-      __syncwarp();
     }
   };
 
@@ -279,8 +295,18 @@ __global__ void __launch_bounds__(32 * (CLU ? cluster_warps(CY) : kMaxSweepWarps
     const int cntx = min(32, ncx - i0), cnty = min(CY, jend - j0);
     const int X0 = 2 * i0 - 4;
     const int yorig = class_coord(ny, cy, j0) - 1;
-    stage(X0, yorig);
-    if (!fill_ok) return;  // a copy timed out: the phase's barrier reports it
+    // the tile's box (staged, or in place in the strip) and its row pitch
+    const uint32_t* tb;
+    int pitch;
+    if constexpr (CLU) {
+      tb = strip + (yorig - row0 + 1) * sp + 2 * i0;
+      pitch = sp;
+    } else {
+      stage(X0, yorig);
+      if (!fill_ok) return;  // a copy timed out: the phase's barrier reports it
+      tb = ws.tile;
+      pitch = kPitch;
+    }
 
     // ---- pass 1: boundary test ---------------------------------------
     int na = 0;
@@ -289,7 +315,7 @@ __global__ void __launch_bounds__(32 * (CLU ? cluster_warps(CY) : kMaxSweepWarps
       bool bnd = false;
       if (lane < cntx && qy < cnty) {
         uint32_t nb[8];
-        const uint32_t t = nbhd<PAR>(ws.tile, lane, qy, nb);
+        const uint32_t t = nbhd<PAR>(tb, pitch, lane, qy, nb);
 #pragma unroll
         for (int k = 0; k < 8; ++k) bnd |= nb[k] != t;
       }
@@ -315,8 +341,8 @@ __global__ void __launch_bounds__(32 * (CLU ? cluster_warps(CY) : kMaxSweepWarps
                  c3 = (uint32_t)(phase >> 32);
         philox4x32_10(c0, c1, c2, c3, k0, k1);
         const int kdir = (int)__umulhi(c0, 8u);
-        const int c = center_idx<PAR>(qx, qy);
-        const uint32_t tv = ws.tile[c], sv = ws.tile[c + nb_off(kdir)];
+        const int c = center_idx<PAR>(pitch, qx, qy);
+        const uint32_t tv = tb[c], sv = tb[c + nb_off(pitch, kdir)];
         keep = sv != tv;
         uint32_t medium = 0;  // 1: the source is replaced by the medium
         if (fixed_mask && keep) {
@@ -347,9 +373,9 @@ __global__ void __launch_bounds__(32 * (CLU ? cluster_warps(CY) : kMaxSweepWarps
         const int q = (int)(entry.x & 0xFFFFu), kdir = (int)((entry.x >> 16) & 0xFFu);
         const int qx = q & 31, qy = q >> 5;
         uint32_t nb[8];
-        const uint32_t t = nbhd<PAR>(ws.tile, qx, qy, nb);
+        const uint32_t t = nbhd<PAR>(tb, pitch, qx, qy, nb);
         const uint32_t s =
-            (entry.x >> 24) ? 0u : ws.tile[center_idx<PAR>(qx, qy) + nb_off(kdir)];
+            (entry.x >> 24) ? 0u : tb[center_idx<PAR>(pitch, qx, qy) + nb_off(pitch, kdir)];
         const uint32_t is = s & 0xFFFFFFu, it = t & 0xFFFFFFu;
         if (is > (uint32_t)ncells || it > (uint32_t)ncells) {
           atomicOr(err, kErrBadId);
@@ -442,9 +468,16 @@ __global__ void __launch_bounds__(32 * (CLU ? cluster_warps(CY) : kMaxSweepWarps
           }
           if (ok) {
             accepted = true;
-            if constexpr (CLU)
-              strip[(y - row0) * nx + x] = s;  // targets lie in this block's rows
-            else
+            if constexpr (CLU) {
+              // targets lie in this block's rows; the padding copies too
+              uint32_t* row = strip + (y - row0 + 1) * sp + 4;
+              row[x] = s;
+              if (x < 4) row[x + nx] = s;
+              if (x >= nx - 4) row[x - nx] = s;
+              // an edge row also into its copy in the neighbour's halo
+              if (y == row0) halo_store(s_halo[0], x, s);
+              if (y == row1 - 1) halo_store(s_halo[1], x, s);
+            } else
               L[(long long)y * nx + x] = s;
             const int crd[2] = {x, y};
             const int dim[2] = {nx, ny};
@@ -577,10 +610,14 @@ __global__ void __launch_bounds__(32 * (CLU ? cluster_warps(CY) : kMaxSweepWarps
   if constexpr (CLU) {
     // this block's rows back to the lattice in global memory; no block
     // leaves while another may still read its shared memory
-    const int nvec = row0 < row1 ? (row1 - row0) * (nx / 4) : 0;
+    const int nvr = nx / 4, nvec = nown * nvr;
     uint4* dst = reinterpret_cast<uint4*>(L + (long long)row0 * nx);
+    const uint4* src = reinterpret_cast<const uint4*>(strip);
     __syncthreads();
-    for (int v = tid; v < nvec; v += blockDim.x) dst[v] = reinterpret_cast<const uint4*>(strip)[v];
+    for (int v = tid; v < nvec; v += blockDim.x) {
+      const int r = v / nvr, k = v - r * nvr;
+      dst[v] = src[(r + 1) * (sp / 4) + 1 + k];
+    }
     cluster.sync();
   }
 }
@@ -675,10 +712,10 @@ const void* cluster_fn(bool perim, int v) {
 }
 size_t warp_area(int v) {
   switch (v) {
-    case 0: return sizeof(Warp2Smem<2>);
-    case 1: return sizeof(Warp2Smem<4>);
-    case 2: return sizeof(Warp2Smem<8>);
-    default: return sizeof(Warp2Smem<1>);
+    case 0: return sizeof(WarpCluSmem<2>);
+    case 1: return sizeof(WarpCluSmem<4>);
+    case 2: return sizeof(WarpCluSmem<8>);
+    default: return sizeof(WarpCluSmem<1>);
   }
 }
 
@@ -690,7 +727,8 @@ long long cluster_list_cap(int nx, int H) {
 }
 
 size_t cluster_smem(int nx, int H, int v) {
-  const size_t strip = (size_t)(((long long)H * nx + 31) & ~31LL) * 4;
+  // own rows and two halo rows, each padded by 4 columns on both sides
+  const size_t strip = (size_t)(((long long)(H + 2) * (nx + 8) + 31) & ~31LL) * 4;
   return strip + warp_area(v) * (size_t)kClusterW[v] + 2 * 4 * (size_t)cluster_list_cap(nx, H);
 }
 
