@@ -124,10 +124,11 @@ __device__ __forceinline__ int nb_off(int pitch, int k) {
 
 // Warps per block of the cluster sweep by tile height: one one-row tile per
 // warp covers the 1,024 targets a block of a 16-block cluster has per phase
-// on 256^2; taller tiles need fewer warps, which then get more registers.
-// One more warp replays the dirty list while the others work their tiles.
+// on 256^2 (32 x 2 tiles: 16 warps, 32 x 4: 8); taller tiles need fewer
+// warps, which then get more registers.  One more warp replays the dirty
+// list while the others work their tiles.
 __host__ __device__ constexpr int cluster_warps(int cy) {
-  return (cy == 1 ? 31 : (cy == 8 ? 8 : 16)) + 1;  // + the replay warp (1,024 threads at most)
+  return (cy == 1 ? 31 : (cy >= 4 ? 8 : 16)) + 1;  // + the replay warp (1,024 threads at most)
 }
 
 template <bool PERIM, int CY, bool CLU = false>
@@ -326,40 +327,71 @@ __global__ void __launch_bounds__(32 * (CLU ? cluster_warps(CY) : kMaxSweepWarps
     __syncwarp();
 
     // ---- pass 2: random draw and source pick -------------------------
+    // Two batches per round where there are two, their draws computed side
+    // by side (two independent Philox chains per lane); entries keep their
+    // order, so the result is that of one batch at a time.
     int nbq = 0;
-    for (int base = 0; base < na; base += 32) {
+    auto counters = [&](int j, uint32_t (&c)[4]) {
+      const int q = ws.qa[j];
+      const int qx = q & 31, qy = q >> 5;
+      const int x = 2 * (i0 + qx) + PAR;
+      const int y = class_coord(ny, cy, j0 + qy);
+      const long long site = (long long)y * nx + x;
+      c[0] = (uint32_t)site;
+      c[1] = (uint32_t)phase;
+      c[2] = a.stream0;
+      c[3] = (uint32_t)(phase >> 32);
+      return q;
+    };
+    auto pick = [&](int q, const uint32_t (&c)[4], uint2& entry) {
+      const int qx = q & 31, qy = q >> 5;
+      const int kdir = (int)__umulhi(c[0], 8u);
+      const int ci = center_idx<PAR>(pitch, qx, qy);
+      const uint32_t tv = tb[ci], sv = tb[ci + nb_off(pitch, kdir)];
+      bool keep = sv != tv;
+      uint32_t medium = 0;  // 1: the source is replaced by the medium
+      if (fixed_mask && keep) {
+        // a target of a fixed type never changes; a source of a fixed type
+        // proposes the medium instead (src/kernels2d.cu:280-290)
+        if ((fixed_mask >> ((tv >> 24) & (kMaxTypes - 1))) & 1u) {
+          keep = false;
+        } else if ((fixed_mask >> ((sv >> 24) & (kMaxTypes - 1))) & 1u) {
+          medium = 1;
+          keep = tv != 0u;
+        }
+      }
+      entry = make_uint2((uint32_t)q | ((uint32_t)kdir << 16) | (medium << 24), c[1]);
+      return keep;
+    };
+    auto push = [&](bool keep, const uint2& entry) {
+      const unsigned ball = __ballot_sync(kFull, keep);
+      if (keep) ws.qb[nbq + __popc(ball & lanemask_lt())] = entry;
+      nbq += __popc(ball);
+    };
+    int base = 0;
+    for (; base + 32 < na; base += 64) {  // two batches, the second maybe partial
+      const int ja = base + lane, jb = min(base + 32 + lane, na - 1);
+      uint32_t ca[4], cb[4];
+      const int qa_ = counters(ja, ca), qb_ = counters(jb, cb);
+      philox4x32_10(ca[0], ca[1], ca[2], ca[3], k0, k1);
+      philox4x32_10(cb[0], cb[1], cb[2], cb[3], k0, k1);
+      uint2 ea, eb;
+      const bool keep_a = pick(qa_, ca, ea);
+      const bool keep_b = pick(qb_, cb, eb) && base + 32 + lane < na;
+      push(keep_a, ea);
+      push(keep_b, eb);
+    }
+    if (base < na) {  // one last batch of at most 32
       const int j = base + lane;
       bool keep = false;
       uint2 entry = make_uint2(0u, 0u);
       if (j < na) {
-        const int q = ws.qa[j];
-        const int qx = q & 31, qy = q >> 5;
-        const int x = 2 * (i0 + qx) + PAR;
-        const int y = class_coord(ny, cy, j0 + qy);
-        const long long site = (long long)y * nx + x;
-        uint32_t c0 = (uint32_t)site, c1 = (uint32_t)phase, c2 = a.stream0,
-                 c3 = (uint32_t)(phase >> 32);
-        philox4x32_10(c0, c1, c2, c3, k0, k1);
-        const int kdir = (int)__umulhi(c0, 8u);
-        const int c = center_idx<PAR>(pitch, qx, qy);
-        const uint32_t tv = tb[c], sv = tb[c + nb_off(pitch, kdir)];
-        keep = sv != tv;
-        uint32_t medium = 0;  // 1: the source is replaced by the medium
-        if (fixed_mask && keep) {
-          // a target of a fixed type never changes; a source of a fixed type
-          // proposes the medium instead (src/kernels2d.cu:280-290)
-          if ((fixed_mask >> ((tv >> 24) & (kMaxTypes - 1))) & 1u) {
-            keep = false;
-          } else if ((fixed_mask >> ((sv >> 24) & (kMaxTypes - 1))) & 1u) {
-            medium = 1;
-            keep = tv != 0u;
-          }
-        }
-        entry = make_uint2((uint32_t)q | ((uint32_t)kdir << 16) | (medium << 24), c1);
+        uint32_t c[4];
+        const int q = counters(j, c);
+        philox4x32_10(c[0], c[1], c[2], c[3], k0, k1);
+        keep = pick(q, c, entry);
       }
-      const unsigned ball = __ballot_sync(kFull, keep);
-      if (keep) ws.qb[nbq + __popc(ball & lanemask_lt())] = entry;
-      nbq += __popc(ball);
+      push(keep, entry);
     }
     __syncwarp();
 
