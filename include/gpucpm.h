@@ -524,10 +524,12 @@ struct cpm_static_params {
  * CPM_STATIC_MAX_CELLS; larger requests fail with CPM_ERR_INVALID before any
  * GPU work.  Every shape within those limits fits the array's dirty-list
  * space, narrow ones (nx far below 64) included.  A non-finite temperature,
- * lambda, adhesion or stickiness fails with CPM_ERR_INVALID.  The first call
- * on a device looks the array's address up on that device (make that call
- * before capturing a CUDA graph on it) and keeps it for the life of the
- * process; after cudaDeviceReset on that device the kept address is stale,
+ * lambda, adhesion or stickiness fails with CPM_ERR_INVALID.  The call is
+ * synchronous and cannot be captured into a CUDA graph: do not call it while
+ * its stream, or a stream in global capture mode, is being captured.  The
+ * first call on a device looks the array's address up on that device (make
+ * that call before any graph capture on the device) and keeps it for the
+ * life of the process; after cudaDeviceReset on that device the kept address is stale,
  * so do not call this entry point on a device the process has reset.  Every
  * call shares the one array: calls must not overlap on the GPU (two host
  * threads calling at once on different streams would race).  The call works
