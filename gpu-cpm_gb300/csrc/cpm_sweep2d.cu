@@ -310,9 +310,10 @@ __global__ void __launch_bounds__(32 * (CLU ? cluster_warps(CY) : kMaxSweepWarps
     }
 
     // ---- pass 1: boundary test ---------------------------------------
-    int na = 0;
-#pragma unroll
-    for (int qy = 0; qy < CY; ++qy) {
+    // (cluster mode: every row's test first, its loads free to overlap,
+    // then the list; the grid sweeps, with more warps to hide latency, are
+    // faster row by row)
+    auto boundary = [&](int qy) {
       bool bnd = false;
       if (lane < cntx && qy < cnty) {
         uint32_t nb[8];
@@ -320,6 +321,17 @@ __global__ void __launch_bounds__(32 * (CLU ? cluster_warps(CY) : kMaxSweepWarps
 #pragma unroll
         for (int k = 0; k < 8; ++k) bnd |= nb[k] != t;
       }
+      return bnd;
+    };
+    unsigned bmask = 0;  // (cluster mode) bit qy: the lane's target of row qy is a boundary site
+    if constexpr (CLU) {
+#pragma unroll
+      for (int qy = 0; qy < CY; ++qy) bmask |= (unsigned)boundary(qy) << qy;
+    }
+    int na = 0;
+#pragma unroll
+    for (int qy = 0; qy < CY; ++qy) {
+      const bool bnd = CLU ? ((bmask >> qy) & 1u) != 0 : boundary(qy);
       const unsigned ball = __ballot_sync(kFull, bnd);
       if (bnd) ws.qa[na + __popc(ball & lanemask_lt())] = (uint16_t)(qy * 32 + lane);
       na += __popc(ball);
