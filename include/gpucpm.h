@@ -333,10 +333,11 @@ int cpm_sweep_config(const cpm_handle* h, int* variant, int* tile_x,
  *                    periodic seam from vector loads
  *   CPM_FILL_CLUSTER (small 2D lattices) one thread-block cluster of 16 (or 8)
  *                    blocks holds the lattice in its shared memory, one
- *                    strip of rows per block, for a whole run; one-row
- *                    tiles are staged from the strips and the phases end at
- *                    a barrier inside the cluster.  cpm_autotune tries it
- *                    wherever it fits and keeps it when it is faster.
+ *                    strip of rows per block with copies of its neighbours'
+ *                    edge rows, for a whole run; tiles are read in place
+ *                    and the phases end at a barrier inside the cluster.
+ *                    cpm_autotune tries it wherever it fits and keeps it
+ *                    when it is faster.
  * Row-major tiles need a single lattice with nx a multiple of 4 and
  * nx >= 72 (in 2D ny >= 66, in 3D ny >= 18 and nz >= 18); such lattices start
  * in CPM_FILL_TMA (CPM_FILL_VECTOR where the tensor maps cannot be encoded),

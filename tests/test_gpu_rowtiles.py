@@ -5,7 +5,8 @@ against the oracle, bit for bit, under each way of staging tiles:
   vector  row-major tiles from 16-byte vector loads
   tma     row-major tiles, interior tiles copied by cp.async.bulk.tensor
   cluster (2D) the lattice held in the shared memory of one thread-block
-          cluster, one-row tiles staged from its strips
+          cluster, a strip of rows per block with copies of its
+          neighbours' edge rows, tiles read in place
 
 Shapes cover partial tiles in x (nx = 76: 38 target columns, a full and a
 6-wide tile), odd heights and depths (one-row or one-plane slots of the last
