@@ -36,10 +36,12 @@
 // never races with a store it depends on (a copied box also holds columns of
 // neighbouring tiles' targets, which the tile never reads).
 //
-// Work split.  Each block sweeps one contiguous band of a slot's tiles, the
-// same band in every phase; its warps claim the band's tiles one at a time
-// from a shared counter, so that the phase ends within about one tile on
-// every warp although tiles differ in how many attempts they evaluate.
+// Work split.  Block b of G sweeps tiles b, b + G, b + 2G, ... of a slot,
+// the same tiles in every phase, so that every block's share samples the
+// whole lattice and blocks finish a phase close together; its warps claim
+// those tiles one at a time from a shared counter, so that the phase ends
+// within about one tile on every warp although tiles differ in how many
+// attempts they evaluate.
 //
 // Cluster mode (CLU).  A small lattice is swept by one thread-block cluster
 // of G blocks instead of the whole grid.  Block r keeps lattice rows
@@ -593,9 +595,9 @@ __global__ void __launch_bounds__(32 * (CLU ? cluster_warps(CY) : kMaxSweepWarps
       const int tnx = ((nx >> 1) + 31) / 32;
       const int tny = (class_count(ny, cy) + CY - 1) / CY;
       const int ntiles = tnx * tny;
-      // each block sweeps one contiguous band of tile rows, the same in
-      // every phase; its warps take the band's tiles in turn.  In cluster
-      // mode the band is the tile rows whose targets lie in the block's rows.
+      // each block sweeps every gridDim.x-th tile (tb1 - tb0 of them), the
+      // same in every phase; its warps take them in turn.  In cluster mode
+      // a block sweeps the band of tile rows whose targets lie in its rows.
       const int ncy = class_count(ny, cy);
       int tb0, tb1, jlo = 0, jhi = 0;
       if constexpr (CLU) {
@@ -614,13 +616,13 @@ __global__ void __launch_bounds__(32 * (CLU ? cluster_warps(CY) : kMaxSweepWarps
       }
       // copies of this phase must see every SM's stores of the last one
       if (!CLU && lane == 0 && use_tma) asm volatile("fence.proxy.async.global;" ::: "memory");
-      // warp w starts with the band's tile w, then claims the next unclaimed
+      // warp w starts with the block's tile w, then claims the next unclaimed
       // one; counter step % 2 serves this phase, the other one (last used
       // before the previous barrier) is cleared for the next phase
       unsigned* ctr = &s_next[step & 1];
       if (tid == 0) s_next[(step + 1) & 1] = 0u;
       for (int k = warp; warp < tile_warps && k < tb1 - tb0;) {
-        const int task = tb0 + k;
+        const int task = CLU ? tb0 + k : (int)blockIdx.x + k * (int)gridDim.x;
         const int ty = task / tnx, tx = task - ty * tnx;
         const int j0 = CLU ? jlo + ty * CY : ty * CY, jend = CLU ? jhi : ncy;
         if (cx)

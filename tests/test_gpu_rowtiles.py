@@ -60,6 +60,7 @@ def _terms(w, seed):
     ((130, 144), 120, 1, True, 10),    # 32 x 8 tiles
     ((132, 200), 150, 2, False, 10),   # 32 x 16 tiles
     ((96, 72), 50, 3, True, 20),       # one-row tiles, nx = one staged row
+    ((66, 72), 40, 0, False, 12),      # cluster: a last block of one row (both its edges)
     ((18, 20, 72), 60, 0, True, 6),    # 3D, 32 x 2 x 2 tiles, every term
     ((19, 21, 76), 60, 1, False, 5),   # 3D, odd ny and nz, partial x tiles
     ((20, 18, 80), 50, 2, True, 4),    # 3D, 32 x 4 x 4 tiles
