@@ -389,16 +389,19 @@ __global__ void __launch_bounds__(32 * kMaxSweepWarps3d, 1)
       const int tny = (class_count(ny, cy) + CY - 1) / CY;
       const int tnz = (class_count(nz, cz) + CZ - 1) / CZ;
       const int ntiles = tnx * tny * tnz;
-      // each block sweeps one contiguous band of the slot's tiles, the same
-      // in every phase; its warps claim the band's tiles from a counter
-      const int per_b = ntiles / (int)gridDim.x, extra = ntiles % (int)gridDim.x;
-      const int tb0 = (int)blockIdx.x * per_b + min((int)blockIdx.x, extra);
-      const int tb1 = tb0 + per_b + ((int)blockIdx.x < extra ? 1 : 0);
+      // the slot's tiles in chunks of half a row of tiles along x (a whole
+      // row where it has an odd number of tiles), dealt to the blocks in
+      // turn, the same in every phase: every block's share samples the
+      // lattice and holds as many boxes across the periodic seam in x (the
+      // first and last tile of a row, loaded without the copy engine) as
+      // the others.  Its warps claim the block's tiles from a counter.
+      const int CH = (tnx & 1) ? tnx : tnx / 2;
       if (lane == 0 && use_tma) asm volatile("fence.proxy.async.global;" ::: "memory");
       unsigned* ctr = &s_next[step & 1];
       if (tid == 0) s_next[(step + 1) & 1] = 0u;
-      for (int k = warp; k < tb1 - tb0;) {
-        const int task = tb0 + k;
+      for (int k = warp;;) {
+        const int task = ((int)blockIdx.x + (k / CH) * (int)gridDim.x) * CH + k % CH;
+        if (task >= ntiles) break;
         const int tx = task % tnx, rest = task / tnx;
         const int ty = rest % tny, tz = rest / tny;
         if (cx)
