@@ -36,9 +36,11 @@
 // never races with a store it depends on (a copied box also holds columns of
 // neighbouring tiles' targets, which the tile never reads).
 //
-// Work split.  Block b of G sweeps tiles b, b + G, b + 2G, ... of a slot,
-// the same tiles in every phase, so that every block's share samples the
-// whole lattice and blocks finish a phase close together; its warps claim
+// Work split.  Block b of G sweeps tiles b, b + G, b + 2G, ... of a slot
+// (row-major, each row of tiles rotated by its row index), the same tiles in
+// every phase, so that every block's share samples the whole lattice, holds
+// its share of the tiles across the periodic seam in x (loaded without the
+// copy engine), and blocks finish a phase close together; its warps claim
 // those tiles one at a time from a shared counter, so that the phase ends
 // within about one tile on every warp although tiles differ in how many
 // attempts they evaluate.
@@ -623,7 +625,12 @@ __global__ void __launch_bounds__(32 * (CLU ? cluster_warps(CY) : kMaxSweepWarps
       if (tid == 0) s_next[(step + 1) & 1] = 0u;
       for (int k = warp; warp < tile_warps && k < tb1 - tb0;) {
         const int task = CLU ? tb0 + k : (int)blockIdx.x + k * (int)gridDim.x;
-        const int ty = task / tnx, tx = task - ty * tnx;
+        const int ty = task / tnx;
+        // (grid mode) tile row ty is taken rotated by ty tiles, so that a
+        // block's tiles, every gridDim.x-th, fall in every column of tiles
+        // and each block gets its share of the seam columns
+        int tx = task - ty * tnx;
+        if (!CLU) tx = (tx + ty) % tnx;
         const int j0 = CLU ? jlo + ty * CY : ty * CY, jend = CLU ? jhi : ncy;
         if (cx)
           run_tile(std::integral_constant<int, 1>{}, pt, tx, j0, jend, cy, phase);
