@@ -440,8 +440,8 @@ int build_engine(int n, int ndim, const int* nx, const int* ny, const int* nz,
     if (n == 1 && (ndim == 2 ? row_tiles_fit(nx[0], ny[0])
                              : box_tiles_fit(nx[0], ny[0], nz[0]))) {
       // the row-tile sweeps of the one lattice: tiles of 32 x ry (x rz)
-      // targets, dealt to the blocks one at a time (2D) or in chunks of half
-      // a row of tiles (3D); a block gets at most ceil(chunks / grid) chunks
+      // targets, dealt to the blocks one at a time; a block gets at most
+      // ceil(tiles / grid) of them
       int rows = 0, planes = 3;
       if (ndim == 2)
         rows = row_tile_rows(v);
@@ -451,8 +451,7 @@ int build_engine(int n, int ndim, const int* nx, const int* ny, const int* nz,
       const long long tnx = ((nx[0] / 2) + 31) / 32;
       const long long tiles = tnx * (((ny[0] + 1) / 2 + ry - 1) / ry) *
                               (ndim == 3 ? (((nz[0] + 1) / 2 + rz - 1) / rz) : 1);
-      const long long ch = ndim == 2 ? 1 : ((tnx & 1) ? tnx : tnx / 2);
-      const long long per_block = ((tiles + ch - 1) / ch + c.grid - 1) / c.grid * ch;
+      const long long per_block = (tiles + c.grid - 1) / c.grid;
       c.list_cap = std::max(c.list_cap, 2LL * per_block * 32 * ry * rz);
     }
     dlist_entries = std::max(dlist_entries, c.list_cap * 2 * c.grid);

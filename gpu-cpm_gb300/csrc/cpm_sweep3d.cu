@@ -389,20 +389,21 @@ __global__ void __launch_bounds__(32 * kMaxSweepWarps3d, 1)
       const int tny = (class_count(ny, cy) + CY - 1) / CY;
       const int tnz = (class_count(nz, cz) + CZ - 1) / CZ;
       const int ntiles = tnx * tny * tnz;
-      // the slot's tiles in chunks of half a row of tiles along x (a whole
-      // row where it has an odd number of tiles), dealt to the blocks in
-      // turn, the same in every phase: every block's share samples the
-      // lattice and holds as many boxes across the periodic seam in x (the
-      // first and last tile of a row, loaded without the copy engine) as
-      // the others.  Its warps claim the block's tiles from a counter.
-      const int CH = (tnx & 1) ? tnx : tnx / 2;
+      // block b of G sweeps tiles b, b + G, b + 2G, ... of the slot, the
+      // same in every phase, each row of tiles along x taken rotated by its
+      // row index: every block's share samples the lattice and holds as many
+      // boxes across the periodic seam in x (the first and last tile of a
+      // row, loaded without the copy engine) as the others, whatever the
+      // number of tiles per row.  Its warps claim the block's tiles from a
+      // counter.
       if (lane == 0 && use_tma) asm volatile("fence.proxy.async.global;" ::: "memory");
       unsigned* ctr = &s_next[step & 1];
       if (tid == 0) s_next[(step + 1) & 1] = 0u;
       for (int k = warp;;) {
-        const int task = ((int)blockIdx.x + (k / CH) * (int)gridDim.x) * CH + k % CH;
+        const int task = (int)blockIdx.x + k * (int)gridDim.x;
         if (task >= ntiles) break;
-        const int tx = task % tnx, rest = task / tnx;
+        const int rest = task / tnx;
+        const int tx = (task % tnx + rest) % tnx;
         const int ty = rest % tny, tz = rest / tny;
         if (cx)
           run_tile(std::integral_constant<int, 1>{}, pt, tx, ty, tz, cy, cz, phase);
